@@ -1,0 +1,196 @@
+// Reference-as-oracle driver (test infrastructure only; never shipped).
+//
+// Links the VEDAS reference's own src/*.cu files, compiled unmodified with g++
+// against Thrust's OpenMP backend and the host shims in oracle/refshim/, and
+// runs them on this project's synthetic inputs:
+//
+//   vedas_ref index <graph.bin> <out.bin> [full]
+//       VedasStorage(RdfData&, preload=false, fullIndex) (src/VedasStorage.cu:25-73)
+//       then dumps every index array through the VedasStorage getters.
+//   vedas_ref query <graph.bin> <queries.txt> <out.bin> [first_query] [full]
+//       For each query line: SparqlQuery + QueryExecutor::query, as vdQuery's
+//       REPL does (src/VedasQuery.cu:136-205), with ENABLE_UPDATE_BOUND_AFTER_JOIN
+//       true (src/VedasQuery.cu:37).  Results are appended and flushed per
+//       query so that a reference abort (its asserts are live) loses only the
+//       query that aborted.
+//
+// Graph file: "VGRAPH1\0", u64 n, u32 s[n], u32 p[n], u32 o[n].
+// Query text: SELECT * | ?v.. WHERE { t t t . ... } with constants written as
+// <ID> (subject/predicate/object IDs) or "ID" (literal object IDs).
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "QueryExecutor.h"
+#include "RdfData.h"
+#include "SparqlQuery.h"
+#include "SparqlResult.h"
+#include "VedasStorage.h"
+
+namespace {
+
+bool read_graph(const char* path, TYPEID_HOST_VEC& s, TYPEID_HOST_VEC& p, TYPEID_HOST_VEC& o) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return false;
+  char magic[8];
+  in.read(magic, 8);
+  if (std::memcmp(magic, "VGRAPH1", 7) != 0) return false;
+  uint64_t n = 0;
+  in.read(reinterpret_cast<char*>(&n), 8);
+  s.resize(n);
+  p.resize(n);
+  o.resize(n);
+  in.read(reinterpret_cast<char*>(s.data()), n * 4);
+  in.read(reinterpret_cast<char*>(p.data()), n * 4);
+  in.read(reinterpret_cast<char*>(o.data()), n * 4);
+  return static_cast<bool>(in);
+}
+
+void put_u32(std::ofstream& out, uint32_t v) { out.write(reinterpret_cast<const char*>(&v), 4); }
+void put_u64(std::ofstream& out, uint64_t v) { out.write(reinterpret_cast<const char*>(&v), 8); }
+void put_str(std::ofstream& out, const std::string& s) {
+  put_u32(out, static_cast<uint32_t>(s.size()));
+  out.write(s.data(), static_cast<std::streamsize>(s.size()));
+}
+void put_arr(std::ofstream& out, const std::string& name, const TYPEID_HOST_VEC* v) {
+  put_str(out, name);
+  put_u64(out, v->size());
+  if (!v->empty()) out.write(reinterpret_cast<const char*>(v->data()), v->size() * 4);
+}
+
+// Every constant of a query line, registered in the dictionaries under the
+// exact key TriplePattern's constructor looks up (src/TriplePattern.cu:62-82).
+void register_constants(const std::string& q, DICTTYPE& so, DICTTYPE& p, DICTTYPE& l) {
+  for (size_t i = 0; i < q.size(); ++i) {
+    char c = q[i];
+    if (c != '<' && c != '"') continue;
+    char close = (c == '<') ? '>' : '"';
+    size_t e = q.find(close, i + 1);
+    if (e == std::string::npos) break;
+    std::string body = q.substr(i + 1, e - i - 1);
+    TYPEID id = static_cast<TYPEID>(std::strtoul(body.c_str(), nullptr, 10));
+    std::string key = std::string(1, c) + body + std::string(1, close);
+    if (c == '<') {
+      so[key] = id;
+      p[key] = id;
+    } else {
+      l[key] = id;
+    }
+    i = e;
+  }
+}
+
+int do_index(const char* graph, const char* outp, bool full) {
+  TYPEID_HOST_VEC s, p, o;
+  if (!read_graph(graph, s, p, o)) return 2;
+  RdfData rdf(s, p, o);
+  VedasStorage st(rdf, false, full);
+  std::ofstream out(outp, std::ios::binary);
+  put_arr(out, "p_idx_values", st.getPredicateIndexValues());
+  put_arr(out, "p_idx_offsets", st.getPredicateIndexOffsets());
+  put_arr(out, "ps_s_idx_values", st.getPredicateSubjectIndexValues());
+  put_arr(out, "ps_idx_offsets", st.getPredicateSubjectIndexOffsets());
+  put_arr(out, "po_o_idx_values", st.getPredicateObjectIndexValues());
+  put_arr(out, "po_idx_offsets", st.getPredicateObjectIndexOffsets());
+  put_arr(out, "ps_data", st.getPSdata());
+  put_arr(out, "po_data", st.getPOdata());
+  put_arr(out, "pso_data", st.getPSOdata());
+  put_arr(out, "pos_data", st.getPOSdata());
+  if (full) {
+    put_arr(out, "s_idx_values", st.getSubjectIndexValues());
+    put_arr(out, "s_idx_offsets", st.getSubjectIndexOffsets());
+    put_arr(out, "sp_p_idx_values", st.getSubjectPredicateIndexValues());
+    put_arr(out, "sp_idx_offsets", st.getSubjectPredicateIndexOffsets());
+    put_arr(out, "so_o_idx_values", st.getSubjectObjectIndexValues());
+    put_arr(out, "so_idx_offsets", st.getSubjectObjectIndexOffsets());
+    put_arr(out, "o_idx_values", st.getObjectIndexValues());
+    put_arr(out, "o_idx_offsets", st.getObjectIndexOffsets());
+    put_arr(out, "os_data", st.getOSdata());
+    put_arr(out, "op_p_idx_values", st.getObjectPredicateIndexValues());
+    put_arr(out, "op_idx_offsets", st.getObjectPredicateIndexOffsets());
+    put_arr(out, "spo_data", st.getSPOdata());
+    put_arr(out, "sop_data", st.getSOPdata());
+    put_arr(out, "ops_data", st.getOPSdata());
+    put_arr(out, "osp_data", st.getOSPdata());
+  }
+  put_str(out, "");
+  return out ? 0 : 3;
+}
+
+int do_query(const char* graph, const char* qpath, const char* outp, size_t first, bool full) {
+  TYPEID_HOST_VEC s, p, o;
+  if (!read_graph(graph, s, p, o)) return 2;
+  RdfData rdf(s, p, o);
+  VedasStorage st(rdf, false, full);
+
+  std::vector<std::string> lines;
+  {
+    std::ifstream qin(qpath);
+    std::string line;
+    while (std::getline(qin, line))
+      if (!line.empty()) lines.push_back(line);
+  }
+  std::ofstream out(outp, std::ios::binary | std::ios::app);
+  std::vector<int> gpu_ids{0};
+  ExecutionWorker worker(gpu_ids);
+  mgpu::standard_context_t context(false);
+  QueryExecutor::ENABLE_UPDATE_BOUND_AFTER_JOIN = true;
+  QueryExecutor::ENABLE_FULL_INDEX = full;
+  QueryExecutor::ENABLE_LITERAL_DICT = false;
+  QueryExecutor::ENABLE_BOUND_DICT_AFTER_JOIN = false;
+
+  for (size_t qi = first; qi < lines.size(); ++qi) {
+    DICTTYPE so_map, p_map, l_map;
+    register_constants(lines[qi], so_map, p_map, l_map);
+    QueryExecutor::initTime();
+    SparqlQuery sq(lines[qi].c_str(), so_map, p_map, l_map);
+    SparqlResult sr;
+    QueryExecutor qe(&st, &worker, &context);
+    qe.query(sq, sr);
+
+    std::vector<std::string> headers = sr.getHeaderVariables();
+    std::vector<std::vector<TYPEID>> cols = sr.get();
+    put_u32(out, static_cast<uint32_t>(qi));
+    put_u32(out, headers.empty() ? 1u : 0u);
+    put_u32(out, static_cast<uint32_t>(headers.size()));
+    uint64_t nrows = cols.empty() ? 0 : cols[0].size();
+    put_u64(out, nrows);
+    for (size_t c = 0; c < headers.size(); ++c) {
+      put_str(out, headers[c]);
+      out.write(reinterpret_cast<const char*>(cols[c].data()), nrows * 4);
+    }
+    // execution log: (op, p1, p2, p3, text) per job, src/vedas.h:87-103
+    put_u32(out, static_cast<uint32_t>(QueryExecutor::exe_log.size()));
+    for (const ExecuteLogRecord& r : QueryExecutor::exe_log) {
+      put_u32(out, static_cast<uint32_t>(r.op));
+      put_u64(out, r.param1);
+      put_u64(out, r.param2);
+      put_u64(out, r.param3);
+      put_str(out, r.paramstr);
+    }
+    out.flush();
+  }
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc >= 4 && std::string(argv[1]) == "index") {
+    bool full = argc >= 5 && std::string(argv[4]) == "full";
+    return do_index(argv[2], argv[3], full);
+  }
+  if (argc >= 5 && std::string(argv[1]) == "query") {
+    size_t first = argc >= 6 ? std::strtoull(argv[5], nullptr, 10) : 0;
+    bool full = argc >= 7 && std::string(argv[6]) == "full";
+    return do_query(argv[2], argv[3], argv[4], first, full);
+  }
+  std::fprintf(stderr, "usage: vedas_ref index|query ...\n");
+  return 1;
+}

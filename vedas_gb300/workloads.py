@@ -1,0 +1,142 @@
+"""Seeded synthetic RDF graphs and query workloads for VEDAS.
+
+The reference's WatDiv/LUBM suites are not available, so seeded synthetic
+graphs with the stated shapes stand in for them.  ID spaces follow the
+reference's loader (src/loader.cu:15, src/vedas.h:31):
+
+* entities (subjects and entity objects) use IDs 1..E,
+* predicates use IDs 1..P where ID k is the predicate of frequency rank k,
+* literals use IDs LITERAL_START_ID + k (LITERAL_START_ID = 5e7).
+
+Duplicate triples are removed (the graph is an RDF set).  Every generator
+uses numpy's PCG64 with an explicit seed, so a configuration always yields
+the same bytes.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+import struct
+
+import numpy as np
+
+LITERAL_START_ID = 50_000_000  # src/vedas.h:31 (5E7)
+
+GRAPH_MAGIC = b"VGRAPH1\0"
+
+
+@dataclasses.dataclass
+class Graph:
+    s: np.ndarray  # uint32 subjects
+    p: np.ndarray  # uint32 predicates
+    o: np.ndarray  # uint32 objects
+    name: str = ""
+
+    @property
+    def n(self) -> int:
+        return int(self.s.shape[0])
+
+    def save(self, path: str) -> None:
+        with open(path, "wb") as f:
+            f.write(GRAPH_MAGIC)
+            f.write(struct.pack("<Q", self.n))
+            for a in (self.s, self.p, self.o):
+                f.write(np.ascontiguousarray(a, dtype=np.uint32).tobytes())
+
+    @staticmethod
+    def load(path: str) -> "Graph":
+        with open(path, "rb") as f:
+            if f.read(8) != GRAPH_MAGIC:
+                raise ValueError(f"{path}: not a graph file")
+            (n,) = struct.unpack("<Q", f.read(8))
+            arr = np.frombuffer(f.read(12 * n), dtype=np.uint32)
+        return Graph(arr[:n].copy(), arr[n:2 * n].copy(), arr[2 * n:].copy(),
+                     os.path.basename(path))
+
+
+def _zipf_probs(k: int, s: float) -> np.ndarray:
+    w = 1.0 / np.arange(1, k + 1, dtype=np.float64) ** s
+    return w / w.sum()
+
+
+def _dedup(s, p, o, n_target):
+    """Remove duplicate triples keeping first occurrences, then cut to n_target."""
+    key = (p.astype(np.uint64) << np.uint64(58)) ^ (s.astype(np.uint64) << np.uint64(29)) \
+        ^ o.astype(np.uint64)
+    # key is injective for s < 2^29, o < 2^29, p < 2^6; fall back to a
+    # structured unique otherwise.
+    if s.max(initial=0) < (1 << 29) and o.max(initial=0) < (1 << 29) and p.max(initial=0) < 64:
+        _, first = np.unique(key, return_index=True)
+    else:
+        rec = np.rec.fromarrays([s, p, o])
+        _, first = np.unique(rec, return_index=True)
+    first.sort()
+    first = first[:n_target]
+    return s[first], p[first], o[first]
+
+
+def graph_small_star(n: int = 1_000_000, n_subjects: int = 50_000, n_predicates: int = 32,
+                     zipf_s: float = 1.1, literal_range: int = 200_000, seed: int = 0) -> Graph:
+    """The 1M-triple graph of the plain star workload (and scaled-down copies).
+
+    Subjects uniform over [1, n_subjects]; predicates Zipf(zipf_s) over
+    n_predicates ranks; objects 70% uniform entities [1, n_subjects] and 30%
+    uniform literals [LITERAL_START_ID, LITERAL_START_ID + literal_range).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m = int(n * 1.02) + 1024
+    s = rng.integers(1, n_subjects + 1, size=m, dtype=np.uint32)
+    p = (rng.choice(n_predicates, size=m, p=_zipf_probs(n_predicates, zipf_s)) + 1).astype(np.uint32)
+    is_lit = rng.random(m) < 0.30
+    ent = rng.integers(1, n_subjects + 1, size=m, dtype=np.uint32)
+    lit = rng.integers(LITERAL_START_ID, LITERAL_START_ID + literal_range, size=m, dtype=np.uint32)
+    o = np.where(is_lit, lit, ent).astype(np.uint32)
+    s, p, o = _dedup(s, p, o, n)
+    return Graph(s, p, o, f"star_n{n}")
+
+
+def graph_chain(n: int = 100_000_000, n_entities: int = 2_000_000, n_predicates: int = 86,
+                zipf_s: float = 1.0, mean_degree: float = 3.0, literal_frac: float = 0.30,
+                seed: int = 0) -> Graph:
+    """The 100M-triple graph of the linear path / batching workloads.
+
+    (subject, predicate) pairs are drawn with subjects uniform over
+    [1, n_entities] and predicates Zipf(zipf_s); each pair gets a
+    Geometric(1/mean_degree) out-degree, and pairs are taken until n triples
+    exist.  Objects are uniform entities (1 - literal_frac) or uniform
+    literals in [LITERAL_START_ID, LITERAL_START_ID + n_entities // 10).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pairs = int(n / mean_degree * 1.05) + 1024
+    ps = rng.integers(1, n_entities + 1, size=pairs, dtype=np.uint32)
+    pp = (rng.choice(n_predicates, size=pairs, p=_zipf_probs(n_predicates, zipf_s)) + 1).astype(np.uint32)
+    deg = rng.geometric(1.0 / mean_degree, size=pairs).astype(np.int64)
+    csum = np.cumsum(deg)
+    take = int(np.searchsorted(csum, int(n * 1.01) + 1024)) + 1
+    ps, pp, deg = ps[:take], pp[:take], deg[:take]
+    s = np.repeat(ps, deg)
+    p = np.repeat(pp, deg)
+    m = s.shape[0]
+    is_lit = rng.random(m) < literal_frac
+    ent = rng.integers(1, n_entities + 1, size=m, dtype=np.uint32)
+    lit = rng.integers(LITERAL_START_ID, LITERAL_START_ID + max(1, n_entities // 10), size=m,
+                       dtype=np.uint32)
+    o = np.where(is_lit, lit, ent).astype(np.uint32)
+    s, p, o = _dedup(s, p, o, n)
+    return Graph(s, p, o, f"chain_n{n}")
+
+
+def star_query(pa: int = 3, pb: int = 7) -> str:
+    """Two-pattern subject-subject star: (?x pa ?a . ?x pb ?b), SELECT *."""
+    return f"SELECT * WHERE {{ ?x <{pa}> ?a . ?x <{pb}> ?b . }}"
+
+
+def chain_query(g: Graph, preds=(1, 2, 5, 9), seed: int = 0) -> str:
+    """Four-pattern chain (?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 c), where c is
+    a sampled existing object of the last predicate."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    objs = g.o[g.p == preds[-1]]
+    c = int(objs[rng.integers(0, objs.shape[0])])
+    a, b, cc, d = preds
+    return (f"SELECT * WHERE {{ ?a <{a}> ?b . ?b <{b}> ?c . ?c <{cc}> ?d . "
+            f"?d <{d}> <{c}> . }}")
