@@ -1,0 +1,182 @@
+/* VEDAS GB300 query-execution core: C-ABI.
+ *
+ * Every entry point returns a vg_status and never throws.  Pointers are plain
+ * host or device pointers as documented per call; sizes are element counts.
+ * A vg_ctx owns one CUDA device, one stream and one HBM arena; calls on the
+ * same context must not overlap (one host thread per context), matching the
+ * reference's one-host-thread-per-GPU execution.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the reference project).
+ */
+#ifndef VEDAS_GB300_H
+#define VEDAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum vg_status {
+  VG_OK = 0,
+  VG_ERR_INVALID = 1,      /* bad argument */
+  VG_ERR_OOM = 2,          /* arena or host allocation failed */
+  VG_ERR_CUDA = 3,         /* CUDA runtime error */
+  VG_ERR_TIMEOUT = 4,      /* a bounded device wait expired */
+  VG_ERR_UNSUPPORTED = 5,  /* input outside what this core implements */
+  VG_ERR_PARSE = 6,        /* query text not understood */
+  VG_ERR_OVERFLOW = 7,     /* an output exceeded its reservation or a size limit */
+  VG_ERR_REJECTED = 8      /* serving: admission refused (memory budget) */
+} vg_status;
+
+/* Human-readable text of a status, and of the last error on this thread. */
+const char* vg_status_string(vg_status s);
+const char* vg_last_error(void);
+
+/* ---- context ----------------------------------------------------------- */
+typedef struct vg_ctx vg_ctx;
+
+/* Creates a context on `device` with an HBM arena of `arena_bytes`
+ * (0 = 90% of the device's free memory).  Replaces the per-column
+ * thrust::device_vector allocations of FullRelationIR
+ * (src/FullRelationIR.cu:19-31) with one up-front slab. */
+vg_status vg_ctx_create(int device, size_t arena_bytes, vg_ctx** out);
+vg_status vg_ctx_destroy(vg_ctx* ctx);
+/* Arena accounting: bytes in use, peak, capacity. */
+vg_status vg_ctx_memory(vg_ctx* ctx, size_t* used, size_t* peak, size_t* capacity);
+/* Blocks until all work queued on the context's stream is done. */
+vg_status vg_ctx_sync(vg_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work after the core's. */
+void* vg_ctx_stream(vg_ctx* ctx);
+
+/* ---- index build (hot path a) ----------------------------------------- */
+typedef struct vg_index vg_index;
+
+/* Builds the permutation indexes from n dictionary-encoded triples.
+ * Replaces VedasStorage::VedasStorage(RdfData&, bool preload, bool fullIndex)
+ * (src/VedasStorage.cu:25-73; createIndex1Level :270-289, createIndex
+ * :306-358).  s, p, o are HOST pointers when inputs_on_device == 0, device
+ * pointers otherwise.  The index stays resident in HBM; host mirrors of the
+ * arrays are made on first request (vg_index_array with a host pointer). */
+vg_status vg_index_build(vg_ctx* ctx, const uint32_t* s, const uint32_t* p, const uint32_t* o,
+                         uint64_t n, int full_index, int inputs_on_device, vg_index** out);
+vg_status vg_index_free(vg_index* ix);
+/* One array of the reference layout, by the VedasStorage member name:
+ * p_idx_values, p_idx_offsets, ps_s_idx_values, ps_idx_offsets,
+ * po_o_idx_values, po_idx_offsets, ps_data, po_data, pso_data, pos_data and,
+ * with the full index, s_idx_values, s_idx_offsets, sp_p_idx_values,
+ * sp_idx_offsets, so_o_idx_values, so_idx_offsets, o_idx_values,
+ * o_idx_offsets, os_data, op_p_idx_values, op_idx_offsets, spo_data,
+ * sop_data, ops_data, osp_data.  Replaces the VedasStorage getters
+ * (src/VedasStorage.h:14-59).  `dev` receives the HBM copy; `host`, if
+ * non-null, receives a host mirror (copied on first use). */
+vg_status vg_index_array(vg_index* ix, const char* name, const uint32_t** dev,
+                         const uint32_t** host, uint64_t* len);
+/* Binary .vds file in the reference's layout: VedasStorage::write / open
+ * (src/VedasStorage.cu:459-516). */
+vg_status vg_index_write(vg_index* ix, const char* path);
+vg_status vg_index_open(vg_ctx* ctx, const char* path, int full_index, vg_index** out);
+
+/* ---- relations (FullRelationIR) ---------------------------------------- */
+#define VG_MAX_COLS 9 /* FullRelationIR::sort supports up to 9 columns (src/FullRelationIR.cu:218-335) */
+
+/* A relation of `ncols` uint32 device columns with `nrows` rows, column-major
+ * (FullRelationIR, src/FullRelationIR.h:10-47).  Column memory comes from the
+ * context arena. */
+typedef struct vg_ir {
+  uint32_t ncols;
+  uint64_t nrows;
+  uint32_t* cols[VG_MAX_COLS];
+} vg_ir;
+
+vg_status vg_ir_alloc(vg_ctx* ctx, uint32_t ncols, uint64_t nrows, vg_ir* out);
+vg_status vg_ir_free(vg_ctx* ctx, vg_ir* ir);
+/* Host <-> device column copies (FullRelationIR::setRelation,
+ * src/FullRelationIR.cu:578-592, and the D2H of SparqlResult::printResult). */
+vg_status vg_ir_upload(vg_ctx* ctx, vg_ir* ir, uint32_t col, const uint32_t* host, uint64_t n);
+vg_status vg_ir_download(vg_ctx* ctx, const vg_ir* ir, uint32_t col, uint32_t* host);
+
+/* ---- hot-path jobs ------------------------------------------------------ */
+
+/* Select (hot path b): one triple pattern against the partial index.
+ * Replaces SelectQueryJob::startJob (src/SelectQueryJob.cu:86-270).
+ *  kind 1: one variable, subject (?s p o) -> POS index, output [?s]
+ *  kind 2: one variable, object  (s p ?o) -> PSO index, output [?o]
+ *  kind 3: two variables (?s p ?o), level-2 data ps_data / pso_data
+ *          (index PSO) or po_data / pos_data (index POS)
+ * bound_lo/hi: the variables_bound entry of the first output variable
+ * (has_bound = 0 for none); eif[4]: its EmptyIntervalDict entry
+ * (lb1, ub1, lb2, ub2).  second_used = 0 keeps only column 0, adjacent-unique.
+ * On return out_bound_update[0..1] holds the (lo, hi) the reference passes
+ * to updateBoundDict for one-variable selects (flag in out_bound_update[2]). */
+typedef struct vg_select_desc {
+  int kind;          /* 1, 2 or 3 */
+  int index_pos;     /* kind 3: 0 = PSO, 1 = POS */
+  uint32_t pred;     /* predicate id */
+  uint32_t constant; /* kinds 1/2: the bound object / subject */
+  int has_bound;
+  uint32_t bound_lo, bound_hi;
+  uint64_t eif[4];
+  int second_used;
+} vg_select_desc;
+vg_status vg_select(vg_ctx* ctx, vg_index* ix, const vg_select_desc* d, vg_ir* out,
+                    uint32_t out_bound_update[3]);
+
+/* Join (hot path c): sorted inner join of l and r on column 0 of each (both
+ * sorted ascending by column 0).  Output rows are ordered by left row, then
+ * right row: column 0 = key, then l's columns 1.., then r's columns 1..
+ * Replaces the inner join and gather of JoinQueryJob::join
+ * (src/JoinQueryJob.cu:262-380; mgpu::inner_join semantics).
+ * first_last receives out column 0's first and last value when rows > 0. */
+vg_status vg_join(vg_ctx* ctx, const vg_ir* l, const vg_ir* r, vg_ir* out,
+                  uint32_t first_last[2]);
+/* Two-variable join: keys are (column 0, column 1) of each side, both
+ * sorted lexicographically by them; output column 0..1 = keys, then the
+ * rest of l, then the rest of r (src/JoinQueryJob.cu:181-225, :360-377). */
+vg_status vg_join2(vg_ctx* ctx, const vg_ir* l, const vg_ir* r, vg_ir* out);
+
+/* Index swap (hot path d): stable re-sort of the relation by column `col`,
+ * which becomes column 0 (swapColumn(0, col) + sortByFirstColumn;
+ * src/IndexSwapJob.cu:28-63, src/FullRelationIR.cu:594-727).  In place. */
+vg_status vg_swap(vg_ctx* ctx, vg_ir* ir, uint32_t col);
+/* Full lexicographic sort over all columns (FullRelationIR::sort,
+ * src/FullRelationIR.cu:218-336).  In place. */
+vg_status vg_sort_rows(vg_ctx* ctx, vg_ir* ir);
+/* Adjacent duplicate-row removal (FullRelationIR::removeDuplicate,
+ * src/FullRelationIR.cu:338-522).  In place; nrows is updated. */
+vg_status vg_unique(vg_ctx* ctx, vg_ir* ir);
+/* Empty-interval scan of column 0 for relations with 2 < nrows < 100
+ * (src/JoinQueryJob.cu:398-433, src/IndexSwapJob.cu:81-118): out4 receives
+ * the four bounds passed to EmptyIntervalDict::updateBound. */
+vg_status vg_eif_scan(vg_ctx* ctx, const vg_ir* ir, uint64_t out4[4]);
+
+/* ---- whole queries ------------------------------------------------------ */
+typedef struct vg_result vg_result;
+
+/* Runs one SPARQL basic-graph-pattern query through the reference's planning
+ * and job semantics on the device.  Replaces QueryExecutor::query
+ * (src/QueryExecutor.cu:294-431) + QueryPlan::execute (src/QueryPlan.cu:114-257).
+ * Query text: SELECT * | ?v ... WHERE { s p o . ... } with constants written
+ * as <ID> or "ID". */
+vg_status vg_query(vg_ctx* ctx, vg_index* ix, const char* sparql, vg_result** out);
+uint32_t vg_result_ncols(const vg_result* r);
+uint64_t vg_result_nrows(const vg_result* r);
+const char* vg_result_header(const vg_result* r, uint32_t c);
+/* Device pointer of a result column, and a D2H copy of it. */
+const uint32_t* vg_result_column_device(const vg_result* r, uint32_t c);
+vg_status vg_result_download(const vg_result* r, uint32_t c, uint32_t* host);
+/* Execution log (QueryExecutor::exe_log, src/vedas.h:87-103): op 0 JOIN,
+ * 1 UPLOAD, 2 SWAP with its three size parameters. */
+uint32_t vg_result_nlog(const vg_result* r);
+void vg_result_log(const vg_result* r, uint32_t i, uint32_t* op, uint64_t* p1, uint64_t* p2,
+                   uint64_t* p3);
+vg_status vg_result_free(vg_result* r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VEDAS_GB300_H */

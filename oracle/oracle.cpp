@@ -566,7 +566,7 @@ struct Planner {
     return false;
   }
   // QueryGraph::mergeEdge (src/QueryGraph.cu:97-117)
-  void merge(const std::string& end1, const std::string& end2) {
+  void merge(const std::string end1, const std::string end2) {  // by value: the callers pass elements of a list this mutates
     for (auto l : adj[end2]) {
       if (!edge_exists(end1, l.first)) add_edge(end1, l.first, l.second);
       auto& other = adj[l.first];

@@ -1,0 +1,317 @@
+"""VEDAS query-execution core for GB300 (sm_103a), Python bindings.
+
+The product is the in-tree shared library ``libvedas_gb300.so`` (CUDA kernels
+plus the host-side mirror of the reference's query path) behind the C-ABI in
+``include/vedas_gb300.h``.  This module only binds that ABI with ctypes; it
+raises if the library is missing rather than falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvedas_gb300.so")
+MAX_COLS = 9
+
+_lib = None
+
+
+class VgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+STATUS = {0: "ok", 1: "invalid", 2: "oom", 3: "cuda", 4: "timeout", 5: "unsupported",
+          6: "parse", 7: "overflow", 8: "rejected"}
+
+
+class vg_ir(ctypes.Structure):
+    _fields_ = [("ncols", ctypes.c_uint32), ("nrows", ctypes.c_uint64),
+                ("cols", ctypes.c_void_p * MAX_COLS)]
+
+
+class vg_select_desc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("index_pos", ctypes.c_int), ("pred", ctypes.c_uint32),
+                ("constant", ctypes.c_uint32), ("has_bound", ctypes.c_int),
+                ("bound_lo", ctypes.c_uint32), ("bound_hi", ctypes.c_uint32),
+                ("eif", ctypes.c_uint64 * 4), ("second_used", ctypes.c_int)]
+
+
+def lib():
+    """Loads the library (it must have been built by __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+        pu32 = ctypes.POINTER(u32)
+        sigs = {
+            "vg_status_string": (ctypes.c_char_p, [i32]),
+            "vg_last_error": (ctypes.c_char_p, []),
+            "vg_ctx_create": (i32, [i32, ctypes.c_size_t, ctypes.POINTER(vp)]),
+            "vg_ctx_destroy": (i32, [vp]),
+            "vg_ctx_memory": (i32, [vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t),
+                                    ctypes.POINTER(ctypes.c_size_t)]),
+            "vg_ctx_sync": (i32, [vp]),
+            "vg_ctx_stream": (vp, [vp]),
+            "vg_index_build": (i32, [vp, vp, vp, vp, u64, i32, i32, ctypes.POINTER(vp)]),
+            "vg_index_free": (i32, [vp]),
+            "vg_index_array": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(vp), ctypes.POINTER(pu32),
+                                     ctypes.POINTER(u64)]),
+            "vg_index_write": (i32, [vp, ctypes.c_char_p]),
+            "vg_index_open": (i32, [vp, ctypes.c_char_p, i32, ctypes.POINTER(vp)]),
+            "vg_ir_alloc": (i32, [vp, u32, u64, ctypes.POINTER(vg_ir)]),
+            "vg_ir_free": (i32, [vp, ctypes.POINTER(vg_ir)]),
+            "vg_ir_upload": (i32, [vp, ctypes.POINTER(vg_ir), u32, pu32, u64]),
+            "vg_ir_download": (i32, [vp, ctypes.POINTER(vg_ir), u32, pu32]),
+            "vg_select": (i32, [vp, vp, ctypes.POINTER(vg_select_desc), ctypes.POINTER(vg_ir), pu32]),
+            "vg_join": (i32, [vp, ctypes.POINTER(vg_ir), ctypes.POINTER(vg_ir), ctypes.POINTER(vg_ir), pu32]),
+            "vg_join2": (i32, [vp, ctypes.POINTER(vg_ir), ctypes.POINTER(vg_ir), ctypes.POINTER(vg_ir)]),
+            "vg_swap": (i32, [vp, ctypes.POINTER(vg_ir), u32]),
+            "vg_sort_rows": (i32, [vp, ctypes.POINTER(vg_ir)]),
+            "vg_unique": (i32, [vp, ctypes.POINTER(vg_ir)]),
+            "vg_eif_scan": (i32, [vp, ctypes.POINTER(vg_ir), ctypes.POINTER(u64)]),
+            "vg_query": (i32, [vp, vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
+            "vg_result_ncols": (u32, [vp]),
+            "vg_result_nrows": (u64, [vp]),
+            "vg_result_header": (ctypes.c_char_p, [vp, u32]),
+            "vg_result_column_device": (vp, [vp, u32]),
+            "vg_result_download": (i32, [vp, u32, pu32]),
+            "vg_result_nlog": (u32, [vp]),
+            "vg_result_log": (None, [vp, u32, pu32, ctypes.POINTER(u64), ctypes.POINTER(u64),
+                                     ctypes.POINTER(u64)]),
+            "vg_result_free": (i32, [vp]),
+        }
+        for name, (res, args) in sigs.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise VgError(status, f"{STATUS.get(status, status)}: {lib().vg_last_error().decode()}")
+
+
+def _p32(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+class Context:
+    """One device, one stream, one HBM arena (vg_ctx)."""
+
+    def __init__(self, device: int = 0, arena_bytes: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().vg_ctx_create(device, arena_bytes, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vg_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def memory(self):
+        u, p, c = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        check(lib().vg_ctx_memory(self.h, ctypes.byref(u), ctypes.byref(p), ctypes.byref(c)))
+        return u.value, p.value, c.value
+
+    def sync(self):
+        check(lib().vg_ctx_sync(self.h))
+
+    @property
+    def stream(self) -> int:
+        return lib().vg_ctx_stream(self.h) or 0
+
+
+class Index:
+    """Resident permutation indexes (VedasStorage layout)."""
+
+    def __init__(self, ctx: Context, s=None, p=None, o=None, full: bool = False, handle=None,
+                 device_ptrs=None, n: int = 0):
+        self.ctx = ctx
+        if handle is not None:
+            self.h = handle
+            return
+        h = ctypes.c_void_p()
+        if device_ptrs is not None:
+            ds, dp, do = device_ptrs
+            check(lib().vg_index_build(ctx.h, ds, dp, do, n, int(full), 1, ctypes.byref(h)))
+        else:
+            s, p, o = (np.ascontiguousarray(x, dtype=np.uint32) for x in (s, p, o))
+            check(lib().vg_index_build(ctx.h, s.ctypes.data, p.ctypes.data, o.ctypes.data,
+                                       s.shape[0], int(full), 0, ctypes.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def open(ctx: Context, path: str, full: bool = False) -> "Index":
+        h = ctypes.c_void_p()
+        check(lib().vg_index_open(ctx.h, path.encode(), int(full), ctypes.byref(h)))
+        return Index(ctx, handle=h)
+
+    def write(self, path: str) -> None:
+        check(lib().vg_index_write(self.h, path.encode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vg_index_free(self.h)
+            self.h = None
+
+    def array(self, name: str) -> np.ndarray:
+        host = ctypes.POINTER(ctypes.c_uint32)()
+        n = ctypes.c_uint64()
+        check(lib().vg_index_array(self.h, name.encode(), None, ctypes.byref(host), ctypes.byref(n)))
+        if n.value == 0:
+            return np.zeros(0, dtype=np.uint32)
+        return np.ctypeslib.as_array(host, shape=(n.value,)).copy()
+
+    def device_array(self, name: str):
+        d = ctypes.c_void_p()
+        n = ctypes.c_uint64()
+        check(lib().vg_index_array(self.h, name.encode(), ctypes.byref(d), None, ctypes.byref(n)))
+        return d.value, n.value
+
+    def query(self, sparql: str) -> "Result":
+        r = ctypes.c_void_p()
+        check(lib().vg_query(self.ctx.h, self.h, sparql.encode(), ctypes.byref(r)))
+        return Result(r)
+
+
+class Result:
+    OPS = {0: "JOIN", 1: "UPLOAD", 2: "SWAP"}
+
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vg_result_free(self.h)
+            self.h = None
+
+    @property
+    def headers(self):
+        L = lib()
+        return [L.vg_result_header(self.h, c).decode() for c in range(L.vg_result_ncols(self.h))]
+
+    @property
+    def nrows(self) -> int:
+        return int(lib().vg_result_nrows(self.h))
+
+    def columns(self):
+        L = lib()
+        n = self.nrows
+        out = []
+        for c in range(L.vg_result_ncols(self.h)):
+            a = np.zeros(n, dtype=np.uint32)
+            if n:
+                check(L.vg_result_download(self.h, c, _p32(a)))
+            out.append(a)
+        return out
+
+    def log(self):
+        L = lib()
+        recs = []
+        for i in range(L.vg_result_nlog(self.h)):
+            op, p1, p2, p3 = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+            L.vg_result_log(self.h, i, ctypes.byref(op), ctypes.byref(p1), ctypes.byref(p2), ctypes.byref(p3))
+            recs.append((self.OPS[op.value], p1.value, p2.value, p3.value))
+        return recs
+
+
+class Relation:
+    """A device relation (vg_ir) owned by a context."""
+
+    def __init__(self, ctx: Context, ir: vg_ir):
+        self.ctx = ctx
+        self.ir = ir
+
+    @staticmethod
+    def from_host(ctx: Context, cols) -> "Relation":
+        cols = [np.ascontiguousarray(c, dtype=np.uint32) for c in cols]
+        ir = vg_ir()
+        n = cols[0].shape[0] if cols else 0
+        check(lib().vg_ir_alloc(ctx.h, len(cols), n, ctypes.byref(ir)))
+        for i, c in enumerate(cols):
+            check(lib().vg_ir_upload(ctx.h, ctypes.byref(ir), i, _p32(c), n))
+        return Relation(ctx, ir)
+
+    @property
+    def nrows(self) -> int:
+        return int(self.ir.nrows)
+
+    @property
+    def ncols(self) -> int:
+        return int(self.ir.ncols)
+
+    def to_host(self):
+        out = []
+        for c in range(self.ir.ncols):
+            a = np.zeros(self.ir.nrows, dtype=np.uint32)
+            check(lib().vg_ir_download(self.ctx.h, ctypes.byref(self.ir), c, _p32(a)))
+            out.append(a)
+        return out
+
+    def free(self):
+        if self.ir.ncols:
+            check(lib().vg_ir_free(self.ctx.h, ctypes.byref(self.ir)))
+
+
+def select(ctx: Context, ix: Index, kind: int, pred: int, constant: int = 0, index_pos: bool = False,
+           bound=None, eif=(0, 0, 0, 0), second_used: bool = True):
+    d = vg_select_desc()
+    d.kind, d.index_pos, d.pred, d.constant = kind, int(index_pos), pred, constant
+    if bound is not None:
+        d.has_bound, d.bound_lo, d.bound_hi = 1, bound[0], bound[1]
+    for i in range(4):
+        d.eif[i] = eif[i]
+    d.second_used = int(second_used)
+    out = vg_ir()
+    bu = (ctypes.c_uint32 * 3)()
+    check(lib().vg_select(ctx.h, ix.h, ctypes.byref(d), ctypes.byref(out), bu))
+    return Relation(ctx, out), (bu[0], bu[1]) if bu[2] else None
+
+
+def join(ctx: Context, l: Relation, r: Relation):
+    out = vg_ir()
+    fl = (ctypes.c_uint32 * 2)()
+    check(lib().vg_join(ctx.h, ctypes.byref(l.ir), ctypes.byref(r.ir), ctypes.byref(out), fl))
+    return Relation(ctx, out), (fl[0], fl[1])
+
+
+def join2(ctx: Context, l: Relation, r: Relation):
+    out = vg_ir()
+    check(lib().vg_join2(ctx.h, ctypes.byref(l.ir), ctypes.byref(r.ir), ctypes.byref(out)))
+    return Relation(ctx, out)
+
+
+def swap(ctx: Context, rel: Relation, col: int) -> None:
+    check(lib().vg_swap(ctx.h, ctypes.byref(rel.ir), col))
+
+
+def sort_rows(ctx: Context, rel: Relation) -> None:
+    check(lib().vg_sort_rows(ctx.h, ctypes.byref(rel.ir)))
+
+
+def unique(ctx: Context, rel: Relation) -> None:
+    check(lib().vg_unique(ctx.h, ctypes.byref(rel.ir)))
+
+
+def eif_scan(ctx: Context, rel: Relation):
+    out = (ctypes.c_uint64 * 4)()
+    check(lib().vg_eif_scan(ctx.h, ctypes.byref(rel.ir), out))
+    return tuple(out)

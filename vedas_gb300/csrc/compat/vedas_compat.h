@@ -1,0 +1,382 @@
+// Host-side mirror of the reference's query-execution interfaces, on top of
+// the GB300 kernels.  Class and method names, argument meaning and job
+// semantics follow the reference (paths relative to the reference project):
+//   VedasStorage        src/VedasStorage.h:8-132
+//   FullRelationIR      src/FullRelationIR.h:10-47
+//   EmptyIntervalDict   src/EmptyIntervalDict.h:6-23
+//   TriplePattern       src/TriplePattern.h:7-36
+//   SparqlQuery         src/SparqlQuery.h:10-47 (structured-text front end)
+//   SparqlResult        src/SparqlResult.h:9-25
+//   QueryJob & jobs     src/QueryJob.h, SelectQueryJob.h, JoinQueryJob.h,
+//                       IndexSwapJob.h, TransferJob.h
+//   QueryPlan           src/QueryPlan.h:15-49 (single-GPU execution)
+//   QueryGraph          src/QueryGraph.h:14-47
+//   QueryExecutor       src/QueryExecutor.h:39-123
+// Relations live in HBM (arena spans) instead of thrust::device_vector, the
+// index is resident in HBM, and the host keeps mirrors of the index arrays
+// for the host-side binary searches the reference performs.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <tuple>
+#include <unordered_map>
+#include <unordered_set>
+#include <utility>
+#include <vector>
+
+#include "../vg_ctx.h"
+#include "../vg_index.h"
+#include "../vg_relops.h"
+
+namespace vedas {
+
+typedef uint32_t TYPEID;
+typedef std::vector<TYPEID> TYPEID_HOST_VEC;
+typedef std::tuple<size_t, size_t, size_t, size_t> VAR_BOUND;
+typedef std::map<std::string, std::pair<TYPEID, TYPEID>> BoundDict;
+
+enum ExecuteLogRecordOp { JOIN_OP, UPLOAD_OP, SWAP_OP };
+struct ExecuteLogRecord {
+  int deviceId;
+  ExecuteLogRecordOp op;
+  size_t param1, param2, param3;
+  std::string paramstr;
+  ExecuteLogRecord(int d, ExecuteLogRecordOp o, std::string s, size_t p1, size_t p2 = 0, size_t p3 = 0)
+      : deviceId(d), op(o), param1(p1), param2(p2), param3(p3), paramstr(std::move(s)) {}
+};
+
+class IR {
+ public:
+  virtual ~IR() = default;
+};
+
+class VedasStorage {
+ public:
+  // Builds the index on the device from host or device columns.
+  VedasStorage(vg::Ctx* ctx, const TYPEID* s, const TYPEID* p, const TYPEID* o, size_t n,
+               bool inputs_on_device, bool fullIndex);
+  // Opens a .vds file written by write() (src/VedasStorage.cu:459-484).
+  VedasStorage(vg::Ctx* ctx, const char* fname, bool fullIndex);
+  ~VedasStorage();
+
+  size_t getTripleSize() const { return ix_.n; }
+  bool isFullIndex() const { return ix_.full; }
+  // Host mirrors (the reference's getters return host vectors).
+  TYPEID_HOST_VEC* getPredicateIndexValues() { return h("p_idx_values"); }
+  TYPEID_HOST_VEC* getPredicateIndexOffsets() { return h("p_idx_offsets"); }
+  TYPEID_HOST_VEC* getPredicateSubjectIndexValues() { return h("ps_s_idx_values"); }
+  TYPEID_HOST_VEC* getPredicateSubjectIndexOffsets() { return h("ps_idx_offsets"); }
+  TYPEID_HOST_VEC* getPredicateObjectIndexValues() { return h("po_o_idx_values"); }
+  TYPEID_HOST_VEC* getPredicateObjectIndexOffsets() { return h("po_idx_offsets"); }
+  TYPEID_HOST_VEC* getPSdata() { return h("ps_data"); }
+  TYPEID_HOST_VEC* getPOdata() { return h("po_data"); }
+  TYPEID_HOST_VEC* getPSOdata() { return h("pso_data"); }
+  TYPEID_HOST_VEC* getPOSdata() { return h("pos_data"); }
+  TYPEID_HOST_VEC* getSOPdata() { return h("sop_data"); }
+  // Device copies (resident).
+  const TYPEID* dev(const char* name) const { return ix_.get(name).ptr; }
+  uint64_t len(const char* name) const { return ix_.get(name).len; }
+  vg::Index& index() { return ix_; }
+  void write(const char* fname);
+
+ private:
+  vg::Index ix_;
+  TYPEID_HOST_VEC* h(const char* name) {
+    return const_cast<TYPEID_HOST_VEC*>(&ix_.host_array(name));
+  }
+};
+
+class FullRelationIR : public IR {
+ public:
+  FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSize);
+  ~FullRelationIR() override;
+  void sort();
+  void removeDuplicate();
+  TYPEID* getRelationRawPointer(size_t i) { return r_.cols[i]; }
+  size_t getColumnNum() const { return headers.size(); }
+  size_t getColumnId(const std::string& var) const;
+  void setHeader(size_t i, const std::string& h, bool is_predicate);
+  std::string getHeader(size_t i) const { return headers[i]; }
+  std::string getHeaders(const std::string& delimitor) const;
+  bool getIsPredicate(size_t i) const { return is_predicates[i]; }
+  void sortByFirstColumn();
+  void swapColumn(size_t i, size_t j);
+  void removeColumn(size_t i);
+  void removeColumn(size_t i, const std::string& maintain_var);
+  size_t size() const { return r_.ncols == 0 ? 0 : r_.nrows; }
+  vg::Rel& rel() { return r_; }
+  vg::Ctx* ctx() const { return ctx_; }
+  // Replaces the columns by `r` (takes ownership), keeping headers.
+  void adopt(vg::Rel& r);
+  // Hands the columns to the caller; the relation keeps its headers only.
+  vg::Rel release();
+
+ private:
+  vg::Ctx* ctx_;
+  vg::Rel r_;
+  std::vector<bool> is_predicates;
+  std::vector<std::string> headers;
+  std::unordered_map<std::string, size_t> var_column_map;
+};
+
+class EmptyIntervalDict {
+ public:
+  VAR_BOUND getBound(const std::string& var) const { return dict.at(var); }
+  void updateBound(const std::string& var, size_t lb1, size_t ub1, size_t lb2, size_t ub2);
+  // The pieces of data[start, end) outside the two empty intervals of var
+  // (offsets relative to the start of `data`).
+  void getUploadRelationData(const std::string& var, const TYPEID* data, size_t start, size_t end,
+                             size_t& relationSize, std::vector<std::pair<size_t, size_t>>& uploadIntervals,
+                             std::vector<size_t>& offsets);
+  size_t emptySize(const std::string& var);
+  bool hasBoundFor(const std::string& var) const { return dict.count(var) > 0; }
+
+ private:
+  std::unordered_map<std::string, VAR_BOUND> dict;
+};
+
+class TriplePattern {
+ public:
+  TriplePattern(size_t id, const std::string& s, const std::string& p, const std::string& o);
+  size_t getId() const { return id; }
+  TYPEID getSubjectId() const { return ids[0]; }
+  TYPEID getPredicateId() const { return ids[1]; }
+  TYPEID getObjectId() const { return ids[2]; }
+  std::string getSubject() const { return names[0]; }
+  std::string getPredicate() const { return names[1]; }
+  std::string getObject() const { return names[2]; }
+  size_t getVariableNum() const { return isVar[0] + isVar[1] + isVar[2]; }
+  size_t getVariableBitmap() const { return isVar[0] * 4 + isVar[1] * 2 + isVar[2]; }
+  bool subjectIsVariable() const { return isVar[0]; }
+  bool predicateIsVariable() const { return isVar[1]; }
+  bool objectIsVariable() const { return isVar[2]; }
+  bool hasVariable(const std::string& v) const;
+  size_t estimate_rows = 0;
+
+ private:
+  size_t id;
+  std::string names[3];
+  TYPEID ids[3] = {0, 0, 0};
+  bool isVar[3] = {false, false, false};
+};
+
+// SPARQL basic-graph-pattern front end (the reference parses with Rasqal,
+// src/SparqlQuery.cu:29-124): SELECT * | ?v.. WHERE { t t t . ... } with
+// constants written as <ID> or "ID".
+class SparqlQuery {
+ public:
+  explicit SparqlQuery(const char* q);
+  size_t getPatternNum() const { return patterns.size(); }
+  TriplePattern* getPatternPtr(size_t i) { return &patterns[i]; }
+  std::map<std::string, int>& getVarCountMap() { return vars_count; }
+  std::set<std::string> getSelectedVariables() const { return selected_variables; }
+  int boundedNum = 0;
+
+ private:
+  std::vector<TriplePattern> patterns;
+  std::set<std::string> selected_variables;
+  std::map<std::string, int> vars_count;
+};
+
+class SparqlResult {
+ public:
+  void setResult(IR* ir);
+  FullRelationIR* getResultIR() { return resultIR; }
+
+ private:
+  FullRelationIR* resultIR = nullptr;
+};
+
+class QueryExecutor;
+
+class QueryJob {
+ public:
+  virtual ~QueryJob() = default;
+  virtual IR* getIR() = 0;
+  virtual int startJob(int gpuId) = 0;
+  virtual std::string jobTypeName() const = 0;
+  int getGpuId() const { return gpuId; }
+
+ protected:
+  int gpuId = 0;
+  IR* intermediateResult = nullptr;
+};
+
+class SelectQueryJob : public QueryJob {
+ public:
+  // two variables (src/SelectQueryJob.h:14-19)
+  SelectQueryJob(QueryExecutor* ex, bool pos_index, std::string v1, std::string v2, TYPEID id1,
+                 bool is_second_var_used);
+  // one variable (src/SelectQueryJob.h:20-24): subject_var selects POS
+  SelectQueryJob(QueryExecutor* ex, bool subject_var, std::string v1, TYPEID id1, TYPEID id2);
+  ~SelectQueryJob() override;
+  int startJob(int gpuId) override;
+  IR* getIR() override { return intermediateResult; }
+  std::string jobTypeName() const override { return "Upload Job"; }
+
+ private:
+  QueryExecutor* ex;
+  bool pos_index = false;     // 2-var: POS vs PSO; 1-var: subject variable
+  std::string variables[2];
+  size_t variable_num;
+  TYPEID dataid[2] = {0, 0};
+  bool is_second_var_used = true;
+};
+
+class JoinQueryJob : public QueryJob {
+ public:
+  JoinQueryJob(QueryExecutor* ex, QueryJob* leftJob, QueryJob* rightJob, std::string joinVariable,
+               bool lastJoinForVar = true);
+  // The reference never frees join results; here the job owns its relation.
+  ~JoinQueryJob() override { delete intermediateResult; }
+  int startJob(int gpuId) override;
+  IR* getIR() override { return intermediateResult; }
+  std::string jobTypeName() const override { return "Join Job"; }
+  void setQueryVarCounter(std::map<std::string, size_t>* c) { query_variable_counter = c; }
+  std::string getJoinVariable() const { return joinVariable; }
+  IR* join(FullRelationIR* lir, FullRelationIR* rir);
+
+ private:
+  QueryExecutor* ex;
+  QueryJob* leftJob;
+  QueryJob* rightJob;
+  std::string joinVariable;
+  bool lastJoinForVar;
+  std::map<std::string, size_t>* query_variable_counter = nullptr;
+};
+
+class IndexSwapJob : public QueryJob {
+ public:
+  IndexSwapJob(QueryExecutor* ex, QueryJob* beforeJob, std::string swapVar);
+  int startJob(int gpuId) override;
+  IR* getIR() override { return intermediateResult; }
+  std::string jobTypeName() const override { return "Index Swap Job"; }
+
+ private:
+  QueryExecutor* ex;
+  QueryJob* beforeJob;
+  std::string swapVar;
+};
+
+// Single-GPU build: the relation already lives on the executing device, so
+// the transfer is a pass-through (src/TransferJob.cu:28-39 moves it by P2P).
+class TransferJob : public QueryJob {
+ public:
+  TransferJob(size_t src_thread_id, size_t dest_thread_id, int src_gpu_id, int dest_gpu_id,
+              QueryJob* job);
+  int startJob(int gpuId) override;
+  IR* getIR() override { return intermediateResult; }
+  std::string jobTypeName() const override { return "Transfer Job"; }
+
+ private:
+  QueryJob* job;
+  int src_gpu_id, dest_gpu_id;
+};
+
+class QueryPlan {
+ public:
+  explicit QueryPlan(std::set<std::string>& select_variable_set);
+  ~QueryPlan();
+  void pushJob(QueryJob* job);
+  QueryJob* getJob(size_t i) { return jobs[i]; }
+  size_t jobNum() const { return jobs.size(); }
+  // Runs the jobs in order, projects and removes adjacent duplicates.
+  void execute(SparqlResult& sparqlResult);
+
+ private:
+  std::map<std::string, size_t> query_variable_counter;
+  std::vector<QueryJob*> jobs;
+  std::vector<std::string> select_variables;
+};
+
+enum PlanOperation { UPLOAD, JOIN, INDEXSWAP };
+struct PlanTreeNode {
+  PlanOperation op;
+  PlanTreeNode* child1 = nullptr;
+  PlanTreeNode* child2 = nullptr;
+  bool reuseVar = false;
+  TriplePattern* tp = nullptr;
+  std::string var;
+};
+
+struct GraphEdge {
+  std::string id, indexVar1, indexVar2;
+  std::set<std::string> vars;
+  TriplePattern* tp = nullptr;
+  size_t estimateCardinality = 0;
+  PlanTreeNode* treeNode = nullptr;
+  bool hasVariable(const std::string& v) const { return vars.count(v) > 0; }
+};
+
+class QueryGraph {
+ public:
+  explicit QueryGraph(SparqlQuery* q);
+  PlanTreeNode* generateQueryPlan();
+
+ private:
+  std::unordered_map<std::string, std::vector<std::pair<std::string, GraphEdge*>>> adjacencyList;
+  std::vector<std::unique_ptr<GraphEdge>> edges;
+  std::vector<std::unique_ptr<PlanTreeNode>> nodes;
+  void addEdge(const std::string& a, const std::string& b, GraphEdge* e);
+  bool edgeExist(const std::string& a, const std::string& b);
+  void mergeEdge(const std::string end1, const std::string end2);
+  std::tuple<size_t, size_t, std::string> sameMaxDegAndTotalCard(
+      std::vector<std::pair<std::string, GraphEdge*>>& links);
+  std::pair<std::string, std::string> findBestStarNode();
+  PlanTreeNode* generateJoinPlanForNode(const std::string& vertex, const std::string& joinVar);
+  PlanTreeNode* newNode(PlanOperation op);
+};
+
+class QueryExecutor {
+ public:
+  QueryExecutor(VedasStorage* storage, vg::Ctx* ctx);
+  // Plans and runs one query (src/QueryExecutor.cu:294-431).
+  void query(SparqlQuery& sq, SparqlResult& sr);
+  // The job list the reference would run (for batching); the plan keeps it.
+  void plan(SparqlQuery& sq, QueryPlan& plan);
+
+  static void updateBoundDict(BoundDict* bound, const std::string& variable, TYPEID lowerBound,
+                              TYPEID upperBound);
+  static std::pair<size_t, size_t> findL2OffsetFromL1(const TYPEID_HOST_VEC* l1v, const TYPEID_HOST_VEC* l1o,
+                                                      TYPEID id1, size_t n);
+  static std::pair<size_t, size_t> findDataOffsetFromL2(const TYPEID_HOST_VEC* l2v,
+                                                        const TYPEID_HOST_VEC* l2o, TYPEID lo, TYPEID hi,
+                                                        TYPEID id2);
+  static std::pair<size_t, size_t> findDataOffsetFromL2(const TYPEID_HOST_VEC* l2_data, size_t lo,
+                                                        size_t hi, TYPEID id2);
+
+  // Execution log of the current query (QueryExecutor::exe_log).
+  std::vector<ExecuteLogRecord> exe_log;
+  static bool ENABLE_UPDATE_BOUND_AFTER_JOIN;
+
+  VedasStorage* storage;
+  vg::Ctx* ctx;
+  BoundDict variables_bound;
+  EmptyIntervalDict empty_interval_dict;
+  std::set<std::string> selected_variables;
+  std::unordered_set<std::string> join_vars;
+
+  // Empty-interval scan of a relation's column 0 (2 < size < 100).
+  void eifScan(FullRelationIR* ir, const std::string& var);
+  // The four bounds that scan passes to EmptyIntervalDict::updateBound.
+  static void eifBounds(const TYPEID* c0, size_t n, size_t out[4]);
+
+ private:
+  void createVariableBound(SparqlQuery& sq);
+  void squeezeQueryBound1Var(TriplePattern* p);
+  void squeezeQueryBound2Var(TriplePattern* p);
+  int postorderTraversal(QueryPlan& plan, PlanTreeNode* root, SparqlQuery& sq);
+  SelectQueryJob* createSelectQueryJob(TriplePattern* p, const std::string& index_used);
+};
+
+// A condition on which the reference itself would read out of bounds or trip
+// an assert; the core refuses the query instead (VG_ERR_UNSUPPORTED).
+struct ReferenceUB : vg::Error {
+  explicit ReferenceUB(const std::string& m) : vg::Error(VG_ERR_UNSUPPORTED, m) {}
+};
+
+}  // namespace vedas

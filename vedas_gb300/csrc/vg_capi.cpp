@@ -1,0 +1,373 @@
+// The C-ABI (include/vedas_gb300.h): status codes at the boundary, no
+// exceptions across it.
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "compat/vedas_compat.h"
+#include "vg_ctx.h"
+#include "vg_index.h"
+#include "vg_relops.h"
+
+struct vg_ctx {
+  vg::Ctx c;
+};
+
+struct vg_index {
+  vg_ctx* ctx = nullptr;
+  std::unique_ptr<vedas::VedasStorage> st;
+};
+
+struct vg_result {
+  vg_ctx* ctx = nullptr;
+  vg::Rel rel;
+  std::vector<std::string> headers;
+  std::vector<vedas::ExecuteLogRecord> log;
+  ~vg_result() {
+    if (ctx) vg::rel_free(ctx->c, rel);
+  }
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+vg_status guard(F&& f) {
+  try {
+    f();
+    return VG_OK;
+  } catch (const vg::Error& e) {
+    g_last_error = e.what();
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return VG_ERR_OOM;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return VG_ERR_INVALID;
+  }
+}
+
+vg::Rel to_rel(const vg_ir* ir) {
+  vg::Rel r;
+  r.ncols = ir->ncols;
+  r.nrows = ir->nrows;
+  for (uint32_t c = 0; c < ir->ncols && c < VG_MAX_COLS; ++c) r.cols[c] = ir->cols[c];
+  return r;
+}
+
+void from_rel(const vg::Rel& r, vg_ir* ir) {
+  std::memset(ir, 0, sizeof(*ir));
+  ir->ncols = r.ncols;
+  ir->nrows = r.nrows;
+  for (uint32_t c = 0; c < r.ncols; ++c) ir->cols[c] = r.cols[c];
+}
+
+void check_ir(const vg_ir* ir) {
+  if (!ir || ir->ncols == 0 || ir->ncols > VG_MAX_COLS) vg::fail(VG_ERR_INVALID, "bad relation");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* vg_status_string(vg_status s) {
+  switch (s) {
+    case VG_OK: return "ok";
+    case VG_ERR_INVALID: return "invalid argument";
+    case VG_ERR_OOM: return "out of memory";
+    case VG_ERR_CUDA: return "CUDA error";
+    case VG_ERR_TIMEOUT: return "bounded device wait expired";
+    case VG_ERR_UNSUPPORTED: return "unsupported input";
+    case VG_ERR_PARSE: return "query parse error";
+    case VG_ERR_OVERFLOW: return "size limit exceeded";
+    case VG_ERR_REJECTED: return "admission rejected";
+  }
+  return "unknown status";
+}
+
+const char* vg_last_error(void) { return g_last_error.c_str(); }
+
+vg_status vg_ctx_create(int device, size_t arena_bytes, vg_ctx** out) {
+  if (!out) return VG_ERR_INVALID;
+  *out = nullptr;
+  auto h = std::make_unique<vg_ctx>();
+  vg_status st = guard([&] {
+    vg::Ctx& c = h->c;
+    c.device = device;
+    VG_CUDA(cudaSetDevice(device));
+    VG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    VG_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+    if (arena_bytes == 0) {
+      size_t fr = 0, tot = 0;
+      VG_CUDA(cudaMemGetInfo(&fr, &tot));
+      arena_bytes = fr / 10 * 9;
+    }
+    c.arena.init(arena_bytes);
+    VG_CUDA(cudaMalloc(&c.d_err, sizeof(vg::DeviceErrors)));
+    VG_CUDA(cudaMemset(c.d_err, 0, sizeof(vg::DeviceErrors)));
+    VG_CUDA(cudaMallocHost(&c.h_small, vg::Ctx::kSmallWords * sizeof(uint64_t)));
+  });
+  if (st != VG_OK) {
+    vg_ctx_destroy(h.release());
+    return st;
+  }
+  *out = h.release();
+  return VG_OK;
+}
+
+vg_status vg_ctx_destroy(vg_ctx* ctx) {
+  if (!ctx) return VG_OK;
+  vg::Ctx& c = ctx->c;
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  c.arena.release();
+  if (c.d_err) cudaFree(c.d_err);
+  if (c.h_small) cudaFreeHost(c.h_small);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  delete ctx;
+  return VG_OK;
+}
+
+vg_status vg_ctx_memory(vg_ctx* ctx, size_t* used, size_t* peak, size_t* capacity) {
+  if (!ctx) return VG_ERR_INVALID;
+  if (used) *used = ctx->c.arena.used();
+  if (peak) *peak = ctx->c.arena.peak();
+  if (capacity) *capacity = ctx->c.arena.capacity();
+  return VG_OK;
+}
+
+vg_status vg_ctx_sync(vg_ctx* ctx) {
+  if (!ctx) return VG_ERR_INVALID;
+  return guard([&] { ctx->c.sync(); });
+}
+
+void* vg_ctx_stream(vg_ctx* ctx) { return ctx ? static_cast<void*>(ctx->c.stream) : nullptr; }
+
+vg_status vg_index_build(vg_ctx* ctx, const uint32_t* s, const uint32_t* p, const uint32_t* o, uint64_t n,
+                         int full_index, int inputs_on_device, vg_index** out) {
+  if (!ctx || !out || (n && (!s || !p || !o))) return VG_ERR_INVALID;
+  *out = nullptr;
+  auto h = std::make_unique<vg_index>();
+  h->ctx = ctx;
+  vg_status st = guard([&] {
+    h->st = std::make_unique<vedas::VedasStorage>(&ctx->c, s, p, o, n, inputs_on_device != 0, full_index != 0);
+  });
+  if (st == VG_OK) *out = h.release();
+  return st;
+}
+
+vg_status vg_index_free(vg_index* ix) {
+  if (!ix) return VG_OK;
+  vg_status st = guard([&] {
+    ix->ctx->c.sync();
+    ix->st.reset();
+  });
+  delete ix;
+  return st;
+}
+
+vg_status vg_index_array(vg_index* ix, const char* name, const uint32_t** dev, const uint32_t** host,
+                         uint64_t* len) {
+  if (!ix || !name) return VG_ERR_INVALID;
+  return guard([&] {
+    vg::Index& I = ix->st->index();
+    if (!I.dev.count(name)) vg::fail(VG_ERR_INVALID, std::string("no index array ") + name);
+    const vg::DevArray& d = I.get(name);
+    if (dev) *dev = d.ptr;
+    if (len) *len = d.len;
+    if (host) *host = I.host_array(name).data();
+  });
+}
+
+vg_status vg_index_write(vg_index* ix, const char* path) {
+  if (!ix || !path) return VG_ERR_INVALID;
+  return guard([&] { ix->st->write(path); });
+}
+
+vg_status vg_index_open(vg_ctx* ctx, const char* path, int full_index, vg_index** out) {
+  if (!ctx || !path || !out) return VG_ERR_INVALID;
+  *out = nullptr;
+  auto h = std::make_unique<vg_index>();
+  h->ctx = ctx;
+  vg_status st = guard([&] { h->st = std::make_unique<vedas::VedasStorage>(&ctx->c, path, full_index != 0); });
+  if (st == VG_OK) *out = h.release();
+  return st;
+}
+
+vg_status vg_ir_alloc(vg_ctx* ctx, uint32_t ncols, uint64_t nrows, vg_ir* out) {
+  if (!ctx || !out || ncols == 0 || ncols > VG_MAX_COLS) return VG_ERR_INVALID;
+  return guard([&] { from_rel(vg::rel_alloc(ctx->c, ncols, nrows), out); });
+}
+
+vg_status vg_ir_free(vg_ctx* ctx, vg_ir* ir) {
+  if (!ctx || !ir) return VG_ERR_INVALID;
+  return guard([&] {
+    vg::Rel r = to_rel(ir);
+    vg::rel_free(ctx->c, r);
+    std::memset(ir, 0, sizeof(*ir));
+  });
+}
+
+vg_status vg_ir_upload(vg_ctx* ctx, vg_ir* ir, uint32_t col, const uint32_t* host, uint64_t n) {
+  if (!ctx || !ir || col >= ir->ncols || n > ir->nrows || (n && !host)) return VG_ERR_INVALID;
+  return guard([&] {
+    if (n) VG_CUDA(cudaMemcpyAsync(ir->cols[col], host, n * 4, cudaMemcpyHostToDevice, ctx->c.stream));
+    ctx->c.sync();
+  });
+}
+
+vg_status vg_ir_download(vg_ctx* ctx, const vg_ir* ir, uint32_t col, uint32_t* host) {
+  if (!ctx || !ir || col >= ir->ncols || (ir->nrows && !host)) return VG_ERR_INVALID;
+  return guard([&] { vg::download(ctx->c, ir->cols[col], ir->nrows, host); });
+}
+
+vg_status vg_select(vg_ctx* ctx, vg_index* ix, const vg_select_desc* d, vg_ir* out, uint32_t bu[3]) {
+  if (!ctx || !ix || !d || !out || d->kind < 1 || d->kind > 3) return VG_ERR_INVALID;
+  return guard([&] {
+    vedas::QueryExecutor ex(ix->st.get(), &ctx->c);
+    const std::string v0 = "?v0", v1 = "?v1";
+    if (d->has_bound) ex.variables_bound[v0] = {d->bound_lo, d->bound_hi};
+    if (d->eif[0] || d->eif[1] || d->eif[2] || d->eif[3])
+      ex.empty_interval_dict.updateBound(v0, d->eif[0], d->eif[1], d->eif[2], d->eif[3]);
+    std::unique_ptr<vedas::SelectQueryJob> job;
+    if (d->kind == 3)
+      job.reset(new vedas::SelectQueryJob(&ex, d->index_pos != 0, v0, v1, d->pred, d->second_used != 0));
+    else
+      job.reset(new vedas::SelectQueryJob(&ex, d->kind == 1, v0, d->pred, d->constant));
+    job->startJob(0);
+    auto* ir = dynamic_cast<vedas::FullRelationIR*>(job->getIR());
+    from_rel(ir->release(), out);
+    if (bu) {
+      bu[2] = 0;
+      if (d->has_bound && d->kind != 3) {
+        bu[0] = ex.variables_bound[v0].first;
+        bu[1] = ex.variables_bound[v0].second;
+        bu[2] = 1;
+      }
+    }
+    ctx->c.sync();
+  });
+}
+
+vg_status vg_join(vg_ctx* ctx, const vg_ir* l, const vg_ir* r, vg_ir* out, uint32_t first_last[2]) {
+  if (!ctx || !out) return VG_ERR_INVALID;
+  return guard([&] {
+    check_ir(l);
+    check_ir(r);
+    vg::Rel o;
+    vg::join(ctx->c, to_rel(l), to_rel(r), false, o);
+    from_rel(o, out);
+    if (first_last && o.nrows > 0) {
+      VG_CUDA(cudaMemcpyAsync(&first_last[0], o.cols[0], 4, cudaMemcpyDeviceToHost, ctx->c.stream));
+      VG_CUDA(cudaMemcpyAsync(&first_last[1], o.cols[0] + o.nrows - 1, 4, cudaMemcpyDeviceToHost, ctx->c.stream));
+    }
+    ctx->c.sync();
+  });
+}
+
+vg_status vg_join2(vg_ctx* ctx, const vg_ir* l, const vg_ir* r, vg_ir* out) {
+  if (!ctx || !out) return VG_ERR_INVALID;
+  return guard([&] {
+    check_ir(l);
+    check_ir(r);
+    vg::Rel o;
+    vg::join(ctx->c, to_rel(l), to_rel(r), true, o);
+    from_rel(o, out);
+    ctx->c.sync();
+  });
+}
+
+vg_status vg_swap(vg_ctx* ctx, vg_ir* ir, uint32_t col) {
+  if (!ctx || !ir || col >= ir->ncols) return VG_ERR_INVALID;
+  return guard([&] {
+    vg::Rel r = to_rel(ir);
+    std::swap(r.cols[0], r.cols[col]);
+    vg::sort_by_first(ctx->c, r);
+    from_rel(r, ir);
+    ctx->c.sync();
+  });
+}
+
+vg_status vg_sort_rows(vg_ctx* ctx, vg_ir* ir) {
+  if (!ctx || !ir) return VG_ERR_INVALID;
+  return guard([&] {
+    check_ir(ir);
+    vg::Rel r = to_rel(ir);
+    vg::sort_rows(ctx->c, r);
+    from_rel(r, ir);
+    ctx->c.sync();
+  });
+}
+
+vg_status vg_unique(vg_ctx* ctx, vg_ir* ir) {
+  if (!ctx || !ir) return VG_ERR_INVALID;
+  return guard([&] {
+    check_ir(ir);
+    vg::Rel r = to_rel(ir);
+    vg::unique_in_place(ctx->c, r);
+    from_rel(r, ir);
+  });
+}
+
+vg_status vg_eif_scan(vg_ctx* ctx, const vg_ir* ir, uint64_t out4[4]) {
+  if (!ctx || !ir || !out4 || ir->ncols == 0 || ir->nrows <= 2 || ir->nrows >= 100) return VG_ERR_INVALID;
+  return guard([&] {
+    std::vector<uint32_t> c0(ir->nrows);
+    vg::download(ctx->c, ir->cols[0], ir->nrows, c0.data());
+    size_t b[4];
+    vedas::QueryExecutor::eifBounds(c0.data(), c0.size(), b);
+    for (int i = 0; i < 4; ++i) out4[i] = b[i];
+  });
+}
+
+vg_status vg_query(vg_ctx* ctx, vg_index* ix, const char* sparql, vg_result** out) {
+  if (!ctx || !ix || !sparql || !out) return VG_ERR_INVALID;
+  *out = nullptr;
+  auto res = std::make_unique<vg_result>();
+  vg_status st = guard([&] {
+    vedas::QueryExecutor ex(ix->st.get(), &ctx->c);
+    vedas::SparqlQuery sq(sparql);
+    std::set<std::string> sel = sq.getSelectedVariables();
+    vedas::QueryPlan plan(sel);
+    ex.plan(sq, plan);
+    vedas::SparqlResult sr;
+    plan.execute(sr);
+    vedas::FullRelationIR* ir = sr.getResultIR();
+    for (size_t c = 0; c < ir->getColumnNum(); ++c) res->headers.push_back(ir->getHeader(c));
+    res->rel = ir->release();
+    res->ctx = ctx;
+    res->log = ex.exe_log;
+    ctx->c.sync();
+  });
+  if (st == VG_OK) *out = res.release();
+  return st;
+}
+
+uint32_t vg_result_ncols(const vg_result* r) { return r ? static_cast<uint32_t>(r->headers.size()) : 0; }
+uint64_t vg_result_nrows(const vg_result* r) { return r ? r->rel.nrows : 0; }
+const char* vg_result_header(const vg_result* r, uint32_t c) {
+  return (r && c < r->headers.size()) ? r->headers[c].c_str() : nullptr;
+}
+const uint32_t* vg_result_column_device(const vg_result* r, uint32_t c) {
+  return (r && c < r->rel.ncols) ? r->rel.cols[c] : nullptr;
+}
+vg_status vg_result_download(const vg_result* r, uint32_t c, uint32_t* host) {
+  if (!r || c >= r->rel.ncols) return VG_ERR_INVALID;
+  return guard([&] { vg::download(r->ctx->c, r->rel.cols[c], r->rel.nrows, host); });
+}
+uint32_t vg_result_nlog(const vg_result* r) { return r ? static_cast<uint32_t>(r->log.size()) : 0; }
+void vg_result_log(const vg_result* r, uint32_t i, uint32_t* op, uint64_t* p1, uint64_t* p2, uint64_t* p3) {
+  if (!r || i >= r->log.size()) return;
+  const auto& l = r->log[i];
+  if (op) *op = static_cast<uint32_t>(l.op);
+  if (p1) *p1 = l.param1;
+  if (p2) *p2 = l.param2;
+  if (p3) *p3 = l.param3;
+}
+vg_status vg_result_free(vg_result* r) {
+  delete r;
+  return VG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// Execution context: one device, one stream, one HBM arena.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vg_common.cuh"
+
+namespace vg {
+
+// First-fit allocator over one cudaMalloc'd slab.  Allocation is host-side
+// bookkeeping only (no device call), so intermediate relations never pay a
+// cudaMalloc.  All work on the slab is ordered on the context stream, so a
+// block may be handed out again as soon as the work that last used it has
+// been enqueued.
+class Arena {
+ public:
+  Arena() = default;
+  Arena(const Arena&) = delete;
+  Arena& operator=(const Arena&) = delete;
+  void init(size_t bytes);
+  void release();
+  void* alloc(size_t bytes);      // throws VG_ERR_OOM
+  void* try_alloc(size_t bytes);  // nullptr when it does not fit
+  void free(void* p);
+  // Returns the tail of a live block beyond new_bytes to the free list.
+  void shrink(void* p, size_t new_bytes);
+  size_t capacity() const { return cap_; }
+  size_t used() const { return used_; }
+  size_t peak() const { return peak_; }
+  size_t largest_free() const;
+
+ private:
+  static constexpr size_t kAlign = 256;
+  char* base_ = nullptr;
+  size_t cap_ = 0, used_ = 0, peak_ = 0;
+  std::map<size_t, size_t> free_;   // offset -> size
+  std::map<size_t, size_t> live_;   // offset -> size
+  mutable std::mutex mu_;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Arena arena;
+  DeviceErrors* d_err = nullptr;   // device error record
+  int num_sms = 0;
+  // pinned staging for small device->host reads (sizes, first/last keys)
+  uint64_t* h_small = nullptr;
+  static constexpr int kSmallWords = 1024;
+
+  template <typename T>
+  T* alloc(uint64_t n) {
+    return static_cast<T*>(arena.alloc((n ? n : 1) * sizeof(T)));
+  }
+  void free(void* p) { arena.free(p); }
+  void sync() { VG_CUDA(cudaStreamSynchronize(stream)); }
+  // Raises VG_ERR_TIMEOUT / VG_ERR_OVERFLOW if a kernel recorded one (syncs).
+  void check_device_errors();
+};
+
+// RAII scratch buffer from the arena.
+template <typename T>
+struct Scratch {
+  Ctx* ctx = nullptr;
+  T* p = nullptr;
+  Scratch() = default;
+  Scratch(Ctx& c, uint64_t n) : ctx(&c), p(c.alloc<T>(n)) {}
+  Scratch(const Scratch&) = delete;
+  Scratch& operator=(const Scratch&) = delete;
+  Scratch(Scratch&& o) noexcept : ctx(o.ctx), p(o.p) { o.p = nullptr; }
+  ~Scratch() {
+    if (p) ctx->free(p);
+  }
+  T* get() const { return p; }
+};
+
+}  // namespace vg

@@ -1,0 +1,154 @@
+// Block-level building blocks: warp/block scans and single-pass decoupled
+// look-back across tiles (bounded spin-waits).
+#pragma once
+
+#include "vg_common.cuh"
+
+namespace vg {
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane_id() >= static_cast<uint32_t>(d)) v += t;
+  }
+  return v;
+}
+
+__device__ __forceinline__ uint64_t warp_incl_scan64(uint64_t v) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint64_t t = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane_id() >= static_cast<uint32_t>(d)) v += t;
+  }
+  return v;
+}
+
+__device__ __forceinline__ uint64_t warp_sum64(uint64_t v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  return v;
+}
+
+// Exclusive scan of one value per thread over a BLOCK-thread block.
+// s_warp: BLOCK/32 words of shared memory.  Contains __syncthreads().
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t& total, uint32_t* s_warp) {
+  constexpr int W = BLOCK / 32;
+  uint32_t incl = warp_incl_scan(v);
+  uint32_t w = threadIdx.x >> 5;
+  if (lane_id() == 31) s_warp[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t x = lane_id() < W ? s_warp[lane_id()] : 0u;
+    uint32_t xi = warp_incl_scan(x);
+    if (lane_id() < W) s_warp[lane_id()] = xi - x;
+    if (lane_id() == W - 1) s_warp[W] = xi;
+  }
+  __syncthreads();
+  uint32_t res = s_warp[w] + incl - v;
+  total = s_warp[W];
+  __syncthreads();
+  return res;
+}
+
+// 64-bit variant; s_warp: BLOCK/32 + 1 words.
+template <int BLOCK>
+__device__ __forceinline__ uint64_t block_excl_scan64(uint64_t v, uint64_t& total, uint64_t* s_warp) {
+  constexpr int W = BLOCK / 32;
+  uint64_t incl = warp_incl_scan64(v);
+  uint32_t w = threadIdx.x >> 5;
+  if (lane_id() == 31) s_warp[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    uint64_t x = lane_id() < W ? s_warp[lane_id()] : 0ull;
+    uint64_t xi = warp_incl_scan64(x);
+    if (lane_id() < W) s_warp[lane_id()] = xi - x;
+    if (lane_id() == W - 1) s_warp[W] = xi;
+  }
+  __syncthreads();
+  uint64_t res = s_warp[w] + incl - v;
+  total = s_warp[W];
+  __syncthreads();
+  return res;
+}
+
+// Polls a look-back status word until a predecessor has published it.
+// Gives up after kSpinLimit polls: records the timeout and returns an
+// inclusive zero so that every waiter still terminates.
+__device__ __forceinline__ uint64_t wait_status(const uint64_t* p, DeviceErrors* err) {
+  uint64_t s = ld_acquire_u64(p);
+  uint32_t spins = 0;
+  while ((s & ~kValueMask) == 0) {
+    if (++spins > kSpinLimit) {
+      atomicExch(&err->timeout, 1u);
+      return kFlagInc;
+    }
+    __nanosleep(32);
+    s = ld_acquire_u64(p);
+  }
+  return s;
+}
+
+// Decoupled look-back (single counter per tile): publishes this tile's total
+// and returns the exclusive prefix of all earlier tiles.  Executed by one full
+// warp; `status` must be zero before the launch.
+__device__ __forceinline__ uint64_t warp_lookback(uint64_t* status, uint32_t tile, uint64_t tile_total,
+                                                  DeviceErrors* err) {
+  const uint32_t lane = lane_id();
+  if (lane == 0) st_release_u64(&status[tile], (tile == 0 ? kFlagInc : kFlagAgg) | tile_total);
+  uint64_t prefix = 0;
+  if (tile > 0) {
+    int64_t j = static_cast<int64_t>(tile) - 1 - lane;
+    while (true) {
+      uint64_t s = (j >= 0) ? wait_status(&status[j], err) : kFlagInc;
+      bool inc = (s & kFlagInc) != 0;
+      uint32_t inc_mask = __ballot_sync(0xffffffffu, inc);
+      uint64_t v = s & kValueMask;
+      if (inc_mask) {
+        uint32_t lim = __ffs(inc_mask) - 1;
+        prefix += warp_sum64(lane <= lim ? v : 0);
+        break;
+      }
+      prefix += warp_sum64(v);
+      j -= 32;
+    }
+    if (lane == 0) st_release_u64(&status[tile], kFlagInc | (prefix + tile_total));
+  }
+  return prefix;
+}
+
+// Whole-block wrapper: warp 0 looks back, the prefix is broadcast.
+__device__ __forceinline__ uint64_t block_lookback(uint64_t* status, uint32_t tile, uint64_t tile_total,
+                                                   DeviceErrors* err, uint64_t* s_bcast) {
+  if (threadIdx.x < 32) {
+    uint64_t p = warp_lookback(status, tile, tile_total, err);
+    if (threadIdx.x == 0) *s_bcast = p;
+  }
+  __syncthreads();
+  uint64_t r = *s_bcast;
+  __syncthreads();
+  return r;
+}
+
+// Branch-free lower/upper bound over a sorted device array.
+template <typename T, typename V>
+__device__ __forceinline__ uint64_t lower_bound_dev(const T* a, uint64_t lo, uint64_t hi, V key) {
+  while (lo < hi) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+template <typename T, typename V>
+__device__ __forceinline__ uint64_t upper_bound_dev(const T* a, uint64_t lo, uint64_t hi, V key) {
+  while (lo < hi) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (key < a[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+}  // namespace vg

@@ -1,0 +1,52 @@
+#pragma once
+
+#include <vector>
+
+#include "vg_ctx.h"
+
+namespace vg {
+
+// A device relation: ncols uint32 columns of nrows rows (column-major).
+struct Rel {
+  uint32_t ncols = 0;
+  uint64_t nrows = 0;
+  uint32_t* cols[VG_MAX_COLS] = {nullptr};
+};
+
+Rel rel_alloc(Ctx& ctx, uint32_t ncols, uint64_t nrows);
+void rel_free(Ctx& ctx, Rel& r);
+
+// One contiguous copy src[0, len) -> dst[0, len).
+struct CopyPiece {
+  const uint32_t* src;
+  uint32_t* dst;
+  uint64_t len;
+};
+// All pieces in one launch (up to 16).
+void multi_copy(Ctx& ctx, const CopyPiece* pieces, int np);
+
+// Adjacent-unique compaction of the rows of `in` (ncols columns, n rows) into
+// `out`; returns the number of rows kept (synchronizes).
+uint64_t unique_rows(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, uint32_t ncols,
+                     uint64_t n);
+
+// Sorted inner join of l and r on column 0 (two_keys: on columns 0 and 1).
+// Output layout: key column(s), l's other columns, r's other columns; rows
+// ordered by (left row, right row).  Allocates `out` from the arena.
+void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out);
+
+// out[c][i] = in[c][perm[i]] for every column.
+void gather_cols(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, uint32_t ncols,
+                 const uint32_t* perm, uint64_t n);
+
+// Stable sort of the rows by column 0 (in place; columns are replaced).
+void sort_by_first(Ctx& ctx, Rel& r);
+// Lexicographic sort of the rows over all columns (in place).
+void sort_rows(Ctx& ctx, Rel& r);
+// Adjacent duplicate-row removal in place.
+void unique_in_place(Ctx& ctx, Rel& r);
+
+// Copies `n` values of a device column to the host (synchronizes).
+void download(Ctx& ctx, const uint32_t* dev, uint64_t n, uint32_t* host);
+
+}  // namespace vg

@@ -126,6 +126,107 @@ def graph_chain(n: int = 100_000_000, n_entities: int = 2_000_000, n_predicates:
     return Graph(s, p, o, f"chain_n{n}")
 
 
+# ---------------------------------------------------------------------------
+# Query templates: star (S), chain (C) and snowflake (F), 1-8 patterns.
+# Placeholders: P<k> a predicate, O<k> an existing object of P<k>,
+# S<k> an existing subject of P<k>.  Variable-only patterns draw their
+# predicate from the rarer half of the ranks to bound result sizes; the
+# globally-last predicate is never used (the reference's own lookups read past
+# its index there, so no workload sends it).
+# ---------------------------------------------------------------------------
+TEMPLATES = [
+    ("S", "SELECT ?x WHERE { ?x P1 O1 . }"),
+    ("S", "SELECT ?o WHERE { S1 P1 ?o . }"),
+    ("S", "SELECT * WHERE { ?x P1 ?a . ?x P2 ?b . }"),
+    ("S", "SELECT * WHERE { ?x P1 O1 . ?x P2 ?b . }"),
+    ("S", "SELECT * WHERE { ?x P1 O1 . ?x P2 ?b . ?x P3 ?c . }"),
+    ("S", "SELECT ?x ?c WHERE { ?x P1 ?a . ?x P2 O2 . ?x P3 ?c . }"),
+    ("S", "SELECT * WHERE { ?x P1 O1 . ?x P2 ?b . ?x P3 ?c . ?x P4 ?d . }"),
+    ("S", "SELECT ?x ?b WHERE { ?x P1 O1 . ?x P2 ?b . ?x P3 ?c . ?x P4 ?d . ?x P5 ?e . }"),
+    ("C", "SELECT * WHERE { ?a P1 ?b . ?b P2 O2 . }"),
+    ("C", "SELECT * WHERE { S1 P1 ?b . ?b P2 ?c . }"),
+    ("C", "SELECT * WHERE { S1 P1 ?b . ?b P2 ?c . ?c P3 ?d . }"),
+    ("C", "SELECT * WHERE { ?a P1 ?b . ?b P2 ?c . ?c P3 O3 . }"),
+    ("C", "SELECT * WHERE { ?a P1 ?b . ?b P2 ?c . ?c P3 ?d . ?d P4 O4 . }"),
+    ("C", "SELECT ?a ?e WHERE { ?a P1 ?b . ?b P2 ?c . ?c P3 ?d . ?d P4 ?e . ?e P5 O5 . }"),
+    ("C", "SELECT ?b WHERE { S1 P1 ?b . ?b P2 ?c . ?c P3 ?d . }"),
+    ("F", "SELECT * WHERE { ?x P1 O1 . ?x P2 ?y . ?y P3 ?c . ?y P4 ?d . }"),
+    ("F", "SELECT * WHERE { ?x P1 O1 . ?x P2 ?a . ?x P3 ?y . ?y P4 ?c . ?y P5 ?d . }"),
+    ("F", "SELECT ?x ?y ?d WHERE { ?x P1 O1 . ?x P2 ?a . ?x P3 ?y . ?y P4 ?c . ?y P5 ?d . ?y P6 ?e . }"),
+    ("F", "SELECT * WHERE { ?x P1 O1 . ?x P2 ?a . ?x P3 ?b . ?x P4 ?y . ?y P5 ?c . ?y P6 ?d . ?y P7 O7 . }"),
+    ("F", "SELECT ?x ?y WHERE { ?x P1 O1 . ?x P2 ?a . ?x P3 ?b . ?x P4 ?y . ?y P5 ?c . ?y P6 ?d . "
+          "?y P7 O7 . ?d P8 ?f . }"),
+]
+
+
+class ConstantSampler:
+    """Per-predicate subjects/objects of a graph, for sampling query constants."""
+
+    def __init__(self, g: Graph):
+        order = np.argsort(g.p, kind="stable")
+        self.p_sorted = g.p[order]
+        self.s_sorted = g.s[order]
+        self.o_sorted = g.o[order]
+        self.preds = np.unique(self.p_sorted)
+        self.start = np.searchsorted(self.p_sorted, self.preds, side="left")
+        self.end = np.searchsorted(self.p_sorted, self.preds, side="right")
+        self.count = {int(p): int(e - b) for p, b, e in zip(self.preds, self.start, self.end)}
+        self.span = {int(p): (int(b), int(e)) for p, b, e in zip(self.preds, self.start, self.end)}
+
+    def usable_predicates(self):
+        return [int(p) for p in self.preds[:-1]]   # never the last predicate id
+
+    def obj(self, rng, p: int) -> int:
+        b, e = self.span[p]
+        return int(self.o_sorted[rng.integers(b, e)])
+
+    def subj(self, rng, p: int) -> int:
+        b, e = self.span[p]
+        return int(self.s_sorted[rng.integers(b, e)])
+
+
+def instantiate(template: str, cs: ConstantSampler, rng) -> str:
+    """Fills a template's placeholders with predicates and existing constants."""
+    preds = cs.usable_predicates()
+    rare = preds[len(preds) // 2:] or preds
+    pats = [t.strip() for t in template.split("{", 1)[1].rsplit("}", 1)[0].split(" . ") if t.strip()]
+    chosen = {}
+    for t in pats:
+        s, p, o = t.rstrip(" .").split()
+        k = p[1:]
+        bound = not (s.startswith("?") and o.startswith("?"))
+        pool = preds if bound else rare
+        chosen[k] = int(pool[rng.integers(0, len(pool))])
+    out = template
+    for k in sorted(chosen, key=lambda x: -int(x)):
+        p = chosen[k]
+        out = out.replace(f"O{k}", f"<{cs.obj(rng, p)}>").replace(f"S{k}", f"<{cs.subj(rng, p)}>")
+        out = out.replace(f"P{k}", f"<{p}>")
+    return out
+
+
+def query_mix(g: Graph, n_queries: int, seed: int = 0, cs: ConstantSampler | None = None,
+              mix=None):
+    """n_queries instantiated templates, round-robin over the 20 templates (or
+    drawn with the given per-shape weights, e.g. {"S": .6, "C": .3, "F": .1})."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cs = cs or ConstantSampler(g)
+    out = []
+    if mix is None:
+        for i in range(n_queries):
+            out.append(instantiate(TEMPLATES[i % len(TEMPLATES)][1], cs, rng))
+        return out
+    shapes = list(mix)
+    w = np.array([mix[s] for s in shapes], dtype=np.float64)
+    w /= w.sum()
+    by_shape = {s: [t for sh, t in TEMPLATES if sh == s] for s in shapes}
+    for _ in range(n_queries):
+        sh = shapes[rng.choice(len(shapes), p=w)]
+        ts = by_shape[sh]
+        out.append(instantiate(ts[rng.integers(0, len(ts))], cs, rng))
+    return out
+
+
 def star_query(pa: int = 3, pb: int = 7) -> str:
     """Two-pattern subject-subject star: (?x pa ?a . ?x pb ?b), SELECT *."""
     return f"SELECT * WHERE {{ ?x <{pa}> ?a . ?x <{pb}> ?b . }}"
