@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""VEDAS GB300 benchmark: the 4096-query mixed batch on the 100M-triple graph.
+
+One step = every query of the batch run through the core (select, join and
+index-swap kernels over the HBM-resident permutation indexes), results left
+in HBM.  `value` is queries/s over all ranks; `e2e` is the same through the
+C-ABI with every result downloaded to host memory inside the timed region.
+
+--impl reference times the reference path's CPU implementation (this
+project's restatement in oracle/, the reference's own build being x86-only
+here) on the host cores, on a bounded sample of the same batch.
+
+Multi-GPU: replicas only.  Every rank holds its own index and runs its own
+4096-query batch (weak scaling); ranks meet only at the barriers around the
+timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched queries/s"
+UNIT = "queries/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="plain", choices=["batch", "plain"])
+    ap.add_argument("--triples", type=int, default=100_000_000)
+    ap.add_argument("--entities", type=int, default=2_000_000)
+    ap.add_argument("--queries", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=256, help="queries per CPU-baseline step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        for row in csv.reader(io.StringIO(out)):
+            if len(row) < 9:
+                continue
+            try:
+                sm.append(float(row[1]))
+                smax.append(float(row[2]))
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for nm, v in zip(names, row[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ---------------------------------------------------------------------------
+def make_workload(args, rank: int):
+    from vedas_gb300 import workloads
+    g = workloads.graph_chain(n=args.triples, n_entities=args.entities, seed=args.seed)
+    cs = workloads.ConstantSampler(g)
+    queries = workloads.query_mix(g, args.queries, seed=args.seed + 1000 * rank, cs=cs)
+    return g, queries
+
+
+def run_plain(ix, queries, download=False):
+    """The reference's one-query-at-a-time loop (vdBench), on the GPU core."""
+    import vedas_gb300 as vg
+    rows = 0
+    d2h = 0
+    for q in queries:
+        r = ix.query(q)
+        rows += r.nrows
+        if download:
+            for c in r.columns():
+                d2h += c.nbytes
+        r.close()
+    return rows, d2h
+
+
+def run_batch(ix, queries, download=False):
+    import vedas_gb300 as vg
+    b = vg.Batch(ix, queries)
+    rows = b.run()
+    d2h = 0
+    if download:
+        for i in range(len(queries)):
+            for c in b.columns(i):
+                d2h += c.nbytes
+    b.close()
+    return rows, d2h
+
+
+def cpu_baseline_run(g, queries, sample: int, steps: int = 1):
+    """Times the oracle port (all host threads) on `sample` queries."""
+    from oracle import oracle_py
+    ox = oracle_py.OracleIndex(g.s, g.p, g.o)
+    qs = queries[:sample]
+    for q in qs[: min(8, len(qs))]:
+        ox.query(q)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        for q in qs:
+            ox.query(q)
+        times.append(time.perf_counter() - t0)
+    return len(qs), times, os.cpu_count()
+
+
+def bench_reference(args, rank, world, pg):
+    if rank != 0:
+        return
+    g, queries = make_workload(args, 0)
+    n, times, cores = cpu_baseline_run(g, queries, args.cpu_sample, steps=args.warmup + args.steps)
+    timed = times[args.warmup:] if len(times) > args.warmup else times
+    total = sum(timed)
+    value = n * len(timed) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(timed),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": f"mixed 20-template batch on the {args.triples // 1_000_000}M-triple "
+                               f"chain graph; each step a {n}-query sample of it",
+                   "triples": args.triples, "queries_per_step": n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{n} queries of the batch per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_ours(args, rank, world, local, pg):
+    import torch
+    import vedas_gb300 as vg
+
+    g, queries = make_workload(args, rank)
+    ctx = vg.Context(local, arena_bytes=0)
+    t0 = time.perf_counter()
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    ctx.sync()
+    build_s = time.perf_counter() - t0
+    # The core refuses queries on which the reference itself would read out of
+    # bounds or trip an assert; drop those before timing (counted below).
+    kept = []
+    for q in queries:
+        try:
+            ix.query(q).close()
+            kept.append(q)
+        except vg.VgError:
+            pass
+    refused = len(queries) - len(kept)
+    run = run_batch if args.mode == "batch" else run_plain
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+
+    for _ in range(args.warmup):
+        run(ix, kept)
+    # L2 (129 MB) is far smaller than the 100M-triple index (2.4 GB of data
+    # columns), so consecutive steps do not reuse each other's lines.
+    clocks = ClockSampler(local)
+    ctx.stats_reset(timing=True)
+    barrier(pg)
+    ctx.sync()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    rows = 0
+    for _ in range(args.steps):
+        r, _ = run(ix, kept)
+        rows += r
+    ev1.record(stream)
+    ctx.sync()
+    clk = clocks.stop()
+    barrier(pg)
+    step_ms = ev0.elapsed_time(ev1) / args.steps
+    launches = ctx.launches()
+    stats = ctx.stats()
+    step_ms_max = max_over_ranks(pg, step_ms)
+    total_q = sum_over_ranks(pg, float(len(kept)))
+    value = total_q / (step_ms_max / 1000.0)
+
+    # end to end: results copied to host memory inside the timed region
+    ctx.stats_reset(timing=False)
+    barrier(pg)
+    ctx.sync()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(args.steps):
+        _, b = run(ix, kept, download=True)
+        d2h += b
+    ctx.sync()
+    e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
+    e2e_value = total_q / e2e_s
+    h2d = sum(len(q) for q in kept)
+
+    peak, peak_kind = peak_hbm()
+    dom = max(stats.items(), key=lambda kv: kv[1][2]) if stats else None
+    roof = None
+    if dom:
+        name, (n_l, bytes_, ms) = dom
+        achieved = bytes_ / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+        tr = traffic_table().get(name)
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
+                "traffic": (tr * (bytes_ / n_l) if tr is not None else None),
+                "algorithmic_bytes_per_launch": bytes_ / max(n_l, 1), "launches": n_l,
+                "avg_launch_us": 1000.0 * ms / max(n_l, 1)}
+    kernels = {k: {"launches": v[0], "ms": round(v[2], 3), "GBps": round(v[1] / v[2] / 1e6, 1) if v[2] else None}
+               for k, v in stats.items()}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        n, times, cores = cpu_baseline_run(g, kept, args.cpu_sample)
+        cpu = {"value": n / times[-1], "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"first {n} queries of the batch, oracle restatement on host cores"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": f"{len(kept)}-query mixed batch (20 star/chain/snowflake templates, "
+                                   f"1-8 patterns) on the {args.triples // 1_000_000}M-triple chain graph",
+                       "mode": args.mode, "triples": args.triples, "entities": args.entities,
+                       "queries": len(kept), "queries_refused": refused,
+                       "result_rows_per_step": rows // max(args.steps, 1),
+                       "parallelism": f"replicas{world}", "l2": "inputs larger than L2",
+                       "index_build_s": round(build_s, 3)},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h // max(args.steps, 1)},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    ix.close()
+    ctx.close()
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        bench_reference(args, rank, world, pg)
+    else:
+        bench_ours(args, rank, world, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

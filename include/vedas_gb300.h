@@ -52,6 +52,17 @@ vg_status vg_ctx_sync(vg_ctx* ctx);
  * own work after the core's. */
 void* vg_ctx_stream(vg_ctx* ctx);
 
+/* Kernel accounting (no reference counterpart; the reference has only
+ * host-side chrono timers, src/QueryExecutor.h:60-77).  vg_stats_reset clears
+ * the counters and turns per-launch CUDA-event timing on or off; the query
+ * calls count every kernel launch with the algorithmic bytes it moves.
+ * vg_stats_get synchronizes and reports kernel i of vg_stats_count. */
+vg_status vg_stats_reset(vg_ctx* ctx, int timing);
+uint32_t vg_stats_count(vg_ctx* ctx);
+uint64_t vg_stats_launches(vg_ctx* ctx);
+vg_status vg_stats_get(vg_ctx* ctx, uint32_t i, const char** name, uint64_t* launches, double* bytes,
+                       double* ms);
+
 /* ---- index build (hot path a) ----------------------------------------- */
 typedef struct vg_index vg_index;
 

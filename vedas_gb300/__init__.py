@@ -59,6 +59,11 @@ def lib():
                                     ctypes.POINTER(ctypes.c_size_t)]),
             "vg_ctx_sync": (i32, [vp]),
             "vg_ctx_stream": (vp, [vp]),
+            "vg_stats_reset": (i32, [vp, i32]),
+            "vg_stats_count": (u32, [vp]),
+            "vg_stats_launches": (u64, [vp]),
+            "vg_stats_get": (i32, [vp, u32, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(u64),
+                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
             "vg_index_build": (i32, [vp, vp, vp, vp, u64, i32, i32, ctypes.POINTER(vp)]),
             "vg_index_free": (i32, [vp]),
             "vg_index_array": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(vp), ctypes.POINTER(pu32),
@@ -134,6 +139,24 @@ class Context:
     @property
     def stream(self) -> int:
         return lib().vg_ctx_stream(self.h) or 0
+
+    def stats_reset(self, timing: bool = False) -> None:
+        check(lib().vg_stats_reset(self.h, int(timing)))
+
+    def launches(self) -> int:
+        return int(lib().vg_stats_launches(self.h))
+
+    def stats(self) -> dict:
+        """{kernel: (launches, algorithmic bytes, total ms)} since the last reset."""
+        L = lib()
+        out = {}
+        for i in range(L.vg_stats_count(self.h)):
+            name = ctypes.c_char_p()
+            n, b, ms = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double()
+            check(L.vg_stats_get(self.h, i, ctypes.byref(name), ctypes.byref(n), ctypes.byref(b),
+                                 ctypes.byref(ms)))
+            out[name.value.decode()] = (n.value, b.value, ms.value)
+        return out
 
 
 class Index:

@@ -144,6 +144,32 @@ vg_status vg_ctx_sync(vg_ctx* ctx) {
 
 void* vg_ctx_stream(vg_ctx* ctx) { return ctx ? static_cast<void*>(ctx->c.stream) : nullptr; }
 
+vg_status vg_stats_reset(vg_ctx* ctx, int timing) {
+  if (!ctx) return VG_ERR_INVALID;
+  return guard([&] {
+    ctx->c.reset_stats();
+    ctx->c.timing = timing != 0;
+  });
+}
+
+uint32_t vg_stats_count(vg_ctx* ctx) { return ctx ? static_cast<uint32_t>(ctx->c.kstats.size()) : 0; }
+
+uint64_t vg_stats_launches(vg_ctx* ctx) { return ctx ? ctx->c.launches : 0; }
+
+vg_status vg_stats_get(vg_ctx* ctx, uint32_t i, const char** name, uint64_t* launches, double* bytes,
+                       double* ms) {
+  if (!ctx || i >= ctx->c.kstats.size()) return VG_ERR_INVALID;
+  return guard([&] {
+    ctx->c.collect_timing();
+    auto it = ctx->c.kstats.begin();
+    std::advance(it, i);
+    if (name) *name = it->first.c_str();
+    if (launches) *launches = it->second.launches;
+    if (bytes) *bytes = it->second.bytes;
+    if (ms) *ms = it->second.ms;
+  });
+}
+
 vg_status vg_index_build(vg_ctx* ctx, const uint32_t* s, const uint32_t* p, const uint32_t* o, uint64_t n,
                          int full_index, int inputs_on_device, vg_index** out) {
   if (!ctx || !out || (n && (!s || !p || !o))) return VG_ERR_INVALID;
@@ -152,6 +178,7 @@ vg_status vg_index_build(vg_ctx* ctx, const uint32_t* s, const uint32_t* p, cons
   h->ctx = ctx;
   vg_status st = guard([&] {
     h->st = std::make_unique<vedas::VedasStorage>(&ctx->c, s, p, o, n, inputs_on_device != 0, full_index != 0);
+    ctx->c.check_device_errors();
   });
   if (st == VG_OK) *out = h.release();
   return st;
@@ -262,7 +289,7 @@ vg_status vg_join(vg_ctx* ctx, const vg_ir* l, const vg_ir* r, vg_ir* out, uint3
       VG_CUDA(cudaMemcpyAsync(&first_last[0], o.cols[0], 4, cudaMemcpyDeviceToHost, ctx->c.stream));
       VG_CUDA(cudaMemcpyAsync(&first_last[1], o.cols[0] + o.nrows - 1, 4, cudaMemcpyDeviceToHost, ctx->c.stream));
     }
-    ctx->c.sync();
+    ctx->c.check_device_errors();
   });
 }
 
@@ -285,7 +312,7 @@ vg_status vg_swap(vg_ctx* ctx, vg_ir* ir, uint32_t col) {
     std::swap(r.cols[0], r.cols[col]);
     vg::sort_by_first(ctx->c, r);
     from_rel(r, ir);
-    ctx->c.sync();
+    ctx->c.check_device_errors();
   });
 }
 
@@ -296,7 +323,7 @@ vg_status vg_sort_rows(vg_ctx* ctx, vg_ir* ir) {
     vg::Rel r = to_rel(ir);
     vg::sort_rows(ctx->c, r);
     from_rel(r, ir);
-    ctx->c.sync();
+    ctx->c.check_device_errors();
   });
 }
 
@@ -338,7 +365,7 @@ vg_status vg_query(vg_ctx* ctx, vg_index* ix, const char* sparql, vg_result** ou
     res->rel = ir->release();
     res->ctx = ctx;
     res->log = ex.exe_log;
-    ctx->c.sync();
+    ctx->c.check_device_errors();
   });
   if (st == VG_OK) *out = res.release();
   return st;

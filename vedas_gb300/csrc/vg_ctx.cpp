@@ -100,6 +100,37 @@ size_t Arena::largest_free() const {
   return m;
 }
 
+cudaEvent_t Ctx::take_event() {
+  if (!event_pool.empty()) {
+    cudaEvent_t e = event_pool.back();
+    event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  VG_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+void Ctx::collect_timing() {
+  sync();
+  for (auto& kv : kstats) {
+    for (auto& pr : kv.second.pending) {
+      float ms = 0;
+      VG_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+      kv.second.ms += ms;
+      event_pool.push_back(pr.first);
+      event_pool.push_back(pr.second);
+    }
+    kv.second.pending.clear();
+  }
+}
+
+void Ctx::reset_stats() {
+  collect_timing();
+  launches = 0;
+  kstats.clear();
+}
+
 void Ctx::check_device_errors() {
   DeviceErrors h{};
   VG_CUDA(cudaMemcpyAsync(&h, d_err, sizeof(h), cudaMemcpyDeviceToHost, stream));

@@ -44,6 +44,16 @@ class Arena {
   mutable std::mutex mu_;
 };
 
+// Per-kernel accounting: launches, algorithmic bytes (the bytes the
+// operation must move, not what the kernel happens to move) and, when timing
+// is on, CUDA-event durations on the context stream.
+struct KernelStat {
+  uint64_t launches = 0;
+  double bytes = 0;
+  double ms = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -53,6 +63,33 @@ struct Ctx {
   // pinned staging for small device->host reads (sizes, first/last keys)
   uint64_t* h_small = nullptr;
   static constexpr int kSmallWords = 1024;
+
+  bool timing = false;
+  uint64_t launches = 0;
+  std::map<std::string, KernelStat> kstats;
+  std::vector<cudaEvent_t> event_pool;
+
+  // Wraps one kernel launch on `stream`.
+  template <typename F>
+  void launch(const char* name, double algo_bytes, F&& f) {
+    ++launches;
+    KernelStat& k = kstats[name];
+    k.launches++;
+    k.bytes += algo_bytes;
+    if (!timing) {
+      f();
+      return;
+    }
+    cudaEvent_t a = take_event(), b = take_event();
+    VG_CUDA(cudaEventRecord(a, stream));
+    f();
+    VG_CUDA(cudaEventRecord(b, stream));
+    k.pending.emplace_back(a, b);
+  }
+  cudaEvent_t take_event();
+  // Converts recorded event pairs into milliseconds (synchronizes).
+  void collect_timing();
+  void reset_stats();
 
   template <typename T>
   T* alloc(uint64_t n) {

@@ -141,7 +141,8 @@ void column_max3(Ctx& ctx, const uint32_t* a, const uint32_t* b, const uint32_t*
   Scratch<uint32_t> d(ctx, 3);
   VG_CUDA(cudaMemsetAsync(d.get(), 0, 3 * sizeof(uint32_t), ctx.stream));
   if (n) {
-    max3_kernel<<<grid_for(ctx, n, 8), kBlock, 0, ctx.stream>>>(a, b, c, n, d.get());
+    ctx.launch("column_max", 12.0 * n,
+               [&] { max3_kernel<<<grid_for(ctx, n, 8), kBlock, 0, ctx.stream>>>(a, b, c, n, d.get()); });
     VG_CUDA(cudaGetLastError());
   }
   VG_CUDA(cudaMemcpyAsync(out, d.get(), 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
@@ -159,7 +160,8 @@ void build_permutation(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const u
   const uint32_t sh1 = static_cast<uint32_t>(b2), sh0 = static_cast<uint32_t>(b1 + b2);
   uint64_t* keys = ctx.alloc<uint64_t>(n);
   uint64_t* keys_alt = ctx.alloc<uint64_t>(n);
-  pack_kernel<<<grid_for(ctx, n, 8), kBlock, 0, ctx.stream>>>(k0, k1, k2, n, sh0, sh1, keys);
+  ctx.launch("index_pack", 20.0 * n,
+             [&] { pack_kernel<<<grid_for(ctx, n, 8), kBlock, 0, ctx.stream>>>(k0, k1, k2, n, sh0, sh1, keys); });
   VG_CUDA(cudaGetLastError());
   const bool alt = radix_sort_u64(ctx, keys, keys_alt, nullptr, nullptr, n, b0 + b1 + b2, false);
   uint64_t* sorted = alt ? keys_alt : keys;
@@ -190,7 +192,9 @@ void build_permutation(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const u
   a.ticket = ticket.get();
   a.counts = counts.get();
   a.err = ctx.d_err;
-  unpack_rle_kernel<<<static_cast<unsigned>(a.tiles), kBlock, 0, ctx.stream>>>(a);
+  const double ub = 8.0 * n + 4.0 * n * ((a.col1 ? 1 : 0) + (a.col2 ? 1 : 0));
+  ctx.launch("index_unpack_rle", ub,
+             [&] { unpack_rle_kernel<<<static_cast<unsigned>(a.tiles), kBlock, 0, ctx.stream>>>(a); });
   VG_CUDA(cudaGetLastError());
   uint64_t hc[2];
   VG_CUDA(cudaMemcpyAsync(hc, counts.get(), sizeof(hc), cudaMemcpyDeviceToHost, ctx.stream));

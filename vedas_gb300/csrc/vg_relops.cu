@@ -284,7 +284,10 @@ void multi_copy(Ctx& ctx, const CopyPiece* pieces, int np) {
     ++a.np;
   }
   if (a.np == 0) return;
-  multi_copy_kernel<<<grid_for(ctx, a.start[a.np], 2), kBlock, 0, ctx.stream>>>(a);
+  double bytes = 0;
+  for (int k = 0; k < a.np; ++k) bytes += 8.0 * a.p[k].len;
+  ctx.launch("select_copy", bytes,
+             [&] { multi_copy_kernel<<<grid_for(ctx, a.start[a.np], 2), kBlock, 0, ctx.stream>>>(a); });
   VG_CUDA(cudaGetLastError());
 }
 
@@ -307,11 +310,14 @@ uint64_t unique_rows(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, 
   a.ticket = ticket.get();
   a.count = count.get();
   a.err = ctx.d_err;
-  unique_kernel<<<static_cast<unsigned>(a.tiles), kBlock, 0, ctx.stream>>>(a);
+  ctx.launch("unique_compact", 4.0 * n * ncols,
+             [&] { unique_kernel<<<static_cast<unsigned>(a.tiles), kBlock, 0, ctx.stream>>>(a); });
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaMemcpyAsync(ctx.h_small, count.get(), sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.sync();
-  return ctx.h_small[0];
+  const uint64_t kept = ctx.h_small[0];
+  ctx.kstats["unique_compact"].bytes += 4.0 * kept * ncols;
+  return kept;
 }
 
 void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
@@ -327,12 +333,17 @@ void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
   }
   Scratch<uint32_t> lo(ctx, l.nrows), cnt(ctx, l.nrows);
   const unsigned cgrid = static_cast<unsigned>(div_up(l.nrows, kBlock));
+  const double cbytes = 4.0 * nk * (l.nrows + r.nrows);
   if (two_keys) {
     KeyOf<true> kl{l.cols[0], l.cols[1]}, kr{r.cols[0], r.cols[1]};
-    join_count_kernel<true><<<cgrid, kBlock, 0, ctx.stream>>>(kl, l.nrows, kr, r.nrows, lo.get(), cnt.get());
+    ctx.launch("join_count", cbytes, [&] {
+      join_count_kernel<true><<<cgrid, kBlock, 0, ctx.stream>>>(kl, l.nrows, kr, r.nrows, lo.get(), cnt.get());
+    });
   } else {
     KeyOf<false> kl{l.cols[0], nullptr}, kr{r.cols[0], nullptr};
-    join_count_kernel<false><<<cgrid, kBlock, 0, ctx.stream>>>(kl, l.nrows, kr, r.nrows, lo.get(), cnt.get());
+    ctx.launch("join_count", cbytes, [&] {
+      join_count_kernel<false><<<cgrid, kBlock, 0, ctx.stream>>>(kl, l.nrows, kr, r.nrows, lo.get(), cnt.get());
+    });
   }
   VG_CUDA(cudaGetLastError());
   const uint64_t tiles = div_up(l.nrows, kTileRows);
@@ -340,8 +351,10 @@ void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
   Scratch<uint32_t> ticket(ctx, 1);
   VG_CUDA(cudaMemsetAsync(status.get(), 0, tiles * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(uint32_t), ctx.stream));
-  scan_counts_kernel<<<static_cast<unsigned>(tiles), kBlock, 0, ctx.stream>>>(
-      cnt.get(), offs.get(), l.nrows, status.get(), ticket.get(), total.get(), tiles, ctx.d_err);
+  ctx.launch("join_scan", 12.0 * l.nrows, [&] {
+    scan_counts_kernel<<<static_cast<unsigned>(tiles), kBlock, 0, ctx.stream>>>(
+        cnt.get(), offs.get(), l.nrows, status.get(), ticket.get(), total.get(), tiles, ctx.d_err);
+  });
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaMemcpyAsync(ctx.h_small, total.get(), sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.sync();
@@ -359,7 +372,9 @@ void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
   for (uint32_t c = 0; c < ncols; ++c) a.oc[c] = out.cols[c];
   a.nlc = l.ncols;
   a.nrc = r.ncols - nk;
-  join_write_kernel<<<static_cast<unsigned>(div_up(t, kTileRows)), kBlock, 0, ctx.stream>>>(a);
+  ctx.launch("join_write", 4.0 * t * (2.0 * ncols - 1), [&] {
+    join_write_kernel<<<static_cast<unsigned>(div_up(t, kTileRows)), kBlock, 0, ctx.stream>>>(a);
+  });
   VG_CUDA(cudaGetLastError());
 }
 
@@ -372,7 +387,8 @@ void gather_cols(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, uint
     g.out[c] = out[c];
   }
   g.ncols = ncols;
-  gather_kernel<<<grid_for(ctx, n, 4), kBlock, 0, ctx.stream>>>(perm, n, g);
+  ctx.launch("gather", static_cast<double>(n) * (4.0 + 8.0 * ncols),
+             [&] { gather_kernel<<<grid_for(ctx, n, 4), kBlock, 0, ctx.stream>>>(perm, n, g); });
   VG_CUDA(cudaGetLastError());
 }
 

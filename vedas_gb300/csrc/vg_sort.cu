@@ -157,8 +157,11 @@ void launch_pass(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uint32_t*
     attr_set = true;
   }
   const uint64_t tiles = div_up(n, kTile);
-  onesweep_kernel<K, HAS_V, IOTA><<<static_cast<unsigned>(tiles), kBlock, smem, ctx.stream>>>(
-      kin, kout, vin, vout, n, shift, bases, status, ticket, ctx.d_err);
+  const double bytes = static_cast<double>(n) * (2 * sizeof(K) + (HAS_V ? (IOTA ? 4 : 8) : 0));
+  ctx.launch("radix_onesweep", bytes, [&] {
+    onesweep_kernel<K, HAS_V, IOTA><<<static_cast<unsigned>(tiles), kBlock, smem, ctx.stream>>>(
+        kin, kout, vin, vout, n, shift, bases, status, ticket, ctx.d_err);
+  });
   VG_CUDA(cudaGetLastError());
 }
 
@@ -178,7 +181,9 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
   const uint64_t gmax = static_cast<uint64_t>(ctx.num_sms) * 8;
   if (grid > gmax) grid = gmax;
   if (grid < 1) grid = 1;
-  radix_hist_kernel<K><<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(keys, n, passes, hist.get());
+  ctx.launch("radix_histogram", static_cast<double>(n) * sizeof(K), [&] {
+    radix_hist_kernel<K><<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(keys, n, passes, hist.get());
+  });
   VG_CUDA(cudaGetLastError());
   std::vector<unsigned long long> h(passes * kRadix);
   VG_CUDA(cudaMemcpyAsync(h.data(), hist.get(), h.size() * sizeof(unsigned long long),
@@ -200,7 +205,7 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
   }
   if (todo.empty()) {
     if (has_v && vals_iota) {
-      iota_kernel<<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(vals, n);
+      ctx.launch("iota", 4.0 * n, [&] { iota_kernel<<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(vals, n); });
       VG_CUDA(cudaGetLastError());
     }
     return false;
@@ -254,7 +259,7 @@ void fill_iota(Ctx& ctx, uint32_t* out, uint64_t n) {
   uint64_t grid = div_up(n, kBlock * 8);
   const uint64_t gmax = static_cast<uint64_t>(ctx.num_sms) * 8;
   if (grid > gmax) grid = gmax;
-  iota_kernel<<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(out, n);
+  ctx.launch("iota", 4.0 * n, [&] { iota_kernel<<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(out, n); });
   VG_CUDA(cudaGetLastError());
 }
 
