@@ -186,6 +186,31 @@ void vg_result_log(const vg_result* r, uint32_t i, uint32_t* op, uint64_t* p1, u
                    uint64_t* p3);
 vg_status vg_result_free(vg_result* r);
 
+/* ---- batched execution -------------------------------------------------- */
+typedef struct vg_batch vg_batch;
+
+/* Runs nq queries together.  Each query follows exactly the job sequence and
+ * semantics of vg_query (QueryExecutor::query + QueryPlan::execute); queries
+ * advance one job per wave and every wave's sorts, selects and joins run as
+ * batched launches.  Replaces the reference's one-query-at-a-time loop
+ * (vdBench, src/VedasBench.cu:144-176).  A query the core refuses gets its
+ * own status; the others complete. */
+vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq,
+                       vg_batch** out);
+uint32_t vg_batch_size(const vg_batch* b);
+uint32_t vg_batch_waves(const vg_batch* b);
+vg_status vg_batch_query_status(const vg_batch* b, uint32_t q);
+const char* vg_batch_query_error(const vg_batch* b, uint32_t q);
+uint32_t vg_batch_ncols(const vg_batch* b, uint32_t q);
+uint64_t vg_batch_nrows(const vg_batch* b, uint32_t q);
+const char* vg_batch_header(const vg_batch* b, uint32_t q, uint32_t c);
+const uint32_t* vg_batch_column_device(const vg_batch* b, uint32_t q, uint32_t c);
+vg_status vg_batch_download(const vg_batch* b, uint32_t q, uint32_t c, uint32_t* host);
+uint32_t vg_batch_nlog(const vg_batch* b, uint32_t q);
+void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint64_t* p1, uint64_t* p2,
+                  uint64_t* p3);
+vg_status vg_batch_free(vg_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

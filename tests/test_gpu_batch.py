@@ -1,0 +1,79 @@
+"""Batched multi-query execution: every query's result (headers, rows in
+order, execution log) equals the oracle's and the one-query-at-a-time path's."""
+import numpy as np
+import pytest
+
+from oracle import oracle_py
+from vedas_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("graph,nq", [("star", 300), ("chain", 400)])
+def test_batch_matches_oracle_and_plain(ctx, graph, nq):
+    import vedas_gb300 as vg
+    if graph == "star":
+        g = workloads.graph_small_star(n=200_000, n_subjects=10_000, seed=4)
+    else:
+        g = workloads.graph_chain(n=400_000, n_entities=40_000, seed=4)
+    qs = workloads.query_mix(g, nq, seed=5)
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    ref = oracle_py.OracleIndex(g.s, g.p, g.o)
+    b = vg.Batch(ix, qs)
+    assert b.waves >= 1
+    ok = 0
+    for i, q in enumerate(qs):
+        r = ref.query(q)
+        if r.status != 0:
+            assert b.status(i) != 0
+            continue
+        assert b.status(i) == 0, b.error(i)
+        assert b.headers(i) == r.headers
+        for a, c in zip(b.columns(i), r.columns):
+            np.testing.assert_array_equal(a, c)
+        assert [x[:4] for x in b.log(i)] == [x[:4] for x in r.log]
+        ok += 1
+    assert ok > 0.9 * nq
+    # the same queries one at a time give the same rows
+    for i in range(0, nq, 37):
+        if b.status(i) != 0:
+            continue
+        res = ix.query(qs[i])
+        for a, c in zip(res.columns(), b.columns(i)):
+            np.testing.assert_array_equal(a, c)
+    b.close()
+    ix.close()
+
+
+def test_batch_isolates_refused_queries(ctx):
+    import vedas_gb300 as vg
+    g = workloads.graph_small_star(n=20_000, n_subjects=1_000, seed=6)
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    qs = [workloads.star_query(3, 7), "SELECT * WHERE { ?x ?p ?o . }", "not a query",
+          workloads.star_query(2, 5)]
+    b = vg.Batch(ix, qs)
+    assert b.status(0) == 0 and b.status(3) == 0
+    assert b.status(1) != 0 and b.status(2) != 0
+    ref = oracle_py.OracleIndex(g.s, g.p, g.o)
+    for i in (0, 3):
+        r = ref.query(qs[i])
+        for a, c in zip(b.columns(i), r.columns):
+            np.testing.assert_array_equal(a, c)
+    b.close()
+    ix.close()
+
+
+def test_batch_empty_and_single(ctx):
+    import vedas_gb300 as vg
+    g = workloads.graph_small_star(n=5_000, n_subjects=500, seed=7)
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    b = vg.Batch(ix, [])
+    assert b.run() == 0
+    b.close()
+    q = workloads.star_query(1, 2)
+    b = vg.Batch(ix, [q])
+    r = oracle_py.OracleIndex(g.s, g.p, g.o).query(q)
+    for a, c in zip(b.columns(0), r.columns):
+        np.testing.assert_array_equal(a, c)
+    b.close()
+    ix.close()

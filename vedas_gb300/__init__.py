@@ -91,6 +91,20 @@ def lib():
             "vg_result_log": (None, [vp, u32, pu32, ctypes.POINTER(u64), ctypes.POINTER(u64),
                                      ctypes.POINTER(u64)]),
             "vg_result_free": (i32, [vp]),
+            "vg_batch_run": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(vp)]),
+            "vg_batch_size": (u32, [vp]),
+            "vg_batch_waves": (u32, [vp]),
+            "vg_batch_query_status": (i32, [vp, u32]),
+            "vg_batch_query_error": (ctypes.c_char_p, [vp, u32]),
+            "vg_batch_ncols": (u32, [vp, u32]),
+            "vg_batch_nrows": (u64, [vp, u32]),
+            "vg_batch_header": (ctypes.c_char_p, [vp, u32, u32]),
+            "vg_batch_column_device": (vp, [vp, u32, u32]),
+            "vg_batch_download": (i32, [vp, u32, u32, pu32]),
+            "vg_batch_nlog": (u32, [vp, u32]),
+            "vg_batch_log": (None, [vp, u32, u32, pu32, ctypes.POINTER(u64), ctypes.POINTER(u64),
+                                    ctypes.POINTER(u64)]),
+            "vg_batch_free": (i32, [vp]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -254,6 +268,70 @@ class Result:
             L.vg_result_log(self.h, i, ctypes.byref(op), ctypes.byref(p1), ctypes.byref(p2), ctypes.byref(p3))
             recs.append((self.OPS[op.value], p1.value, p2.value, p3.value))
         return recs
+
+
+class Batch:
+    """Many queries executed together (vg_batch_run)."""
+
+    OPS = Result.OPS
+
+    def __init__(self, ix: "Index", queries):
+        self.ix = ix
+        self.n = len(queries)
+        arr = (ctypes.c_char_p * self.n)(*[q.encode() for q in queries])
+        h = ctypes.c_void_p()
+        check(lib().vg_batch_run(ix.ctx.h, ix.h, arr, self.n, ctypes.byref(h)))
+        self.h = h
+
+    def run(self) -> int:
+        """Total result rows (the batch already ran in the constructor)."""
+        L = lib()
+        return sum(int(L.vg_batch_nrows(self.h, q)) for q in range(self.n))
+
+    @property
+    def waves(self) -> int:
+        return int(lib().vg_batch_waves(self.h))
+
+    def status(self, q: int) -> int:
+        return int(lib().vg_batch_query_status(self.h, q))
+
+    def error(self, q: int) -> str:
+        return lib().vg_batch_query_error(self.h, q).decode()
+
+    def headers(self, q: int):
+        L = lib()
+        return [L.vg_batch_header(self.h, q, c).decode() for c in range(L.vg_batch_ncols(self.h, q))]
+
+    def nrows(self, q: int) -> int:
+        return int(lib().vg_batch_nrows(self.h, q))
+
+    def columns(self, q: int):
+        L = lib()
+        n = self.nrows(q)
+        out = []
+        for c in range(L.vg_batch_ncols(self.h, q)):
+            a = np.zeros(n, dtype=np.uint32)
+            if n:
+                check(L.vg_batch_download(self.h, q, c, _p32(a)))
+            out.append(a)
+        return out
+
+    def log(self, q: int):
+        L = lib()
+        recs = []
+        for i in range(L.vg_batch_nlog(self.h, q)):
+            op, p1, p2, p3 = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+            L.vg_batch_log(self.h, q, i, ctypes.byref(op), ctypes.byref(p1), ctypes.byref(p2), ctypes.byref(p3))
+            recs.append((self.OPS[op.value], p1.value, p2.value, p3.value))
+        return recs
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vg_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 class Relation:

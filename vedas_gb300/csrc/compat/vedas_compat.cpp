@@ -107,11 +107,14 @@ void FullRelationIR::removeColumn(size_t i) {  // src/FullRelationIR.cu:729-736
 }
 
 void FullRelationIR::removeColumn(size_t i, const std::string& maintain_var) {  // :738-745
+  if (removeColumnDeferSort(i, maintain_var)) sortByFirstColumn();
+}
+
+bool FullRelationIR::removeColumnDeferSort(size_t i, const std::string& maintain_var) {
   removeColumn(i);
-  if (i == 0) {
-    swapColumn(0, getColumnId(maintain_var));
-    sortByFirstColumn();
-  }
+  if (i != 0) return false;
+  swapColumn(0, getColumnId(maintain_var));
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -565,6 +568,24 @@ SelectQueryJob::~SelectQueryJob() { delete intermediateResult; }
 
 int SelectQueryJob::startJob(int gpu) {
   gpuId = gpu;
+  SelectWork w;
+  prepare(w);
+  if (w.unique) {
+    const uint32_t* in[1] = {w.uniq_src};
+    uint32_t* out[1] = {w.ir->getRelationRawPointer(0)};
+    finishUnique(w, vg::unique_rows(*ex->ctx, in, out, 1, w.uniq_n));
+  } else if (!w.pieces.empty()) {
+    vg::multi_copy(*ex->ctx, w.pieces.data(), static_cast<int>(w.pieces.size()));
+  }
+  return 0;
+}
+
+void SelectQueryJob::finishUnique(SelectWork& w, uint64_t kept) {
+  w.ir->ctx()->arena.shrink(w.ir->getRelationRawPointer(0), kept * sizeof(uint32_t));
+  w.ir->rel().nrows = kept;
+}
+
+void SelectQueryJob::prepare(SelectWork& w) {
   VedasStorage* st = ex->storage;
   vg::Ctx* ctx = ex->ctx;
   TYPEID_HOST_VEC* l1v = st->getPredicateIndexValues();
@@ -582,8 +603,9 @@ int SelectQueryJob::startJob(int gpu) {
     const size_t rows = r2.second - r2.first;
     auto* ir = new FullRelationIR(ctx, 1, rows);
     ir->setHeader(0, variables[0], false);
-    vg::CopyPiece pc{ddata + r2.first, ir->getRelationRawPointer(0), rows};
-    vg::multi_copy(*ctx, &pc, 1);
+    intermediateResult = ir;
+    w.ir = ir;
+    if (rows) w.pieces.push_back({ddata + r2.first, ir->getRelationRawPointer(0), rows});
     ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), rows, 1));
     if (ex->variables_bound.count(variables[0]) > 0) {
       if (rows == 0) QueryExecutor::updateBoundDict(&ex->variables_bound, variables[0], 0, 0);
@@ -591,8 +613,7 @@ int SelectQueryJob::startJob(int gpu) {
         QueryExecutor::updateBoundDict(&ex->variables_bound, variables[0], (*data)[r2.first],
                                        (*data)[r2.second - 1]);
     }
-    intermediateResult = ir;
-    return 0;
+    return;
   }
   // two variables: level-2 data ps_data (PSO) or po_data (POS)
   TYPEID_HOST_VEC* l2d = pos_index ? st->getPOdata() : st->getPSdata();
@@ -618,17 +639,16 @@ int SelectQueryJob::startJob(int gpu) {
     const size_t row = second - first;
     auto* ir = new FullRelationIR(ctx, 1, row);
     ir->setHeader(0, variables[0], false);
+    intermediateResult = ir;
+    w.ir = ir;
     if (row > 0) {
       // copy + adjacent unique fused: compact straight from the index slice
-      const uint32_t* in[1] = {dl2d + first};
-      uint32_t* out[1] = {ir->getRelationRawPointer(0)};
-      const uint64_t kept = vg::unique_rows(*ctx, in, out, 1, row);
-      ctx->arena.shrink(out[0], kept * sizeof(uint32_t));
-      ir->rel().nrows = kept;
+      w.unique = true;
+      w.uniq_src = dl2d + first;
+      w.uniq_n = row;
     }
     ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), row, 1));
-    intermediateResult = ir;
-    return 0;
+    return;
   }
   size_t total = 0;
   std::vector<std::pair<size_t, size_t>> up;
@@ -637,18 +657,17 @@ int SelectQueryJob::startJob(int gpu) {
   auto* ir = new FullRelationIR(ctx, 2, total);
   ir->setHeader(0, variables[0], false);
   ir->setHeader(1, variables[1], false);
+  intermediateResult = ir;
+  w.ir = ir;
   ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), total, 2));
-  std::vector<vg::CopyPiece> pcs;
   for (size_t i = 0; i < up.size(); ++i) {
     if (up[i].second < up[i].first) throw ReferenceUB("negative upload interval");
     const size_t len = up[i].second - up[i].first;
     if (offs[i] + len > total) throw ReferenceUB("upload interval past the relation");
-    pcs.push_back({dl2d + up[i].first, ir->getRelationRawPointer(0) + offs[i], len});
-    pcs.push_back({ddata + up[i].first, ir->getRelationRawPointer(1) + offs[i], len});
+    if (!len) continue;
+    w.pieces.push_back({dl2d + up[i].first, ir->getRelationRawPointer(0) + offs[i], len});
+    w.pieces.push_back({ddata + up[i].first, ir->getRelationRawPointer(1) + offs[i], len});
   }
-  vg::multi_copy(*ctx, pcs.data(), static_cast<int>(pcs.size()));
-  intermediateResult = ir;
-  return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -667,6 +686,68 @@ int JoinQueryJob::startJob(int gpu) {
 }
 
 IR* JoinQueryJob::join(FullRelationIR* lir, FullRelationIR* rir) {
+  (void)lir;
+  (void)rir;
+  JoinWork w;
+  prepare(w);
+  if (w.empty) return intermediateResult;
+  if (w.sortL) w.lir->sortByFirstColumn();
+  if (w.sortR) w.rir->sortByFirstColumn();
+  vg::Rel joined;
+  vg::join(*ex->ctx, w.lir->rel(), w.rir->rel(), false, joined);
+  TYPEID fl[2] = {0, 0};
+  std::vector<TYPEID> c0;
+  if (joined.nrows > 0) {
+    VG_CUDA(cudaMemcpyAsync(&fl[0], joined.cols[0], 4, cudaMemcpyDeviceToHost, ex->ctx->stream));
+    VG_CUDA(cudaMemcpyAsync(&fl[1], joined.cols[0] + joined.nrows - 1, 4, cudaMemcpyDeviceToHost,
+                            ex->ctx->stream));
+    if (joined.nrows > 2 && joined.nrows < 100) {
+      c0.resize(joined.nrows);
+      VG_CUDA(cudaMemcpyAsync(c0.data(), joined.cols[0], joined.nrows * 4, cudaMemcpyDeviceToHost,
+                              ex->ctx->stream));
+    }
+    ex->ctx->sync();
+  }
+  finish(w, joined, fl[0], fl[1], &c0);
+  return intermediateResult;
+}
+
+void JoinQueryJob::setHeaders(JoinWork& w, FullRelationIR* out) {
+  const size_t ls = w.lir->getColumnNum(), rs = w.rir->getColumnNum();
+  size_t h = 0;
+  out->setHeader(h++, w.lir->getHeader(0), w.lir->getIsPredicate(0));
+  for (size_t i = 1; i < ls; ++i) out->setHeader(h++, w.lir->getHeader(i), w.lir->getIsPredicate(i));
+  for (size_t i = 1; i < rs; ++i) out->setHeader(h++, w.rir->getHeader(i), w.rir->getIsPredicate(i));
+}
+
+void JoinQueryJob::finish(JoinWork& w, vg::Rel& joined, TYPEID first, TYPEID last,
+                          const std::vector<TYPEID>* col0) {
+  auto* out = new FullRelationIR(ex->ctx, w.new_col_num, 0);
+  out->adopt(joined);
+  setHeaders(w, out);
+  intermediateResult = out;
+  const size_t result_size = out->size();
+  ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP, w.lir->getHeaders("") + " x " + w.rir->getHeaders(""),
+                                         w.lir->size(), w.rir->size(), result_size));
+  if (QueryExecutor::ENABLE_UPDATE_BOUND_AFTER_JOIN) {
+    if (result_size > 0) {
+      QueryExecutor::updateBoundDict(&ex->variables_bound, joinVariable, first, last);
+      if (!lastJoinForVar && result_size > 2 && result_size < 100) {
+        if (!col0 || col0->size() != result_size) throw vg::Error(VG_ERR_INVALID, "join: column 0 not staged");
+        size_t b[4];
+        QueryExecutor::eifBounds(col0->data(), result_size, b);
+        ex->empty_interval_dict.updateBound(joinVariable, b[0], b[1], b[2], b[3]);
+      }
+    } else {
+      QueryExecutor::updateBoundDict(&ex->variables_bound, joinVariable, 0, 0);
+    }
+  }
+}
+
+void JoinQueryJob::prepare(JoinWork& w) {
+  auto* lir = dynamic_cast<FullRelationIR*>(leftJob->getIR());
+  auto* rir = dynamic_cast<FullRelationIR*>(rightJob->getIR());
+  if (!lir || !rir) throw vg::Error(VG_ERR_INVALID, "join operands are not relations");
   if (lir->size() > rir->size()) std::swap(lir, rir);
   std::vector<std::string> jvs;
   {
@@ -685,63 +766,48 @@ IR* JoinQueryJob::join(FullRelationIR* lir, FullRelationIR* rir) {
   const std::string& jv = jvs[0];
   auto& counter = *query_variable_counter;
   size_t new_col_num = lir->getColumnNum() + rir->getColumnNum() - 1;
+  // Pruning (src/JoinQueryJob.cu:136-155).  Removing column 0 re-sorts the
+  // relation by the join variable; that sort is deferred to the caller.
+  bool sortL = false, sortR = false;
   for (int i = static_cast<int>(lir->getColumnNum()) - 1; i >= 0; --i)
     if (counter[lir->getHeader(i)] == 0 && lir->getHeader(i) != jv) {
-      lir->removeColumn(static_cast<size_t>(i), jv);
+      sortL = lir->removeColumnDeferSort(static_cast<size_t>(i), jv) || sortL;
       new_col_num -= 1;
     }
   for (int i = static_cast<int>(rir->getColumnNum()) - 1; i >= 0; --i)
     if (counter[rir->getHeader(i)] == 0 && rir->getHeader(i) != jv) {
-      rir->removeColumn(static_cast<size_t>(i), jv);
+      sortR = rir->removeColumnDeferSort(static_cast<size_t>(i), jv) || sortR;
       new_col_num -= 1;
     }
   counter[jv] -= 1;
+  // Implicit index swaps (src/JoinQueryJob.cu:162-180).
   const size_t lj = lir->getColumnId(jv), rj = rir->getColumnId(jv);
   if (lj != 0) {
     lir->swapColumn(0, lj);
-    lir->sortByFirstColumn();
+    sortL = true;
     ex->exe_log.push_back(ExecuteLogRecord(gpuId, SWAP_OP, "", lir->size(), lir->getColumnNum()));
   }
   if (rj != 0) {
     rir->swapColumn(0, rj);
-    rir->sortByFirstColumn();
+    sortR = true;
     ex->exe_log.push_back(ExecuteLogRecord(gpuId, SWAP_OP, "", rir->size(), rir->getColumnNum()));
   }
-  const size_t ls = lir->getColumnNum(), rs = rir->getColumnNum();
-  auto set_headers = [&](FullRelationIR* out) {
-    size_t h = 0;
-    out->setHeader(h++, lir->getHeader(0), lir->getIsPredicate(0));
-    for (size_t i = 1; i < ls; ++i) out->setHeader(h++, lir->getHeader(i), lir->getIsPredicate(i));
-    for (size_t i = 1; i < rs; ++i) out->setHeader(h++, rir->getHeader(i), rir->getIsPredicate(i));
-  };
-  const std::string detail = lir->getHeaders("") + " x " + rir->getHeaders("");
+  w.lir = lir;
+  w.rir = rir;
+  w.sortL = sortL;
+  w.sortR = sortR;
+  w.new_col_num = new_col_num;
+  w.empty = false;
   if (lir->size() == 0 || rir->size() == 0) {
+    // Output decided on the host; the operands' re-sorts cannot be observed.
+    w.empty = true;
+    w.sortL = w.sortR = false;
     auto* out = new FullRelationIR(ex->ctx, new_col_num, 0);
-    set_headers(out);
-    ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP, detail, lir->size(), rir->size(), 0));
-    return out;
+    setHeaders(w, out);
+    intermediateResult = out;
+    ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP, lir->getHeaders("") + " x " + rir->getHeaders(""),
+                                           lir->size(), rir->size(), 0));
   }
-  vg::Rel joined;
-  vg::join(*ex->ctx, lir->rel(), rir->rel(), false, joined);
-  auto* out = new FullRelationIR(ex->ctx, new_col_num, 0);
-  out->adopt(joined);
-  set_headers(out);
-  const size_t result_size = out->size();
-  ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP, detail, lir->size(), rir->size(), result_size));
-  if (QueryExecutor::ENABLE_UPDATE_BOUND_AFTER_JOIN) {
-    if (result_size > 0) {
-      TYPEID fl[2];
-      const TYPEID* c0 = out->getRelationRawPointer(0);
-      VG_CUDA(cudaMemcpyAsync(&fl[0], c0, 4, cudaMemcpyDeviceToHost, ex->ctx->stream));
-      VG_CUDA(cudaMemcpyAsync(&fl[1], c0 + result_size - 1, 4, cudaMemcpyDeviceToHost, ex->ctx->stream));
-      ex->ctx->sync();
-      QueryExecutor::updateBoundDict(&ex->variables_bound, joinVariable, fl[0], fl[1]);
-      if (!lastJoinForVar && result_size > 2 && result_size < 100) ex->eifScan(out, joinVariable);
-    } else {
-      QueryExecutor::updateBoundDict(&ex->variables_bound, joinVariable, 0, 0);
-    }
-  }
-  return out;
 }
 
 // ---------------------------------------------------------------------------
@@ -752,16 +818,37 @@ IndexSwapJob::IndexSwapJob(QueryExecutor* e, QueryJob* before, std::string v)
 
 int IndexSwapJob::startJob(int gpu) {
   gpuId = gpu;
+  FullRelationIR* ir = prepare();
+  ir->sortByFirstColumn();
+  std::vector<TYPEID> c0;
+  if (ir->size() > 2 && ir->size() < 100) {
+    c0.resize(ir->size());
+    vg::download(*ex->ctx, ir->getRelationRawPointer(0), ir->size(), c0.data());
+  }
+  finish(&c0);
+  return 0;
+}
+
+FullRelationIR* IndexSwapJob::prepare() {
   auto* ir = dynamic_cast<FullRelationIR*>(beforeJob->getIR());
   if (!ir) throw vg::Error(VG_ERR_INVALID, "swap operand is not a relation");
-  const size_t c = ir->getColumnId(swapVar);
-  ir->swapColumn(0, c);
-  ir->sortByFirstColumn();
-  ex->exe_log.push_back(ExecuteLogRecord(gpuId, SWAP_OP, ir->getHeader(0) + " <-> " + ir->getHeader(c),
-                                         ir->size(), ir->getColumnNum()));
-  if (ir->size() > 2 && ir->size() < 100) ex->eifScan(ir, ir->getHeader(0));
+  swapped_col = ir->getColumnId(swapVar);
+  ir->swapColumn(0, swapped_col);
   intermediateResult = ir;
-  return 0;
+  return ir;
+}
+
+void IndexSwapJob::finish(const std::vector<TYPEID>* col0) {
+  auto* ir = dynamic_cast<FullRelationIR*>(intermediateResult);
+  ex->exe_log.push_back(ExecuteLogRecord(gpuId, SWAP_OP,
+                                         ir->getHeader(0) + " <-> " + ir->getHeader(swapped_col), ir->size(),
+                                         ir->getColumnNum()));
+  if (ir->size() > 2 && ir->size() < 100) {
+    if (!col0 || col0->size() != ir->size()) throw vg::Error(VG_ERR_INVALID, "swap: column 0 not staged");
+    size_t b[4];
+    QueryExecutor::eifBounds(col0->data(), ir->size(), b);
+    ex->empty_interval_dict.updateBound(ir->getHeader(0), b[0], b[1], b[2], b[3]);
+  }
 }
 
 TransferJob::TransferJob(size_t, size_t, int src, int dest, QueryJob* j)
@@ -791,16 +878,24 @@ void QueryPlan::pushJob(QueryJob* job) {
   if (auto* jj = dynamic_cast<JoinQueryJob*>(job)) query_variable_counter[jj->getJoinVariable()] += 1;
 }
 
-void QueryPlan::execute(SparqlResult& sr) {
+void QueryPlan::beginExecution() {
   for (const std::string& v : select_variables) query_variable_counter[v] = ULONG_MAX;
-  for (QueryJob* job : jobs) {
+  for (QueryJob* job : jobs)
     if (auto* jj = dynamic_cast<JoinQueryJob*>(job)) jj->setQueryVarCounter(&query_variable_counter);
-    job->startJob(0);
-  }
+}
+
+FullRelationIR* QueryPlan::project() {
   auto* res = dynamic_cast<FullRelationIR*>(jobs.back()->getIR());
   for (int i = static_cast<int>(res->getColumnNum()) - 1; i >= 1; --i)
     if (query_variable_counter[res->getHeader(static_cast<size_t>(i))] == 0)
       res->removeColumn(static_cast<size_t>(i));
+  return res;
+}
+
+void QueryPlan::execute(SparqlResult& sr) {
+  beginExecution();
+  for (QueryJob* job : jobs) job->startJob(0);
+  FullRelationIR* res = project();
   res->removeDuplicate();
   sr.setResult(res);
 }

@@ -107,6 +107,9 @@ class FullRelationIR : public IR {
   void swapColumn(size_t i, size_t j);
   void removeColumn(size_t i);
   void removeColumn(size_t i, const std::string& maintain_var);
+  // removeColumn(i, maintain_var) without its re-sort; true when the caller
+  // must still sort by column 0 (i == 0).
+  bool removeColumnDeferSort(size_t i, const std::string& maintain_var);
   size_t size() const { return r_.ncols == 0 ? 0 : r_.nrows; }
   vg::Rel& rel() { return r_; }
   vg::Ctx* ctx() const { return ctx_; }
@@ -206,6 +209,28 @@ class QueryJob {
   IR* intermediateResult = nullptr;
 };
 
+// Device work a select needs once its host-side lookups are done: either
+// copies of index slices into the new relation, or an adjacent-unique
+// compaction of one slice into its single column.
+struct SelectWork {
+  FullRelationIR* ir = nullptr;
+  std::vector<vg::CopyPiece> pieces;
+  bool unique = false;
+  const TYPEID* uniq_src = nullptr;
+  size_t uniq_n = 0;
+};
+
+// Host state of a join between its phases: operands (possibly swapped),
+// which operand still needs its stable re-sort by the join column, and the
+// output once built.
+struct JoinWork {
+  FullRelationIR* lir = nullptr;
+  FullRelationIR* rir = nullptr;
+  bool sortL = false, sortR = false;
+  size_t new_col_num = 0;
+  bool empty = false;     // an operand is empty: output decided on the host
+};
+
 class SelectQueryJob : public QueryJob {
  public:
   // two variables (src/SelectQueryJob.h:14-19)
@@ -217,6 +242,11 @@ class SelectQueryJob : public QueryJob {
   int startJob(int gpuId) override;
   IR* getIR() override { return intermediateResult; }
   std::string jobTypeName() const override { return "Upload Job"; }
+  // Phase 1 (host): index lookups, bounds, empty intervals; allocates the
+  // relation and describes the device work.
+  void prepare(SelectWork& w);
+  // Phase 2 (after the device work): the unique compaction's row count.
+  static void finishUnique(SelectWork& w, uint64_t kept);
 
  private:
   QueryExecutor* ex;
@@ -239,8 +269,19 @@ class JoinQueryJob : public QueryJob {
   void setQueryVarCounter(std::map<std::string, size_t>* c) { query_variable_counter = c; }
   std::string getJoinVariable() const { return joinVariable; }
   IR* join(FullRelationIR* lir, FullRelationIR* rir);
+  // Phase 1 (host): operand swap, column pruning and implicit index swaps
+  // (their re-sorts are left to the caller: w.sortL / w.sortR).
+  void prepare(JoinWork& w);
+  // Phase 3 (after the join kernels): output relation, log, bound update and
+  // the empty-interval scan.  `col0` holds output column 0 when
+  // 2 < rows < 100 (else unused); first/last its first and last value.
+  void finish(JoinWork& w, vg::Rel& joined, TYPEID first, TYPEID last, const std::vector<TYPEID>* col0);
+  bool isLastJoinForVar() const { return lastJoinForVar; }
+  QueryJob* left() const { return leftJob; }
+  QueryJob* right() const { return rightJob; }
 
  private:
+  void setHeaders(JoinWork& w, FullRelationIR* out);
   QueryExecutor* ex;
   QueryJob* leftJob;
   QueryJob* rightJob;
@@ -255,8 +296,15 @@ class IndexSwapJob : public QueryJob {
   int startJob(int gpuId) override;
   IR* getIR() override { return intermediateResult; }
   std::string jobTypeName() const override { return "Index Swap Job"; }
+  // Phase 1 (host): moves the swap column to position 0; the relation then
+  // needs its stable re-sort by column 0.
+  FullRelationIR* prepare();
+  // Phase 2 (after the sort): log and the empty-interval scan (`col0` holds
+  // column 0 when 2 < rows < 100).
+  void finish(const std::vector<TYPEID>* col0);
 
  private:
+  size_t swapped_col = 0;
   QueryExecutor* ex;
   QueryJob* beforeJob;
   std::string swapVar;
@@ -286,6 +334,11 @@ class QueryPlan {
   size_t jobNum() const { return jobs.size(); }
   // Runs the jobs in order, projects and removes adjacent duplicates.
   void execute(SparqlResult& sparqlResult);
+  // The pieces of execute() for callers that run the jobs themselves:
+  // counters before the first job, projection of the final relation after
+  // the last (the adjacent-unique step is left to the caller).
+  void beginExecution();
+  FullRelationIR* project();
 
  private:
   std::map<std::string, size_t> query_variable_counter;

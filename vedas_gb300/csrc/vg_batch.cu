@@ -1,0 +1,513 @@
+// Batched relation kernels.  Work from many queries is laid out as segments;
+// a kernel maps its block/tile/row index to a segment by an upper-bound
+// search over a per-segment prefix array in device memory.
+#include "vg_batch.h"
+
+#include <algorithm>
+#include <cstring>
+
+#include "vg_prims.cuh"
+#include "vg_sort.h"
+
+namespace vg {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kRows = 8;
+constexpr int kTileRows = kBlock * kRows;
+
+// Segment s of unit u: the last s with start[s] <= u (start has S+1 entries).
+__device__ __forceinline__ uint32_t seg_of(const uint64_t* start, uint32_t S, uint64_t u) {
+  return static_cast<uint32_t>(upper_bound_dev(start, 0, S + 1, u) - 1);
+}
+
+template <typename T>
+T* upload(Ctx& ctx, const std::vector<T>& v) {
+  T* d = static_cast<T*>(ctx.arena.alloc((v.empty() ? 1 : v.size()) * sizeof(T)));
+  if (!v.empty())
+    VG_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx.stream));
+  return d;
+}
+
+unsigned grid_cap(const Ctx& ctx, uint64_t units, int per_thread) {
+  uint64_t g = div_up(units, static_cast<uint64_t>(kBlock) * per_thread);
+  const uint64_t gmax = static_cast<uint64_t>(ctx.num_sms) * 16;
+  if (g > gmax) g = gmax;
+  return static_cast<unsigned>(g < 1 ? 1 : g);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) bcopy_kernel(const CopyPiece* __restrict__ p,
+                                                       const uint64_t* __restrict__ cstart, uint32_t P) {
+  const uint64_t total = cstart[P];
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
+  for (uint64_t q = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; q < total; q += stride) {
+    const uint32_t k = seg_of(cstart, P, q);
+    const CopyPiece pc = p[k];
+    const uint64_t c = q - cstart[k];
+    const uint64_t head = (4 - ((reinterpret_cast<uintptr_t>(pc.dst) >> 2) & 3)) & 3;
+    const uint64_t h = head < pc.len ? head : pc.len;
+    if (c == 0) {
+      for (uint64_t e = 0; e < h; ++e) pc.dst[e] = pc.src[e];
+      const uint64_t body = (pc.len - h) / 4 * 4;
+      for (uint64_t e = h + body; e < pc.len; ++e) pc.dst[e] = pc.src[e];
+    }
+    const uint64_t e0 = h + c * 4;
+    if (e0 + 4 > pc.len) continue;
+    const uint32_t* s = pc.src + e0;
+    uint4 v;
+    if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
+      v = *reinterpret_cast<const uint4*>(s);
+    } else {
+      v.x = s[0];
+      v.y = s[1];
+      v.z = s[2];
+      v.w = s[3];
+    }
+    *reinterpret_cast<uint4*>(pc.dst + e0) = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restrict__ segs,
+                                                         const uint64_t* __restrict__ tstart, uint32_t S,
+                                                         uint64_t* status, uint32_t* ticket,
+                                                         uint64_t* counts, DeviceErrors* err) {
+  __shared__ uint32_t s_scan[kBlock / 32 + 1];
+  __shared__ uint64_t s_b;
+  __shared__ uint32_t s_tile;
+  __shared__ SegRows s_seg;
+  __shared__ uint32_t s_s;
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(ticket, 1u);
+    s_s = seg_of(tstart, S, s_tile);
+    s_seg = segs[s_s];
+  }
+  __syncthreads();
+  const uint64_t tile = s_tile;
+  const uint32_t s = s_s;
+  const uint64_t n = s_seg.n;
+  const uint32_t ncols = s_seg.ncols;
+  const uint64_t r0 = (tile - tstart[s]) * kTileRows + threadIdx.x * kRows;
+  uint32_t diff = (r0 == 0) ? 1u : 0u;
+  for (uint32_t c = 0; c < ncols; ++c) {
+    const uint32_t* col = s_seg.in[c];
+    uint32_t prev = (r0 > 0 && r0 - 1 < n) ? col[r0 - 1] : 0u;
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+      const uint64_t r = r0 + i;
+      const uint32_t v = (r < n) ? col[r] : 0u;
+      if (r < n && r > 0 && v != prev) diff |= 1u << i;
+      prev = v;
+    }
+  }
+  if (r0 >= n) diff = 0;
+  else if (n - r0 < kRows) diff &= (1u << (n - r0)) - 1u;
+  uint32_t tot;
+  const uint32_t e = block_excl_scan<kBlock>(__popc(diff), tot, s_scan);
+  if (threadIdx.x < 32) {
+    const uint64_t p = warp_lookback_seg(status, tile, tstart[s], tot, err);
+    if (threadIdx.x == 0) s_b = p;
+  }
+  __syncthreads();
+  const uint64_t g = s_b;
+  if (tile == tstart[s + 1] - 1 && threadIdx.x == 0) counts[s] = g + tot;
+  uint64_t o = g + e;
+  for (int i = 0; i < kRows; ++i) {
+    if (!(diff >> i & 1u)) continue;
+    for (uint32_t c = 0; c < ncols; ++c) s_seg.out[c][o] = s_seg.in[c][r0 + i];
+    ++o;
+  }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) composite_keys_kernel(const uint32_t* const* __restrict__ col0,
+                                                                const uint64_t* __restrict__ rstart, uint32_t S,
+                                                                uint64_t* __restrict__ keys) {
+  const uint64_t total = rstart[S];
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
+  for (uint64_t r = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; r < total; r += stride) {
+    const uint32_t s = seg_of(rstart, S, r);
+    keys[r] = (static_cast<uint64_t>(s) << 32) | col0[s][r - rstart[s]];
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) seg_gather_kernel(const SegRows* __restrict__ segs,
+                                                            const uint64_t* __restrict__ rstart, uint32_t S,
+                                                            const uint32_t* __restrict__ perm) {
+  const uint64_t total = rstart[S];
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
+  for (uint64_t r = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; r < total; r += stride) {
+    const uint32_t s = seg_of(rstart, S, r);
+    const uint64_t base = rstart[s];
+    const uint64_t src = perm[r] - base;
+    const uint64_t dst = r - base;
+    const SegRows& g = segs[s];
+    for (uint32_t c = 0; c < g.ncols; ++c) g.out[c][dst] = g.in[c][src];
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct JoinSeg {
+  const uint32_t* lk;
+  const uint32_t* rk;
+  uint64_t nl, nr;
+  uint64_t row0;   // offset of this join's left rows in the lo/cnt/offs arrays
+};
+
+__global__ void __launch_bounds__(kBlock) bjoin_count_kernel(const JoinSeg* __restrict__ js,
+                                                             const uint64_t* __restrict__ bstart, uint32_t J,
+                                                             uint32_t* __restrict__ lo, uint32_t* __restrict__ cnt) {
+  __shared__ uint64_t s_win[2];
+  __shared__ uint32_t s_j;
+  if (threadIdx.x == 0) s_j = seg_of(bstart, J, blockIdx.x);
+  __syncthreads();
+  const JoinSeg g = js[s_j];
+  const uint64_t i0 = (blockIdx.x - bstart[s_j]) * kBlock;
+  if (threadIdx.x == 0) {
+    const uint64_t i1 = (i0 + kBlock < g.nl ? i0 + kBlock : g.nl) - 1;
+    const uint64_t w0 = lower_bound_dev(g.rk, 0, g.nr, g.lk[i0]);
+    s_win[0] = w0;
+    s_win[1] = upper_bound_dev(g.rk, w0, g.nr, g.lk[i1]);
+  }
+  __syncthreads();
+  const uint64_t i = i0 + threadIdx.x;
+  if (i >= g.nl) return;
+  const uint32_t k = g.lk[i];
+  const uint64_t a = lower_bound_dev(g.rk, s_win[0], s_win[1], k);
+  const uint64_t b = upper_bound_dev(g.rk, a, s_win[1], k);
+  lo[g.row0 + i] = static_cast<uint32_t>(a);
+  cnt[g.row0 + i] = static_cast<uint32_t>(b - a);
+}
+
+__global__ void __launch_bounds__(kBlock) bjoin_scan_kernel(const JoinSeg* __restrict__ js,
+                                                            const uint64_t* __restrict__ tstart, uint32_t J,
+                                                            const uint32_t* __restrict__ cnt,
+                                                            uint64_t* __restrict__ offs, uint64_t* status,
+                                                            uint32_t* ticket, uint64_t* totals, DeviceErrors* err) {
+  __shared__ uint64_t s_scan[kBlock / 32 + 1];
+  __shared__ uint64_t s_b;
+  __shared__ uint32_t s_tile, s_j;
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(ticket, 1u);
+    s_j = seg_of(tstart, J, s_tile);
+  }
+  __syncthreads();
+  const uint64_t tile = s_tile;
+  const uint32_t j = s_j;
+  const JoinSeg g = js[j];
+  const uint64_t r0 = (tile - tstart[j]) * kTileRows + threadIdx.x * kRows;
+  uint32_t v[kRows];
+  uint64_t sum = 0;
+#pragma unroll
+  for (int i = 0; i < kRows; ++i) {
+    v[i] = (r0 + i < g.nl) ? cnt[g.row0 + r0 + i] : 0u;
+    sum += v[i];
+  }
+  uint64_t tot;
+  const uint64_t e = block_excl_scan64<kBlock>(sum, tot, s_scan);
+  if (threadIdx.x < 32) {
+    const uint64_t p = warp_lookback_seg(status, tile, tstart[j], tot, err);
+    if (threadIdx.x == 0) s_b = p;
+  }
+  __syncthreads();
+  if (tile == tstart[j + 1] - 1 && threadIdx.x == 0) totals[j] = s_b + tot;
+  uint64_t run = s_b + e;
+#pragma unroll
+  for (int i = 0; i < kRows; ++i) {
+    if (r0 + i < g.nl) offs[g.row0 + r0 + i] = run;
+    run += v[i];
+  }
+}
+
+struct JoinOut {
+  const uint64_t* offs;
+  const uint32_t* lo;
+  uint64_t nl, total;
+  const uint32_t* lc[VG_MAX_COLS];
+  const uint32_t* rc[VG_MAX_COLS];
+  uint32_t* oc[VG_MAX_COLS];
+  uint32_t nlc, nrc;
+};
+
+__global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __restrict__ jo,
+                                                             const uint64_t* __restrict__ ostart, uint32_t J) {
+  __shared__ JoinOut s_o;
+  __shared__ uint64_t s_i[2];
+  __shared__ uint64_t s_kb;
+  if (threadIdx.x == 0) {
+    const uint32_t j = seg_of(ostart, J, blockIdx.x);
+    s_o = jo[j];
+    const uint64_t kb = (blockIdx.x - ostart[j]) * kTileRows;
+    s_kb = kb;
+    const uint64_t klast = (kb + kTileRows < s_o.total ? kb + kTileRows : s_o.total) - 1;
+    const uint64_t f = upper_bound_dev(s_o.offs, 0, s_o.nl, kb) - 1;
+    s_i[0] = f;
+    s_i[1] = upper_bound_dev(s_o.offs, f, s_o.nl, klast);
+  }
+  __syncthreads();
+  const uint64_t ib = s_i[0], ie = s_i[1], kb = s_kb;
+  for (int it = 0; it < kRows; ++it) {
+    const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
+    if (k >= s_o.total) break;
+    const uint64_t i = upper_bound_dev(s_o.offs, ib, ie, k) - 1;
+    const uint64_t jj = s_o.lo[i] + (k - s_o.offs[i]);
+    uint32_t c = 0;
+    for (uint32_t x = 0; x < s_o.nlc; ++x) s_o.oc[c++][k] = s_o.lc[x][i];
+    for (uint32_t x = 0; x < s_o.nrc; ++x) s_o.oc[c++][k] = s_o.rc[x][jj];
+  }
+}
+
+__global__ void first_last_kernel(const JoinOut* __restrict__ jo, uint32_t J, uint32_t* __restrict__ fl) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= J) return;
+  const JoinOut& o = jo[j];
+  if (o.total == 0) return;
+  fl[2 * j] = o.oc[0][0];
+  fl[2 * j + 1] = o.oc[0][o.total - 1];
+}
+
+struct Col0Req {
+  const uint32_t* src;
+  uint64_t n;
+  uint64_t dst;
+};
+
+__global__ void col0_kernel(const Col0Req* __restrict__ rq, uint32_t R, uint32_t* __restrict__ out) {
+  for (uint32_t q = blockIdx.x; q < R; q += gridDim.x)
+    for (uint64_t i = threadIdx.x; i < rq[q].n; i += blockDim.x) out[rq[q].dst + i] = rq[q].src[i];
+}
+
+int bits_for_segments(uint32_t S) {
+  int b = 0;
+  while ((1ull << b) < S) ++b;
+  return b;
+}
+
+}  // namespace
+
+void batched_copy(Ctx& ctx, const std::vector<CopyPiece>& pieces) {
+  std::vector<CopyPiece> p;
+  std::vector<uint64_t> cstart(1, 0);
+  double bytes = 0;
+  for (const CopyPiece& pc : pieces) {
+    if (pc.len == 0) continue;
+    const uint64_t head = (4 - ((reinterpret_cast<uintptr_t>(pc.dst) >> 2) & 3)) & 3;
+    const uint64_t h = head < pc.len ? head : pc.len;
+    const uint64_t chunks = (pc.len - h) / 4;
+    p.push_back(pc);
+    cstart.push_back(cstart.back() + (chunks ? chunks : 1));
+    bytes += 8.0 * pc.len;
+  }
+  if (p.empty()) return;
+  CopyPiece* dp = upload(ctx, p);
+  uint64_t* dc = upload(ctx, cstart);
+  const uint32_t P = static_cast<uint32_t>(p.size());
+  ctx.launch("select_copy", bytes, [&] {
+    bcopy_kernel<<<grid_cap(ctx, cstart.back(), 2), kBlock, 0, ctx.stream>>>(dp, dc, P);
+  });
+  VG_CUDA(cudaGetLastError());
+  ctx.free(dp);
+  ctx.free(dc);
+}
+
+std::vector<uint64_t> batched_unique(Ctx& ctx, const std::vector<SegRows>& segs) {
+  const uint32_t S = static_cast<uint32_t>(segs.size());
+  std::vector<uint64_t> counts(S, 0);
+  if (S == 0) return counts;
+  std::vector<uint64_t> tstart(S + 1, 0);
+  double bytes = 0;
+  for (uint32_t s = 0; s < S; ++s) {
+    tstart[s + 1] = tstart[s] + div_up(segs[s].n, kTileRows);
+    bytes += 4.0 * segs[s].n * segs[s].ncols;
+  }
+  const uint64_t tiles = tstart[S];
+  if (tiles == 0) return counts;
+  SegRows* ds = upload(ctx, segs);
+  uint64_t* dt = upload(ctx, tstart);
+  Scratch<uint64_t> status(ctx, tiles), dcount(ctx, S);
+  Scratch<uint32_t> ticket(ctx, 1);
+  VG_CUDA(cudaMemsetAsync(status.get(), 0, tiles * sizeof(uint64_t), ctx.stream));
+  VG_CUDA(cudaMemsetAsync(dcount.get(), 0, S * sizeof(uint64_t), ctx.stream));
+  VG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(uint32_t), ctx.stream));
+  ctx.launch("unique_compact", bytes, [&] {
+    bunique_kernel<<<static_cast<unsigned>(tiles), kBlock, 0, ctx.stream>>>(ds, dt, S, status.get(), ticket.get(),
+                                                                           dcount.get(), ctx.d_err);
+  });
+  VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaMemcpyAsync(counts.data(), dcount.get(), S * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
+  double wb = 0;
+  for (uint32_t s = 0; s < S; ++s) wb += 4.0 * counts[s] * segs[s].ncols;
+  ctx.kstats["unique_compact"].bytes += wb;
+  ctx.free(ds);
+  ctx.free(dt);
+  return counts;
+}
+
+void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in) {
+  std::vector<Rel*> rels;
+  for (Rel* r : rels_in)
+    if (r->nrows > 1 && r->ncols > 0) rels.push_back(r);
+  const uint32_t S = static_cast<uint32_t>(rels.size());
+  if (S == 0) return;
+  std::vector<uint64_t> rstart(S + 1, 0);
+  std::vector<const uint32_t*> col0(S);
+  for (uint32_t s = 0; s < S; ++s) {
+    rstart[s + 1] = rstart[s] + rels[s]->nrows;
+    col0[s] = rels[s]->cols[0];
+  }
+  const uint64_t N = rstart[S];
+  if (N > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "batched sort is limited to 2^32 rows");
+  uint64_t* drs = upload(ctx, rstart);
+  const uint32_t** dc0 = upload(ctx, col0);
+  uint64_t* keys = ctx.alloc<uint64_t>(N);
+  uint64_t* keys_alt = ctx.alloc<uint64_t>(N);
+  uint32_t* vals = ctx.alloc<uint32_t>(N);
+  uint32_t* vals_alt = ctx.alloc<uint32_t>(N);
+  ctx.launch("sort_keys", 12.0 * N, [&] {
+    composite_keys_kernel<<<grid_cap(ctx, N, 4), kBlock, 0, ctx.stream>>>(dc0, drs, S, keys);
+  });
+  VG_CUDA(cudaGetLastError());
+  const bool alt = radix_sort_u64(ctx, keys, keys_alt, vals, vals_alt, N, 32 + bits_for_segments(S), true);
+  uint32_t* perm = alt ? vals_alt : vals;
+  ctx.free(keys);
+  ctx.free(keys_alt);
+  std::vector<SegRows> segs(S);
+  double bytes = 4.0 * N;
+  for (uint32_t s = 0; s < S; ++s) {
+    segs[s].ncols = rels[s]->ncols;
+    segs[s].n = rels[s]->nrows;
+    for (uint32_t c = 0; c < rels[s]->ncols; ++c) {
+      segs[s].in[c] = rels[s]->cols[c];
+      segs[s].out[c] = ctx.alloc<uint32_t>(rels[s]->nrows);
+    }
+    bytes += 8.0 * rels[s]->nrows * rels[s]->ncols;
+  }
+  SegRows* dsg = upload(ctx, segs);
+  ctx.launch("gather", bytes, [&] {
+    seg_gather_kernel<<<grid_cap(ctx, N, 4), kBlock, 0, ctx.stream>>>(dsg, drs, S, perm);
+  });
+  VG_CUDA(cudaGetLastError());
+  for (uint32_t s = 0; s < S; ++s)
+    for (uint32_t c = 0; c < rels[s]->ncols; ++c) {
+      ctx.free(rels[s]->cols[c]);
+      rels[s]->cols[c] = segs[s].out[c];
+    }
+  ctx.free(vals);
+  ctx.free(vals_alt);
+  ctx.free(dsg);
+  ctx.free(drs);
+  ctx.free(const_cast<uint32_t**>(dc0));
+}
+
+void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r,
+                  std::vector<Rel>& out, std::vector<uint32_t>& first_last) {
+  const uint32_t J = static_cast<uint32_t>(l.size());
+  out.assign(J, Rel());
+  first_last.assign(2 * J, 0);
+  if (J == 0) return;
+  std::vector<JoinSeg> js(J);
+  std::vector<uint64_t> bstart(J + 1, 0), tstart(J + 1, 0);
+  uint64_t rows = 0;
+  double cbytes = 0;
+  for (uint32_t j = 0; j < J; ++j) {
+    if (l[j]->nrows == 0 || r[j]->nrows == 0) fail(VG_ERR_INVALID, "batched join of an empty relation");
+    if (l[j]->nrows > 0xFFFFFFFFull || r[j]->nrows > 0xFFFFFFFFull)
+      fail(VG_ERR_OVERFLOW, "join inputs are limited to 2^32 rows");
+    if (l[j]->ncols + r[j]->ncols - 1 > VG_MAX_COLS) fail(VG_ERR_UNSUPPORTED, "join output has more than 9 columns");
+    js[j] = {l[j]->cols[0], r[j]->cols[0], l[j]->nrows, r[j]->nrows, rows};
+    rows += l[j]->nrows;
+    bstart[j + 1] = bstart[j] + div_up(l[j]->nrows, kBlock);
+    tstart[j + 1] = tstart[j] + div_up(l[j]->nrows, kTileRows);
+    cbytes += 4.0 * (l[j]->nrows + r[j]->nrows);
+  }
+  JoinSeg* djs = upload(ctx, js);
+  uint64_t* dbs = upload(ctx, bstart);
+  uint64_t* dts = upload(ctx, tstart);
+  Scratch<uint32_t> lo(ctx, rows), cnt(ctx, rows);
+  Scratch<uint64_t> offs(ctx, rows), status(ctx, tstart[J]), totals(ctx, J);
+  Scratch<uint32_t> ticket(ctx, 1);
+  VG_CUDA(cudaMemsetAsync(status.get(), 0, tstart[J] * sizeof(uint64_t), ctx.stream));
+  VG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(uint32_t), ctx.stream));
+  ctx.launch("join_count", cbytes, [&] {
+    bjoin_count_kernel<<<static_cast<unsigned>(bstart[J]), kBlock, 0, ctx.stream>>>(djs, dbs, J, lo.get(), cnt.get());
+  });
+  VG_CUDA(cudaGetLastError());
+  ctx.launch("join_scan", 12.0 * rows, [&] {
+    bjoin_scan_kernel<<<static_cast<unsigned>(tstart[J]), kBlock, 0, ctx.stream>>>(
+        djs, dts, J, cnt.get(), offs.get(), status.get(), ticket.get(), totals.get(), ctx.d_err);
+  });
+  VG_CUDA(cudaGetLastError());
+  std::vector<uint64_t> tot(J);
+  VG_CUDA(cudaMemcpyAsync(tot.data(), totals.get(), J * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
+  std::vector<JoinOut> jo(J);
+  std::vector<uint64_t> ostart(J + 1, 0);
+  double wbytes = 0;
+  for (uint32_t j = 0; j < J; ++j) {
+    if (tot[j] > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
+    const uint32_t ncols = l[j]->ncols + r[j]->ncols - 1;
+    out[j] = rel_alloc(ctx, ncols, tot[j]);
+    JoinOut& o = jo[j];
+    std::memset(&o, 0, sizeof(o));
+    o.offs = offs.get() + js[j].row0;
+    o.lo = lo.get() + js[j].row0;
+    o.nl = l[j]->nrows;
+    o.total = tot[j];
+    for (uint32_t c = 0; c < l[j]->ncols; ++c) o.lc[c] = l[j]->cols[c];
+    for (uint32_t c = 1; c < r[j]->ncols; ++c) o.rc[c - 1] = r[j]->cols[c];
+    for (uint32_t c = 0; c < ncols; ++c) o.oc[c] = out[j].cols[c];
+    o.nlc = l[j]->ncols;
+    o.nrc = r[j]->ncols - 1;
+    ostart[j + 1] = ostart[j] + div_up(tot[j], kTileRows);
+    wbytes += 4.0 * tot[j] * (2.0 * ncols - 1);
+  }
+  JoinOut* djo = upload(ctx, jo);
+  Scratch<uint32_t> dfl(ctx, 2 * J);
+  if (ostart[J] > 0) {
+    uint64_t* dos = upload(ctx, ostart);
+    ctx.launch("join_write", wbytes, [&] {
+      bjoin_write_kernel<<<static_cast<unsigned>(ostart[J]), kBlock, 0, ctx.stream>>>(djo, dos, J);
+    });
+    VG_CUDA(cudaGetLastError());
+    ctx.free(dos);
+  }
+  ctx.launch("join_first_last", 8.0 * J, [&] {
+    first_last_kernel<<<static_cast<unsigned>(div_up(J, 128)), 128, 0, ctx.stream>>>(djo, J, dfl.get());
+  });
+  VG_CUDA(cudaGetLastError());
+  VG_CUDA(cudaMemcpyAsync(first_last.data(), dfl.get(), 2 * J * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                          ctx.stream));
+  ctx.sync();
+  ctx.free(djo);
+  ctx.free(djs);
+  ctx.free(dbs);
+  ctx.free(dts);
+}
+
+void batched_col0(Ctx& ctx, const std::vector<const Rel*>& rels, std::vector<std::vector<uint32_t>>& out) {
+  const uint32_t R = static_cast<uint32_t>(rels.size());
+  out.assign(R, {});
+  if (R == 0) return;
+  std::vector<Col0Req> rq(R);
+  uint64_t total = 0;
+  for (uint32_t q = 0; q < R; ++q) {
+    rq[q] = {rels[q]->cols[0], rels[q]->nrows, total};
+    total += rels[q]->nrows;
+  }
+  if (total == 0) return;
+  Col0Req* drq = upload(ctx, rq);
+  Scratch<uint32_t> buf(ctx, total);
+  ctx.launch("col0_stage", 8.0 * total, [&] {
+    col0_kernel<<<R < 1024 ? R : 1024, 128, 0, ctx.stream>>>(drq, R, buf.get());
+  });
+  VG_CUDA(cudaGetLastError());
+  std::vector<uint32_t> h(total);
+  VG_CUDA(cudaMemcpyAsync(h.data(), buf.get(), total * 4, cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
+  for (uint32_t q = 0; q < R; ++q) out[q].assign(h.begin() + rq[q].dst, h.begin() + rq[q].dst + rq[q].n);
+  ctx.free(drq);
+}
+
+}  // namespace vg

@@ -5,6 +5,7 @@
 #include <string>
 
 #include "compat/vedas_compat.h"
+#include "vg_batch_host.h"
 #include "vg_ctx.h"
 #include "vg_index.h"
 #include "vg_relops.h"
@@ -16,6 +17,10 @@ struct vg_ctx {
 struct vg_index {
   vg_ctx* ctx = nullptr;
   std::unique_ptr<vedas::VedasStorage> st;
+};
+
+struct vg_batch {
+  vg::BatchResult r;
 };
 
 struct vg_result {
@@ -394,6 +399,66 @@ void vg_result_log(const vg_result* r, uint32_t i, uint32_t* op, uint64_t* p1, u
 }
 vg_status vg_result_free(vg_result* r) {
   delete r;
+  return VG_OK;
+}
+
+vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, vg_batch** out) {
+  if (!ctx || !ix || !out || (nq && !queries)) return VG_ERR_INVALID;
+  *out = nullptr;
+  auto b = std::make_unique<vg_batch>();
+  vg_status st = guard([&] {
+    std::vector<std::string> texts;
+    texts.reserve(nq);
+    for (uint32_t i = 0; i < nq; ++i) texts.emplace_back(queries[i] ? queries[i] : "");
+    vg::run_batch(ctx->c, ix->st.get(), texts, b->r);
+  });
+  if (st == VG_OK) *out = b.release();
+  return st;
+}
+
+uint32_t vg_batch_size(const vg_batch* b) { return b ? static_cast<uint32_t>(b->r.queries.size()) : 0; }
+uint32_t vg_batch_waves(const vg_batch* b) { return b ? b->r.waves : 0; }
+vg_status vg_batch_query_status(const vg_batch* b, uint32_t q) {
+  return (b && q < b->r.queries.size()) ? b->r.queries[q].status : VG_ERR_INVALID;
+}
+const char* vg_batch_query_error(const vg_batch* b, uint32_t q) {
+  return (b && q < b->r.queries.size()) ? b->r.queries[q].error.c_str() : "";
+}
+uint32_t vg_batch_ncols(const vg_batch* b, uint32_t q) {
+  return (b && q < b->r.queries.size()) ? static_cast<uint32_t>(b->r.queries[q].headers.size()) : 0;
+}
+uint64_t vg_batch_nrows(const vg_batch* b, uint32_t q) {
+  return (b && q < b->r.queries.size()) ? b->r.queries[q].rel.nrows : 0;
+}
+const char* vg_batch_header(const vg_batch* b, uint32_t q, uint32_t c) {
+  if (!b || q >= b->r.queries.size() || c >= b->r.queries[q].headers.size()) return nullptr;
+  return b->r.queries[q].headers[c].c_str();
+}
+const uint32_t* vg_batch_column_device(const vg_batch* b, uint32_t q, uint32_t c) {
+  if (!b || q >= b->r.queries.size() || c >= b->r.queries[q].rel.ncols) return nullptr;
+  return b->r.queries[q].rel.cols[c];
+}
+vg_status vg_batch_download(const vg_batch* b, uint32_t q, uint32_t c, uint32_t* host) {
+  if (!b || q >= b->r.queries.size() || c >= b->r.queries[q].rel.ncols) return VG_ERR_INVALID;
+  return guard([&] {
+    const vg::Rel& r = b->r.queries[q].rel;
+    vg::download(*b->r.ctx, r.cols[c], r.nrows, host);
+  });
+}
+uint32_t vg_batch_nlog(const vg_batch* b, uint32_t q) {
+  return (b && q < b->r.queries.size()) ? static_cast<uint32_t>(b->r.queries[q].log.size()) : 0;
+}
+void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint64_t* p1, uint64_t* p2,
+                  uint64_t* p3) {
+  if (!b || q >= b->r.queries.size() || i >= b->r.queries[q].log.size()) return;
+  const auto& l = b->r.queries[q].log[i];
+  if (op) *op = static_cast<uint32_t>(l.op);
+  if (p1) *p1 = l.param1;
+  if (p2) *p2 = l.param2;
+  if (p3) *p3 = l.param3;
+}
+vg_status vg_batch_free(vg_batch* b) {
+  delete b;
   return VG_OK;
 }
 

@@ -118,6 +118,34 @@ __device__ __forceinline__ uint64_t warp_lookback(uint64_t* status, uint32_t til
   return prefix;
 }
 
+// Segmented variant: tiles [first_tile, tile) of one segment only; the
+// segment's first tile starts a new chain.
+__device__ __forceinline__ uint64_t warp_lookback_seg(uint64_t* status, uint64_t tile, uint64_t first_tile,
+                                                      uint64_t tile_total, DeviceErrors* err) {
+  const uint32_t lane = lane_id();
+  const bool head = tile == first_tile;
+  if (lane == 0) st_release_u64(&status[tile], (head ? kFlagInc : kFlagAgg) | tile_total);
+  uint64_t prefix = 0;
+  if (!head) {
+    int64_t j = static_cast<int64_t>(tile) - 1 - lane;
+    while (true) {
+      uint64_t s = (j >= static_cast<int64_t>(first_tile)) ? wait_status(&status[j], err) : kFlagInc;
+      bool inc = (s & kFlagInc) != 0;
+      uint32_t inc_mask = __ballot_sync(0xffffffffu, inc);
+      uint64_t v = s & kValueMask;
+      if (inc_mask) {
+        uint32_t lim = __ffs(inc_mask) - 1;
+        prefix += warp_sum64(lane <= lim ? v : 0);
+        break;
+      }
+      prefix += warp_sum64(v);
+      j -= 32;
+    }
+    if (lane == 0) st_release_u64(&status[tile], kFlagInc | (prefix + tile_total));
+  }
+  return prefix;
+}
+
 // Whole-block wrapper: warp 0 looks back, the prefix is broadcast.
 __device__ __forceinline__ uint64_t block_lookback(uint64_t* status, uint32_t tile, uint64_t tile_total,
                                                    DeviceErrors* err, uint64_t* s_bcast) {
