@@ -186,6 +186,19 @@ void vg_result_log(const vg_result* r, uint32_t i, uint32_t* op, uint64_t* p1, u
                    uint64_t* p3);
 vg_status vg_result_free(vg_result* r);
 
+/* ---- host planning logic (no device needed) ----------------------------- */
+/* The job list QueryGraph::generateQueryPlan (src/QueryGraph.cu:64-74) and
+ * QueryExecutor::postorderTraversal (src/QueryExecutor.cu:106-135) produce
+ * for `sparql` when its patterns have the given estimate_rows, written to
+ * buf as "U<pattern>:<PSO|POS|->;" selects, "J<left job>,<right job>:<var>:
+ * <last join for var>;" joins and "W<job>:<var>;" index swaps. */
+vg_status vg_plan_describe(const char* sparql, const uint64_t* estimate_rows, uint32_t npatterns, char* buf,
+                           size_t cap);
+/* EmptyIntervalDict::updateBound (src/EmptyIntervalDict.cu:33-106) applied
+ * n times to one variable (quads: n x (lb1, ub1, lb2, ub2)); out4 receives
+ * the variable's final entry. */
+vg_status vg_eid_sequence(const uint64_t* quads, uint32_t n, uint64_t out4[4]);
+
 /* ---- batched execution -------------------------------------------------- */
 typedef struct vg_batch vg_batch;
 
@@ -199,6 +212,9 @@ vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, ui
                        vg_batch** out);
 uint32_t vg_batch_size(const vg_batch* b);
 uint32_t vg_batch_waves(const vg_batch* b);
+/* Seconds spent: out6 = {host planning, host job preparation, batched device
+ * work (with its waits), host job completion, final de-duplication, total}. */
+vg_status vg_batch_profile(const vg_batch* b, double out6[6]);
 vg_status vg_batch_query_status(const vg_batch* b, uint32_t q);
 const char* vg_batch_query_error(const vg_batch* b, uint32_t q);
 uint32_t vg_batch_ncols(const vg_batch* b, uint32_t q);
@@ -206,6 +222,11 @@ uint64_t vg_batch_nrows(const vg_batch* b, uint32_t q);
 const char* vg_batch_header(const vg_batch* b, uint32_t q, uint32_t c);
 const uint32_t* vg_batch_column_device(const vg_batch* b, uint32_t q, uint32_t c);
 vg_status vg_batch_download(const vg_batch* b, uint32_t q, uint32_t c, uint32_t* host);
+/* All result columns of the batch in one device-to-host copy: query by
+ * query, column by column, nrows words each; `host` holds
+ * vg_batch_result_words(b) uint32 words (pinned memory is fastest). */
+uint64_t vg_batch_result_words(const vg_batch* b);
+vg_status vg_batch_download_all(const vg_batch* b, uint32_t* host);
 uint32_t vg_batch_nlog(const vg_batch* b, uint32_t q);
 void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint64_t* p1, uint64_t* p2,
                   uint64_t* p3);

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -1159,6 +1160,59 @@ void vo_result_log(const vo_result* r, uint32_t i, uint32_t* op, uint64_t* p1, u
   *text = l.text.c_str();
 }
 void vo_result_free(vo_result* r) { delete r; }
+
+// Plan description (post-order job list) for given per-pattern estimates:
+// "U<tp>:<index>;" selects, "J<l>,<r>:<var>:<last>;" joins, "W<child>:<var>;" swaps.
+int vo_plan_describe(const char* text, const uint64_t* est, uint32_t n, char* buf, uint64_t cap) {
+  try {
+    Query q = parse_query(text);
+    for (uint32_t i = 0; i < n && i < q.patterns.size(); ++i) q.patterns[i].estimate_rows = est[i];
+    std::vector<std::unique_ptr<PlanNode>> pool;
+    Planner pl(q, pool);
+    PlanNode* root = pl.plan();
+    std::string s;
+    int counter = 0;
+    std::function<int(PlanNode*)> walk = [&](PlanNode* nd) -> int {
+      if (!nd) return -1;
+      int a = -1, b = -1;
+      if (nd->c1) a = walk(nd->c1);
+      if (nd->c2) b = walk(nd->c2);
+      if (nd->op == Op::Upload) {
+        const Pattern& tp = q.patterns[static_cast<size_t>(nd->tp)];
+        std::string idx = "-";
+        if (tp.nvars() == 2) idx = (tp.var[0] && tp.name[0] == nd->var) ? "PSO" : "POS";
+        s += "U" + std::to_string(nd->tp) + ":" + idx + ";";
+      } else if (nd->op == Op::Join) {
+        s += "J" + std::to_string(a) + "," + std::to_string(b) + ":" + nd->var + ":" + (nd->reuse ? "0" : "1") + ";";
+      } else {
+        s += "W" + std::to_string(a) + ":" + nd->var + ";";
+      }
+      return counter++;
+    };
+    walk(root);
+    if (s.size() + 1 > cap) return 3;
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return 0;
+  } catch (const OracleParse&) {
+    return 1;
+  } catch (const OracleUB&) {
+    return 2;
+  }
+}
+
+// updateBound applied n times to one variable; out4 = the final entry.
+int vo_eid_sequence(const uint64_t* quads, uint32_t n, uint64_t* out4) {
+  EmptyIntervals e;
+  for (uint32_t i = 0; i < n; ++i)
+    e.update("?x", quads[4 * i], quads[4 * i + 1], quads[4 * i + 2], quads[4 * i + 3]);
+  if (!e.dict.count("?x")) return 1;
+  Quad qd = e.dict["?x"];
+  out4[0] = std::get<0>(qd);
+  out4[1] = std::get<1>(qd);
+  out4[2] = std::get<2>(qd);
+  out4[3] = std::get<3>(qd);
+  return 0;
+}
 
 void vo_sort_by_first(uint32_t** cols, uint32_t ncols, uint64_t nrows) {
   Relation rel;

@@ -44,6 +44,12 @@ void vo_result_log(const vo_result* r, uint32_t i, uint32_t* op, uint64_t* p1, u
                    uint64_t* p3, const char** text);
 void vo_result_free(vo_result* r);
 
+/* Host logic: the plan for given per-pattern estimates, as a post-order job
+ * list "U<tp>:<index>;", "J<l>,<r>:<var>:<last>;", "W<child>:<var>;"; and the
+ * empty-interval entry after n updateBound calls (quads = n x 4 values). */
+int vo_plan_describe(const char* text, const uint64_t* est, uint32_t n, char* buf, uint64_t cap);
+int vo_eid_sequence(const uint64_t* quads, uint32_t n, uint64_t* out4);
+
 /* Job-level checkers used by the kernel parity tests. */
 /* Stable sort of rows by column 0 (FullRelationIR::sortByFirstColumn). */
 void vo_sort_by_first(uint32_t** cols, uint32_t ncols, uint64_t nrows);

@@ -90,8 +90,10 @@ def parse_index(buf: bytes) -> dict:
 def build_index(graph_path: str, full: bool = False) -> dict:
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "idx.bin")
-        cmd = [REF_BIN, "index", graph_path, out] + (["full"] if full else [])
-        subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        cmd = [REF_BIN, "index", os.path.abspath(graph_path), out] + (["full"] if full else [])
+        # the reference's full-index build writes histogram files into its
+        # working directory (VedasStorage::writeHistogram): keep them in td
+        subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, cwd=td)
         with open(out, "rb") as f:
             return parse_index(f.read())
 
@@ -107,9 +109,10 @@ def run_queries(graph_path: str, queries: list, full: bool = False, timeout: flo
         out = os.path.join(td, "res.bin")
         first = 0
         while first < len(queries):
-            cmd = [REF_BIN, "query", graph_path, qpath, out, str(first)] + (["full"] if full else [])
+            cmd = [REF_BIN, "query", os.path.abspath(graph_path), qpath, out, str(first)] + \
+                (["full"] if full else [])
             proc = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
-                                  timeout=timeout)
+                                  timeout=timeout, cwd=td)
             with open(out, "rb") as f:
                 parsed = parse_results(f.read())
             for r in parsed:

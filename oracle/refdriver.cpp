@@ -27,7 +27,12 @@
 #include <string>
 #include <vector>
 
+#include <memory>
+
+#include "EmptyIntervalDict.h"
+#include "PlanTreeNode.h"
 #include "QueryExecutor.h"
+#include "QueryGraph.h"
 #include "RdfData.h"
 #include "SparqlQuery.h"
 #include "SparqlResult.h"
@@ -179,9 +184,81 @@ int do_query(const char* graph, const char* qpath, const char* outp, size_t firs
   return 0;
 }
 
+// Plan of one query line "<e0> <e1> ... | <query>" with the given per-pattern
+// estimate_rows, through the reference's QueryGraph::generateQueryPlan
+// (src/QueryGraph.cu:64-74), printed in the post-order that
+// QueryExecutor::postorderTraversal emits jobs (src/QueryExecutor.cu:106-135).
+int plan_node(PlanTreeNode* n, std::string& out, int& counter) {
+  if (!n) return -1;
+  int a = -1, b = -1;
+  if (n->child1) a = plan_node(n->child1, out, counter);
+  if (n->child2) b = plan_node(n->child2, out, counter);
+  if (n->op == UPLOAD) {
+    std::string idx = "-";
+    if (n->tp->getVariableNum() == 2) idx = (n->tp->getSubject() == n->var) ? "PSO" : "POS";
+    out += "U" + std::to_string(n->tp->getId()) + ":" + idx + ";";
+  } else if (n->op == JOIN) {
+    out += "J" + std::to_string(a) + "," + std::to_string(b) + ":" + n->var + ":" +
+           (n->reuseVar ? "0" : "1") + ";";
+  } else {
+    out += "W" + std::to_string(a) + ":" + n->var + ";";
+  }
+  return counter++;
+}
+
+int do_plan(const char* qpath, const char* outp) {
+  std::ifstream qin(qpath);
+  std::ofstream out(outp);
+  std::string line;
+  while (std::getline(qin, line)) {
+    if (line.empty()) continue;
+    size_t bar = line.find('|');
+    std::istringstream es(line.substr(0, bar));
+    std::vector<size_t> est;
+    size_t e;
+    while (es >> e) est.push_back(e);
+    std::string q = line.substr(bar + 1);
+    DICTTYPE so_map, p_map, l_map;
+    register_constants(q, so_map, p_map, l_map);
+    SparqlQuery sq(q.c_str(), so_map, p_map, l_map);
+    for (size_t i = 0; i < sq.getPatternNum() && i < est.size(); ++i) sq.getPatternPtr(i)->estimate_rows = est[i];
+    QueryGraph qg(&sq, nullptr);
+    PlanTreeNode* root = qg.generateQueryPlan();
+    std::string s;
+    int counter = 0;
+    plan_node(root, s, counter);
+    out << s << "\n";
+  }
+  return 0;
+}
+
+// EmptyIntervalDict sequences: lines "update lb1 ub1 lb2 ub2", "get" and
+// "reset" on one variable; every "get" prints the bound tuple.
+int do_eid(const char* inp, const char* outp) {
+  std::ifstream in(inp);
+  std::ofstream out(outp);
+  std::unique_ptr<EmptyIntervalDict> d(new EmptyIntervalDict());
+  std::string op;
+  while (in >> op) {
+    if (op == "reset") {
+      d.reset(new EmptyIntervalDict());
+    } else if (op == "update") {
+      size_t a, b, c, e;
+      in >> a >> b >> c >> e;
+      d->updateBound("?x", a, b, c, e);
+    } else if (op == "get") {
+      VAR_BOUND v = d->getBound("?x");
+      out << std::get<0>(v) << " " << std::get<1>(v) << " " << std::get<2>(v) << " " << std::get<3>(v) << "\n";
+    }
+  }
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
+  if (argc >= 4 && std::string(argv[1]) == "plan") return do_plan(argv[2], argv[3]);
+  if (argc >= 4 && std::string(argv[1]) == "eid") return do_eid(argv[2], argv[3]);
   if (argc >= 4 && std::string(argv[1]) == "index") {
     bool full = argc >= 5 && std::string(argv[4]) == "full";
     return do_index(argv[2], argv[3], full);

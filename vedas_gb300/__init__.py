@@ -101,6 +101,9 @@ def lib():
             "vg_batch_header": (ctypes.c_char_p, [vp, u32, u32]),
             "vg_batch_column_device": (vp, [vp, u32, u32]),
             "vg_batch_download": (i32, [vp, u32, u32, pu32]),
+            "vg_batch_result_words": (u64, [vp]),
+            "vg_batch_download_all": (i32, [vp, vp]),
+            "vg_batch_profile": (i32, [vp, ctypes.POINTER(ctypes.c_double)]),
             "vg_batch_nlog": (u32, [vp, u32]),
             "vg_batch_log": (None, [vp, u32, u32, pu32, ctypes.POINTER(u64), ctypes.POINTER(u64),
                                     ctypes.POINTER(u64)]),
@@ -315,6 +318,24 @@ class Batch:
                 check(L.vg_batch_download(self.h, q, c, _p32(a)))
             out.append(a)
         return out
+
+    def result_words(self) -> int:
+        return int(lib().vg_batch_result_words(self.h))
+
+    def download_all(self, host_ptr: int) -> int:
+        """Copies every result column into host memory at host_ptr (one copy);
+        returns the number of bytes copied."""
+        words = self.result_words()
+        if words:
+            check(lib().vg_batch_download_all(self.h, ctypes.c_void_p(host_ptr)))
+        return 4 * words
+
+    def profile(self) -> dict:
+        """Host/device time split of the run, in seconds."""
+        out = (ctypes.c_double * 6)()
+        check(lib().vg_batch_profile(self.h, out))
+        keys = ["plan_s", "prepare_s", "device_s", "finish_s", "final_s", "total_s"]
+        return dict(zip(keys, list(out)))
 
     def log(self, q: int):
         L = lib()

@@ -2,13 +2,13 @@
 //
 // Every query keeps the reference's own plan and job semantics (the host
 // mirror in compat/).  Queries advance in waves, one job per query per wave,
-// so each query still sees its jobs strictly in plan order (its bounds and
+// so each query still runs its jobs strictly in plan order (its bounds and
 // empty intervals flow from job to job exactly as in QueryPlan::execute).
 // Within a wave the device work of all queries is issued together: one
 // segmented stable sort for every index swap and implicit join re-sort, one
 // copy launch and one unique launch for every select, and one count / scan /
-// write chain for every join.  Host planning of the queries runs on a thread
-// pool.
+// write chain for every join.  The host phases of a wave (index lookups,
+// bounds, empty intervals, relation bookkeeping) run on a thread pool.
 #include "vg_batch_host.h"
 
 #include <algorithm>
@@ -21,14 +21,21 @@ namespace vg {
 
 namespace {
 
+using Clock = std::chrono::steady_clock;
+
+double since(Clock::time_point t0) {
+  return std::chrono::duration<double>(Clock::now() - t0).count();
+}
+
 template <typename F>
-void parallel_for(size_t n, F&& f) {
+void pfor(size_t n, F&& f) {
   unsigned hw = std::thread::hardware_concurrency();
   unsigned nt = hw ? std::min<unsigned>(hw, 32) : 4;
-  if (n < 64 || nt <= 1) {
+  if (n < 128 || nt <= 1) {
     for (size_t i = 0; i < n; ++i) f(i);
     return;
   }
+  nt = static_cast<unsigned>(std::min<size_t>(nt, (n + 63) / 64));
   std::atomic<size_t> next{0};
   std::vector<std::thread> th;
   for (unsigned t = 0; t < nt; ++t)
@@ -39,32 +46,42 @@ void parallel_for(size_t n, F&& f) {
 }
 
 template <typename F>
-bool guarded(BatchQuery& q, F&& f) {
+bool guarded(BatchQuery* q, F&& f) {
   try {
     f();
     return true;
   } catch (const Error& e) {
-    q.status = e.status;
-    q.error = e.what();
+    q->status = e.status;
+    q->error = e.what();
   } catch (const std::exception& e) {
-    q.status = VG_ERR_INVALID;
-    q.error = e.what();
+    q->status = VG_ERR_INVALID;
+    q->error = e.what();
   }
   return false;
 }
 
-}  // namespace
-
-BatchResult::~BatchResult() {
-  if (ctx)
-    for (auto& q : queries) rel_free(*ctx, q.rel);
+// Estimated HBM of a query's relations: every pattern's selected rows times
+// its variables, in uint32 cells, three times over (the relation, a re-sort's
+// key and value buffers).
+uint64_t estimate_bytes(vedas::VedasStorage* st, vedas::SparqlQuery& sq) {
+  uint64_t est = 0;
+  for (size_t i = 0; i < sq.getPatternNum(); ++i) {
+    vedas::TriplePattern* tp = sq.getPatternPtr(i);
+    uint64_t rows = tp->estimate_rows;
+    if (sq.getPatternNum() == 1) {
+      auto r = vedas::QueryExecutor::findL2OffsetFromL1(st->getPredicateIndexValues(),
+                                                        st->getPredicateIndexOffsets(), tp->getPredicateId(),
+                                                        st->getTripleSize());
+      rows = r.second >= r.first ? r.second - r.first : 0;
+    }
+    est += rows * std::max<size_t>(tp->getVariableNum(), 1) * 4 * 3;
+  }
+  return est + 4096;
 }
 
-void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts, BatchResult& out) {
-  out.ctx = &ctx;
-  out.queries.clear();
-  out.queries.resize(texts.size());
-  // Host mirrors are created lazily; make them all before planning in parallel.
+}  // namespace
+
+void prepare_mirrors(vedas::VedasStorage* storage) {
   storage->getPredicateIndexValues();
   storage->getPredicateIndexOffsets();
   storage->getPredicateSubjectIndexValues();
@@ -75,92 +92,108 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   storage->getPOdata();
   storage->getPSOdata();
   storage->getPOSdata();
+}
 
-  std::vector<std::unique_ptr<vedas::QueryExecutor>> ex(texts.size());
-  std::vector<std::unique_ptr<vedas::SparqlQuery>> sq(texts.size());
-  std::vector<std::unique_ptr<vedas::QueryPlan>> plan(texts.size());
-  std::vector<size_t> next(texts.size(), 0);
-
-  // Planning (pre-scan, QueryGraph, job list) is host-only: run it in parallel.
-  parallel_for(texts.size(), [&](size_t i) {
-    BatchQuery& q = out.queries[i];
-    guarded(q, [&] {
-      ex[i] = std::make_unique<vedas::QueryExecutor>(storage, &ctx);
-      sq[i] = std::make_unique<vedas::SparqlQuery>(texts[i].c_str());
-      std::set<std::string> sel = sq[i]->getSelectedVariables();
-      plan[i] = std::make_unique<vedas::QueryPlan>(sel);
-      ex[i]->plan(*sq[i], *plan[i]);
-      plan[i]->beginExecution();
-    });
+void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text, PlannedQuery& pq) {
+  guarded(pq.out, [&] {
+    pq.ex = std::make_unique<vedas::QueryExecutor>(storage, &ctx);
+    pq.sq = std::make_unique<vedas::SparqlQuery>(text.c_str());
+    std::set<std::string> sel = pq.sq->getSelectedVariables();
+    pq.plan = std::make_unique<vedas::QueryPlan>(sel);
+    pq.ex->plan(*pq.sq, *pq.plan);
+    pq.plan->beginExecution();
+    pq.est_bytes = estimate_bytes(storage, *pq.sq);
   });
+}
 
-  out.waves = 0;
-  while (true) {
-    std::vector<size_t> active;
-    for (size_t i = 0; i < texts.size(); ++i)
-      if (out.queries[i].status == VG_OK && plan[i] && next[i] < plan[i]->jobNum()) active.push_back(i);
-    if (active.empty()) break;
-    ++out.waves;
+BatchResult::~BatchResult() {
+  if (ctx)
+    for (auto& q : queries) rel_free(*ctx, q.rel);
+}
 
-    struct SelectItem { size_t q; vedas::SelectWork w; };
-    struct JoinItem { size_t q; vedas::JoinQueryJob* job; vedas::JoinWork w; };
-    struct SwapItem { size_t q; vedas::IndexSwapJob* job; vedas::FullRelationIR* ir; };
-    std::vector<SelectItem> sels;
-    std::vector<JoinItem> joins;
-    std::vector<SwapItem> swaps;
-    for (size_t i : active) {
-      vedas::QueryJob* job = plan[i]->getJob(next[i]);
-      BatchQuery& q = out.queries[i];
-      guarded(q, [&] {
+void WaveEngine::add(PlannedQuery* pq) { active_.push_back(pq); }
+
+void WaveEngine::wave(std::vector<PlannedQuery*>& completed) {
+  // Queries that failed while planning, or have no job left, finish now.
+  std::vector<PlannedQuery*> run, done;
+  for (PlannedQuery* q : active_) {
+    if (q->out->status != VG_OK || !q->plan || q->next >= q->plan->jobNum()) done.push_back(q);
+    else run.push_back(q);
+  }
+  if (!run.empty()) {
+    ++waves_;
+    enum Kind { kNone, kSelect, kJoin, kSwap };
+    struct Item {
+      Kind kind = kNone;
+      vedas::SelectWork sw;
+      vedas::JoinQueryJob* jj = nullptr;
+      vedas::JoinWork jw;
+      vedas::IndexSwapJob* xj = nullptr;
+      vedas::FullRelationIR* xir = nullptr;
+    };
+    std::vector<Item> items(run.size());
+    auto t0 = Clock::now();
+    pfor(run.size(), [&](size_t k) {
+      PlannedQuery* q = run[k];
+      vedas::QueryJob* job = q->plan->getJob(q->next);
+      Item& it = items[k];
+      guarded(q->out, [&] {
         if (auto* s = dynamic_cast<vedas::SelectQueryJob*>(job)) {
-          SelectItem it{i, {}};
-          s->prepare(it.w);
-          sels.push_back(std::move(it));
+          s->prepare(it.sw);
+          it.kind = kSelect;
         } else if (auto* j = dynamic_cast<vedas::JoinQueryJob*>(job)) {
-          JoinItem it{i, j, {}};
-          j->prepare(it.w);
-          if (!it.w.empty) joins.push_back(it);
-        } else if (auto* w = dynamic_cast<vedas::IndexSwapJob*>(job)) {
-          swaps.push_back({i, w, w->prepare()});
+          j->prepare(it.jw);
+          it.jj = j;
+          it.kind = it.jw.empty ? kNone : kJoin;
+        } else if (auto* x = dynamic_cast<vedas::IndexSwapJob*>(job)) {
+          it.xj = x;
+          it.xir = x->prepare();
+          it.kind = kSwap;
         } else {
           job->startJob(0);  // transfer: a pass-through on one device
         }
       });
-    }
+      if (q->out->status != VG_OK) it.kind = kNone;
+    });
+    prof.prepare_s += since(t0);
 
     // 1. every stable re-sort by column 0 of this wave in one segmented sort
+    t0 = Clock::now();
     std::vector<Rel*> to_sort;
-    for (auto& it : joins) {
-      if (it.w.sortL) to_sort.push_back(&it.w.lir->rel());
-      if (it.w.sortR) to_sort.push_back(&it.w.rir->rel());
+    for (auto& it : items) {
+      if (it.kind == kJoin) {
+        if (it.jw.sortL) to_sort.push_back(&it.jw.lir->rel());
+        if (it.jw.sortR) to_sort.push_back(&it.jw.rir->rel());
+      } else if (it.kind == kSwap) {
+        to_sort.push_back(&it.xir->rel());
+      }
     }
-    for (auto& it : swaps) to_sort.push_back(&it.ir->rel());
-    batched_sort_by_first(ctx, to_sort);
+    batched_sort_by_first(ctx_, to_sort);
 
-    // 2. index swaps: empty-interval scans need column 0 of small relations
+    // 2. empty-interval scans of swapped relations need column 0 of the small ones
+    std::vector<std::vector<uint32_t>> swap_c0;
+    std::vector<const std::vector<uint32_t>*> swap_c0_of(items.size(), nullptr);
     {
       std::vector<const Rel*> small;
       std::vector<size_t> who;
-      for (size_t k = 0; k < swaps.size(); ++k)
-        if (swaps[k].ir->size() > 2 && swaps[k].ir->size() < 100) {
-          small.push_back(&swaps[k].ir->rel());
+      for (size_t k = 0; k < items.size(); ++k)
+        if (items[k].kind == kSwap && items[k].xir->size() > 2 && items[k].xir->size() < 100) {
+          small.push_back(&items[k].xir->rel());
           who.push_back(k);
         }
-      std::vector<std::vector<uint32_t>> c0;
-      batched_col0(ctx, small, c0);
-      std::vector<const std::vector<uint32_t>*> per(swaps.size(), nullptr);
-      for (size_t m = 0; m < who.size(); ++m) per[who[m]] = &c0[m];
-      for (size_t k = 0; k < swaps.size(); ++k)
-        guarded(out.queries[swaps[k].q], [&] { swaps[k].job->finish(per[k]); });
+      batched_col0(ctx_, small, swap_c0);
+      for (size_t m = 0; m < who.size(); ++m) swap_c0_of[who[m]] = &swap_c0[m];
     }
 
     // 3. selects: all copies in one launch, all unique compactions in one
+    std::vector<uint64_t> kept_of(items.size(), 0);
     {
       std::vector<CopyPiece> pieces;
       std::vector<SegRows> useg;
       std::vector<size_t> uwho;
-      for (size_t k = 0; k < sels.size(); ++k) {
-        auto& w = sels[k].w;
+      for (size_t k = 0; k < items.size(); ++k) {
+        if (items[k].kind != kSelect) continue;
+        auto& w = items[k].sw;
         if (w.unique) {
           SegRows s;
           s.ncols = 1;
@@ -173,85 +206,139 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
           pieces.insert(pieces.end(), w.pieces.begin(), w.pieces.end());
         }
       }
-      batched_copy(ctx, pieces);
-      std::vector<uint64_t> kept = batched_unique(ctx, useg);
-      for (size_t m = 0; m < uwho.size(); ++m) vedas::SelectQueryJob::finishUnique(sels[uwho[m]].w, kept[m]);
+      batched_copy(ctx_, pieces);
+      std::vector<uint64_t> kept = batched_unique(ctx_, useg);
+      for (size_t m = 0; m < uwho.size(); ++m) kept_of[uwho[m]] = kept[m];
     }
 
     // 4. joins: one count / scan / write chain for all of them
-    if (!joins.empty()) {
+    std::vector<size_t> jwho;
+    std::vector<Rel> jouts;
+    std::vector<uint32_t> jfl;
+    std::vector<std::vector<uint32_t>> join_c0;
+    std::vector<const std::vector<uint32_t>*> join_c0_of(items.size(), nullptr);
+    {
       std::vector<const Rel*> L, R;
-      for (auto& it : joins) {
-        L.push_back(&it.w.lir->rel());
-        R.push_back(&it.w.rir->rel());
-      }
-      std::vector<Rel> outs;
-      std::vector<uint32_t> fl;
-      batched_join(ctx, L, R, outs, fl);
+      for (size_t k = 0; k < items.size(); ++k)
+        if (items[k].kind == kJoin) {
+          L.push_back(&items[k].jw.lir->rel());
+          R.push_back(&items[k].jw.rir->rel());
+          jwho.push_back(k);
+        }
+      batched_join(ctx_, L, R, jouts, jfl);
       std::vector<const Rel*> small;
       std::vector<size_t> who;
-      for (size_t k = 0; k < joins.size(); ++k)
-        if (!joins[k].job->isLastJoinForVar() && outs[k].nrows > 2 && outs[k].nrows < 100) {
-          small.push_back(&outs[k]);
-          who.push_back(k);
+      for (size_t m = 0; m < jwho.size(); ++m)
+        if (!items[jwho[m]].jj->isLastJoinForVar() && jouts[m].nrows > 2 && jouts[m].nrows < 100) {
+          small.push_back(&jouts[m]);
+          who.push_back(jwho[m]);
         }
-      std::vector<std::vector<uint32_t>> c0;
-      batched_col0(ctx, small, c0);
-      std::vector<const std::vector<uint32_t>*> per(joins.size(), nullptr);
-      for (size_t m = 0; m < who.size(); ++m) per[who[m]] = &c0[m];
-      for (size_t k = 0; k < joins.size(); ++k) {
-        BatchQuery& q = out.queries[joins[k].q];
-        if (!guarded(q, [&] { joins[k].job->finish(joins[k].w, outs[k], fl[2 * k], fl[2 * k + 1], per[k]); }))
-          rel_free(ctx, outs[k]);
-      }
+      batched_col0(ctx_, small, join_c0);
+      for (size_t m = 0; m < who.size(); ++m) join_c0_of[who[m]] = &join_c0[m];
     }
-    for (size_t i : active) ++next[i];
-  }
+    prof.device_s += since(t0);
 
-  // Projection and the final adjacent-unique pass of every query at once.
+    // 5. host finishing of every job of the wave
+    t0 = Clock::now();
+    std::vector<size_t> jpos(items.size(), 0);
+    for (size_t m = 0; m < jwho.size(); ++m) jpos[jwho[m]] = m;
+    pfor(items.size(), [&](size_t k) {
+      Item& it = items[k];
+      BatchQuery* out = run[k]->out;
+      if (it.kind == kSwap) {
+        guarded(out, [&] { it.xj->finish(swap_c0_of[k]); });
+      } else if (it.kind == kSelect) {
+        if (it.sw.unique) vedas::SelectQueryJob::finishUnique(it.sw, kept_of[k]);
+      } else if (it.kind == kJoin) {
+        const size_t m = jpos[k];
+        if (!guarded(out, [&] { it.jj->finish(it.jw, jouts[m], jfl[2 * m], jfl[2 * m + 1], join_c0_of[k]); }))
+          rel_free(ctx_, jouts[m]);
+      }
+    });
+    for (PlannedQuery* q : run) {
+      ++q->next;
+      if (q->out->status != VG_OK || q->next >= q->plan->jobNum()) done.push_back(q);
+    }
+    prof.finish_s += since(t0);
+  }
+  if (!done.empty()) {
+    auto t0 = Clock::now();
+    finalize(done, completed);
+    prof.final_s += since(t0);
+  }
+  std::vector<PlannedQuery*> still;
+  for (PlannedQuery* q : active_)
+    if (std::find(done.begin(), done.end(), q) == done.end()) still.push_back(q);
+  active_.swap(still);
+}
+
+// Projection and the final adjacent-unique pass (QueryPlan::execute, after
+// its job loop) of every query that just finished, in one batched launch.
+void WaveEngine::finalize(std::vector<PlannedQuery*>& done, std::vector<PlannedQuery*>& completed) {
   std::vector<SegRows> fin;
-  std::vector<size_t> fwho;
+  std::vector<PlannedQuery*> fq;
   std::vector<vedas::FullRelationIR*> fres;
-  for (size_t i = 0; i < texts.size(); ++i) {
-    BatchQuery& q = out.queries[i];
-    if (q.status != VG_OK || !plan[i]) continue;
-    guarded(q, [&] {
-      vedas::FullRelationIR* res = plan[i]->project();
+  for (PlannedQuery* q : done) {
+    BatchQuery* out = q->out;
+    if (out->status != VG_OK || !q->plan) continue;
+    guarded(out, [&] {
+      vedas::FullRelationIR* res = q->plan->project();
       SegRows s;
       s.ncols = static_cast<uint32_t>(res->getColumnNum());
       s.n = res->size();
       for (uint32_t c = 0; c < s.ncols; ++c) {
         s.in[c] = res->getRelationRawPointer(c);
-        s.out[c] = ctx.alloc<uint32_t>(s.n);
+        s.out[c] = ctx_.alloc<uint32_t>(s.n);
       }
       fin.push_back(s);
-      fwho.push_back(i);
+      fq.push_back(q);
       fres.push_back(res);
     });
   }
-  std::vector<uint64_t> kept = batched_unique(ctx, fin);
-  for (size_t m = 0; m < fwho.size(); ++m) {
-    BatchQuery& q = out.queries[fwho[m]];
+  std::vector<uint64_t> kept = batched_unique(ctx_, fin);
+  for (size_t m = 0; m < fq.size(); ++m) {
+    BatchQuery* out = fq[m]->out;
     vedas::FullRelationIR* res = fres[m];
-    for (size_t c = 0; c < res->getColumnNum(); ++c) q.headers.push_back(res->getHeader(c));
+    for (size_t c = 0; c < res->getColumnNum(); ++c) out->headers.push_back(res->getHeader(c));
     Rel r = res->release();
-    rel_free(ctx, r);
+    rel_free(ctx_, r);
     Rel o;
     o.ncols = fin[m].ncols;
     o.nrows = kept[m];
     for (uint32_t c = 0; c < o.ncols; ++c) {
       o.cols[c] = fin[m].out[c];
-      ctx.arena.shrink(o.cols[c], o.nrows * sizeof(uint32_t));
+      ctx_.arena.shrink(o.cols[c], o.nrows * sizeof(uint32_t));
     }
-    q.rel = o;
-    q.log = ex[fwho[m]]->exe_log;
+    out->rel = o;
   }
-  for (size_t i = 0; i < texts.size(); ++i) {
-    BatchQuery& q = out.queries[i];
-    if (q.status != VG_OK && ex[i]) q.log = ex[i]->exe_log;
+  for (PlannedQuery* q : done) {
+    if (q->ex) q->out->log = q->ex->exe_log;
+    q->plan.reset();  // frees every intermediate relation of the query
+    completed.push_back(q);
   }
-  plan.clear();  // frees every intermediate relation
+}
+
+void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts, BatchResult& out) {
+  auto t_all = Clock::now();
+  out.ctx = &ctx;
+  out.queries.clear();
+  out.queries.resize(texts.size());
+  prepare_mirrors(storage);
+  std::vector<PlannedQuery> pq(texts.size());
+  auto t0 = Clock::now();
+  pfor(texts.size(), [&](size_t i) {
+    pq[i].out = &out.queries[i];
+    plan_query(ctx, storage, texts[i], pq[i]);
+  });
+  WaveEngine eng(ctx);
+  eng.prof.plan_s = since(t0);
+  for (auto& q : pq) eng.add(&q);
+  std::vector<PlannedQuery*> completed;
+  while (eng.active() > 0) eng.wave(completed);
+  out.waves = eng.waves();
+  out.prof = eng.prof;
   ctx.check_device_errors();
+  out.prof.total_s = since(t_all);
 }
 
 }  // namespace vg

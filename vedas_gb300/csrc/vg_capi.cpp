@@ -5,6 +5,7 @@
 #include <string>
 
 #include "compat/vedas_compat.h"
+#include "vg_batch.h"
 #include "vg_batch_host.h"
 #include "vg_ctx.h"
 #include "vg_index.h"
@@ -402,6 +403,54 @@ vg_status vg_result_free(vg_result* r) {
   return VG_OK;
 }
 
+namespace {
+int describe(vedas::PlanTreeNode* n, vedas::SparqlQuery& sq, std::string& out, int& counter) {
+  if (!n) return -1;
+  int a = -1, b = -1;
+  if (n->child1) a = describe(n->child1, sq, out, counter);
+  if (n->child2) b = describe(n->child2, sq, out, counter);
+  if (n->op == vedas::UPLOAD) {
+    std::string idx = "-";
+    if (n->tp->getVariableNum() == 2) idx = (n->tp->getSubject() == n->var) ? "PSO" : "POS";
+    out += "U" + std::to_string(n->tp->getId()) + ":" + idx + ";";
+  } else if (n->op == vedas::JOIN) {
+    out += "J" + std::to_string(a) + "," + std::to_string(b) + ":" + n->var + ":" + (n->reuseVar ? "0" : "1") + ";";
+  } else {
+    out += "W" + std::to_string(a) + ":" + n->var + ";";
+  }
+  return counter++;
+}
+}  // namespace
+
+vg_status vg_plan_describe(const char* sparql, const uint64_t* est, uint32_t n, char* buf, size_t cap) {
+  if (!sparql || !buf || (n && !est)) return VG_ERR_INVALID;
+  return guard([&] {
+    vedas::SparqlQuery sq(sparql);
+    for (uint32_t i = 0; i < n && i < sq.getPatternNum(); ++i) sq.getPatternPtr(i)->estimate_rows = est[i];
+    vedas::QueryGraph qg(&sq);
+    vedas::PlanTreeNode* root = qg.generateQueryPlan();
+    std::string s;
+    int counter = 0;
+    describe(root, sq, s, counter);
+    if (s.size() + 1 > cap) vg::fail(VG_ERR_OVERFLOW, "plan text exceeds the buffer");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+  });
+}
+
+vg_status vg_eid_sequence(const uint64_t* quads, uint32_t n, uint64_t out4[4]) {
+  if ((n && !quads) || !out4 || n == 0) return VG_ERR_INVALID;
+  return guard([&] {
+    vedas::EmptyIntervalDict d;
+    for (uint32_t i = 0; i < n; ++i)
+      d.updateBound("?x", quads[4 * i], quads[4 * i + 1], quads[4 * i + 2], quads[4 * i + 3]);
+    vedas::VAR_BOUND v = d.getBound("?x");
+    out4[0] = std::get<0>(v);
+    out4[1] = std::get<1>(v);
+    out4[2] = std::get<2>(v);
+    out4[3] = std::get<3>(v);
+  });
+}
+
 vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, vg_batch** out) {
   if (!ctx || !ix || !out || (nq && !queries)) return VG_ERR_INVALID;
   *out = nullptr;
@@ -418,6 +467,17 @@ vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, ui
 
 uint32_t vg_batch_size(const vg_batch* b) { return b ? static_cast<uint32_t>(b->r.queries.size()) : 0; }
 uint32_t vg_batch_waves(const vg_batch* b) { return b ? b->r.waves : 0; }
+vg_status vg_batch_profile(const vg_batch* b, double out6[6]) {
+  if (!b || !out6) return VG_ERR_INVALID;
+  const vg::BatchProfile& p = b->r.prof;
+  out6[0] = p.plan_s;
+  out6[1] = p.prepare_s;
+  out6[2] = p.device_s;
+  out6[3] = p.finish_s;
+  out6[4] = p.final_s;
+  out6[5] = p.total_s;
+  return VG_OK;
+}
 vg_status vg_batch_query_status(const vg_batch* b, uint32_t q) {
   return (b && q < b->r.queries.size()) ? b->r.queries[q].status : VG_ERR_INVALID;
 }
@@ -445,6 +505,34 @@ vg_status vg_batch_download(const vg_batch* b, uint32_t q, uint32_t c, uint32_t*
     vg::download(*b->r.ctx, r.cols[c], r.nrows, host);
   });
 }
+uint64_t vg_batch_result_words(const vg_batch* b) {
+  if (!b) return 0;
+  uint64_t w = 0;
+  for (const auto& q : b->r.queries) w += q.rel.nrows * q.rel.ncols;
+  return w;
+}
+
+vg_status vg_batch_download_all(const vg_batch* b, uint32_t* host) {
+  if (!b) return VG_ERR_INVALID;
+  return guard([&] {
+    vg::Ctx& ctx = *b->r.ctx;
+    const uint64_t words = vg_batch_result_words(b);
+    if (words == 0) return;
+    if (!host) vg::fail(VG_ERR_INVALID, "null host buffer");
+    vg::Scratch<uint32_t> stage(ctx, words);
+    std::vector<vg::CopyPiece> pieces;
+    uint64_t off = 0;
+    for (const auto& q : b->r.queries)
+      for (uint32_t c = 0; c < q.rel.ncols; ++c) {
+        pieces.push_back({q.rel.cols[c], stage.get() + off, q.rel.nrows});
+        off += q.rel.nrows;
+      }
+    vg::batched_copy(ctx, pieces);
+    VG_CUDA(cudaMemcpyAsync(host, stage.get(), words * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+  });
+}
+
 uint32_t vg_batch_nlog(const vg_batch* b, uint32_t q) {
   return (b && q < b->r.queries.size()) ? static_cast<uint32_t>(b->r.queries[q].log.size()) : 0;
 }
