@@ -232,6 +232,37 @@ void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint6
                   uint64_t* p3);
 vg_status vg_batch_free(vg_batch* b);
 
+/* ---- serving (continuous batching) -------------------------------------- */
+typedef struct vg_server vg_server;
+
+/* Starts a serving loop on the context: one worker thread owns the device.
+ * Submitted queries are planned on the caller's thread, then admitted first
+ * come first served at wave boundaries while the sum of their estimated
+ * relation bytes stays within `budget_bytes`; admitted queries share the
+ * batched launches of every wave until they finish.  Replaces vdQuery's REPL
+ * loop (src/VedasQuery.cu:136-205), which runs one query at a time.
+ * Only vg_serve_* calls may use the context while the server runs. */
+vg_status vg_serve_start(vg_ctx* ctx, vg_index* ix, size_t budget_bytes, vg_server** out);
+/* Queues one query; `ticket` identifies it.  A query whose estimate alone
+ * exceeds the budget finishes at once with VG_ERR_REJECTED. */
+vg_status vg_serve_submit(vg_server* s, const char* sparql, uint64_t* ticket);
+/* Waits up to timeout_s seconds (< 0: forever); *done = 1 when finished. */
+vg_status vg_serve_wait(vg_server* s, uint64_t ticket, double timeout_s, int* done);
+/* The finished query's own status, and its result (as for vg_result_*). */
+vg_status vg_serve_query_status(vg_server* s, uint64_t ticket);
+uint32_t vg_serve_ncols(vg_server* s, uint64_t ticket);
+uint64_t vg_serve_nrows(vg_server* s, uint64_t ticket);
+const char* vg_serve_header(vg_server* s, uint64_t ticket, uint32_t c);
+vg_status vg_serve_download(vg_server* s, uint64_t ticket, uint32_t c, uint32_t* host);
+/* Seconds from submission to admission and to completion. */
+vg_status vg_serve_latency(vg_server* s, uint64_t ticket, double* queued_s, double* total_s);
+/* Frees a finished query's result. */
+vg_status vg_serve_release(vg_server* s, uint64_t ticket);
+/* out6 = {submitted, completed, rejected, waves, reserved bytes, peak queries in flight}. */
+vg_status vg_serve_stats(vg_server* s, uint64_t out6[6]);
+/* Lets the queries in flight finish, then stops the worker. */
+vg_status vg_serve_stop(vg_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,104 @@
+"""The full-size configurations: the 100M-triple graph against the oracle,
+and the 500M-triple hub graph through size-independent properties."""
+import numpy as np
+import pytest
+
+from oracle import oracle_py
+from vedas_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def big_ctx(built):
+    import vedas_gb300 as vg
+    c = vg.Context(0, arena_bytes=120 << 30)
+    yield c
+    c.close()
+
+
+def _same(res, ref):
+    cols = res.columns()
+    assert res.headers == ref.headers
+    for a, b in zip(cols, ref.columns):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_c2_100m_index_chain_and_batch_match_oracle(big_ctx):
+    import vedas_gb300 as vg
+    g = workloads.graph_chain()                      # 100M triples, seed 0
+    ix = vg.Index(big_ctx, g.s, g.p, g.o)
+    ox = oracle_py.OracleIndex(g.s, g.p, g.o)
+    for name in ("p_idx_values", "p_idx_offsets", "ps_s_idx_values", "ps_idx_offsets", "po_o_idx_values",
+                 "po_idx_offsets", "ps_data", "po_data", "pso_data", "pos_data"):
+        np.testing.assert_array_equal(ix.array(name), ox.array(name), err_msg=name)
+    q = workloads.chain_query(g)                     # ?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 c
+    r = ox.query(q)
+    assert r.status == 0
+    res = ix.query(q)
+    _same(res, r)
+    assert [x[0] for x in res.log()].count("SWAP") >= 2          # index swaps between the joins
+    qs = workloads.query_mix(g, 96, seed=3)
+    b = vg.Batch(ix, qs)
+    for i, qq in enumerate(qs):
+        rr = ox.query(qq)
+        if rr.status != 0:
+            assert b.status(i) != 0
+            continue
+        assert b.headers(i) == rr.headers
+        for x, y in zip(b.columns(i), rr.columns):
+            np.testing.assert_array_equal(x, y)
+    b.close()
+    ix.close()
+
+
+def _gpu_dedup(g):
+    """Sorted set of the triples, deduplicated on the device (test input prep)."""
+    import torch
+    bs = int(g.s.max()).bit_length()
+    bo = int(g.o.max()).bit_length()
+    key = (torch.from_numpy(g.p.astype(np.int64)) << (bs + bo)) | (torch.from_numpy(g.s.astype(np.int64)) << bo) \
+        | torch.from_numpy(g.o.astype(np.int64))
+    u = torch.unique(key.cuda()).cpu().numpy()
+    o = (u & ((1 << bo) - 1)).astype(np.uint32)
+    s = ((u >> bo) & ((1 << bs) - 1)).astype(np.uint32)
+    p = (u >> (bs + bo)).astype(np.uint32)
+    return workloads.Graph(s, p, o, g.name + "_set")
+
+
+def test_c3_500m_index_properties_and_star_count(big_ctx):
+    import vedas_gb300 as vg
+    g = _gpu_dedup(workloads.graph_hub(dedup=False))  # 500M generated, then made a set
+    n = g.n
+    ix = vg.Index(big_ctx, g.s, g.p, g.o)
+    pv, po = ix.array("p_idx_values"), ix.array("p_idx_offsets")
+    cnt = np.bincount(g.p)
+    np.testing.assert_array_equal(pv, np.nonzero(cnt)[0].astype(np.uint32))
+    np.testing.assert_array_equal(np.diff(np.append(po.astype(np.int64), n)), cnt[pv])
+    ps, pso = ix.array("ps_data"), ix.array("pso_data")
+    pos, poo = ix.array("pos_data"), ix.array("po_data")
+    # permutations of the same multiset
+    for a, b in ((ps, g.s), (pso, g.o), (pos, g.s), (poo, g.o)):
+        assert int(a.sum(dtype=np.uint64)) == int(b.sum(dtype=np.uint64))
+    # (p, s, o) order and its level-2 boundaries
+    prow = np.repeat(pv, cnt[pv]).astype(np.uint64)
+    k1 = (prow << np.uint64(32)) | ps.astype(np.uint64)
+    d = np.diff(k1)
+    assert (k1[1:] >= k1[:-1]).all()
+    assert ((d > 0) | (pso[1:] > pso[:-1])).all()                 # strict: a set
+    starts = np.flatnonzero(np.concatenate(([True], d > 0)))
+    np.testing.assert_array_equal(ix.array("ps_idx_offsets"), starts.astype(np.uint32))
+    np.testing.assert_array_equal(ix.array("ps_s_idx_values"), ps[starts])
+    del k1, d, starts
+    k2 = (prow << np.uint64(32)) | poo.astype(np.uint64)
+    assert (k2[1:] >= k2[:-1]).all()
+    del k2, prow
+    # a two-pattern subject star: sum over subjects of the two out-degrees
+    pa, pb = 3, 7
+    da = np.bincount(g.s[g.p == pa], minlength=int(g.s.max()) + 1).astype(np.int64)
+    db = np.bincount(g.s[g.p == pb], minlength=int(g.s.max()) + 1).astype(np.int64)
+    res = ix.query(workloads.star_query(pa, pb))
+    assert res.nrows == int((da * db).sum())
+    c0 = res.columns()[0]
+    assert (c0[1:] >= c0[:-1]).all()
+    ix.close()

@@ -108,6 +108,19 @@ def lib():
             "vg_batch_log": (None, [vp, u32, u32, pu32, ctypes.POINTER(u64), ctypes.POINTER(u64),
                                     ctypes.POINTER(u64)]),
             "vg_batch_free": (i32, [vp]),
+            "vg_serve_start": (i32, [vp, vp, ctypes.c_size_t, ctypes.POINTER(vp)]),
+            "vg_serve_submit": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64)]),
+            "vg_serve_wait": (i32, [vp, u64, ctypes.c_double, ctypes.POINTER(i32)]),
+            "vg_serve_query_status": (i32, [vp, u64]),
+            "vg_serve_ncols": (u32, [vp, u64]),
+            "vg_serve_nrows": (u64, [vp, u64]),
+            "vg_serve_header": (ctypes.c_char_p, [vp, u64, u32]),
+            "vg_serve_download": (i32, [vp, u64, u32, pu32]),
+            "vg_serve_latency": (i32, [vp, u64, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_double)]),
+            "vg_serve_release": (i32, [vp, u64]),
+            "vg_serve_stats": (i32, [vp, ctypes.POINTER(u64)]),
+            "vg_serve_stop": (i32, [vp]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -353,6 +366,65 @@ class Batch:
 
     def __del__(self):
         self.close()
+
+
+class Server:
+    """Continuous-batching serving loop (vg_serve_*)."""
+
+    def __init__(self, ix: "Index", budget_bytes: int):
+        h = ctypes.c_void_p()
+        check(lib().vg_serve_start(ix.ctx.h, ix.h, budget_bytes, ctypes.byref(h)))
+        self.h = h
+
+    def submit(self, sparql: str) -> int:
+        t = ctypes.c_uint64()
+        check(lib().vg_serve_submit(self.h, sparql.encode(), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = -1.0) -> bool:
+        done = ctypes.c_int()
+        check(lib().vg_serve_wait(self.h, ticket, timeout_s, ctypes.byref(done)))
+        return bool(done.value)
+
+    def status(self, ticket: int) -> int:
+        return int(lib().vg_serve_query_status(self.h, ticket))
+
+    def headers(self, ticket: int):
+        L = lib()
+        return [L.vg_serve_header(self.h, ticket, c).decode() for c in range(L.vg_serve_ncols(self.h, ticket))]
+
+    def columns(self, ticket: int):
+        L = lib()
+        n = int(L.vg_serve_nrows(self.h, ticket))
+        out = []
+        for c in range(L.vg_serve_ncols(self.h, ticket)):
+            a = np.zeros(n, dtype=np.uint32)
+            if n:
+                check(L.vg_serve_download(self.h, ticket, c, _p32(a)))
+            out.append(a)
+        return out
+
+    def latency(self, ticket: int):
+        q, t = ctypes.c_double(), ctypes.c_double()
+        check(lib().vg_serve_latency(self.h, ticket, ctypes.byref(q), ctypes.byref(t)))
+        return q.value, t.value
+
+    def release(self, ticket: int) -> None:
+        check(lib().vg_serve_release(self.h, ticket))
+
+    def stats(self) -> dict:
+        out = (ctypes.c_uint64 * 6)()
+        check(lib().vg_serve_stats(self.h, out))
+        keys = ["submitted", "completed", "rejected", "waves", "reserved_bytes", "peak_inflight"]
+        return dict(zip(keys, [int(x) for x in out]))
+
+    def stop(self) -> None:
+        if getattr(self, "h", None):
+            lib().vg_serve_stop(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.stop()
 
 
 class Relation:

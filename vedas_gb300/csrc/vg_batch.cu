@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "vg_join_tile.cuh"
 #include "vg_prims.cuh"
 #include "vg_sort.h"
 
@@ -155,29 +156,19 @@ struct JoinSeg {
   uint64_t row0;   // offset of this join's left rows in the lo/cnt/offs arrays
 };
 
-__global__ void __launch_bounds__(kBlock) bjoin_count_kernel(const JoinSeg* __restrict__ js,
-                                                             const uint64_t* __restrict__ bstart, uint32_t J,
-                                                             uint32_t* __restrict__ lo, uint32_t* __restrict__ cnt) {
-  __shared__ uint64_t s_win[2];
+// One block per tile of kJcTile left keys of one join (block -> join by the
+// per-join tile prefix); the right-key window is staged by a bulk copy.
+__global__ void __launch_bounds__(kJcBlock) bjoin_count_kernel(const JoinSeg* __restrict__ js,
+                                                               const uint64_t* __restrict__ bstart, uint32_t J,
+                                                               uint32_t* __restrict__ lo, uint32_t* __restrict__ cnt,
+                                                               DeviceErrors* err) {
+  __shared__ JoinCountSmem sm;
   __shared__ uint32_t s_j;
   if (threadIdx.x == 0) s_j = seg_of(bstart, J, blockIdx.x);
   __syncthreads();
   const JoinSeg g = js[s_j];
-  const uint64_t i0 = (blockIdx.x - bstart[s_j]) * kBlock;
-  if (threadIdx.x == 0) {
-    const uint64_t i1 = (i0 + kBlock < g.nl ? i0 + kBlock : g.nl) - 1;
-    const uint64_t w0 = lower_bound_dev(g.rk, 0, g.nr, g.lk[i0]);
-    s_win[0] = w0;
-    s_win[1] = upper_bound_dev(g.rk, w0, g.nr, g.lk[i1]);
-  }
-  __syncthreads();
-  const uint64_t i = i0 + threadIdx.x;
-  if (i >= g.nl) return;
-  const uint32_t k = g.lk[i];
-  const uint64_t a = lower_bound_dev(g.rk, s_win[0], s_win[1], k);
-  const uint64_t b = upper_bound_dev(g.rk, a, s_win[1], k);
-  lo[g.row0 + i] = static_cast<uint32_t>(a);
-  cnt[g.row0 + i] = static_cast<uint32_t>(b - a);
+  const uint64_t i0 = (blockIdx.x - bstart[s_j]) * static_cast<uint64_t>(kJcTile);
+  join_count_tile(g.lk, g.nl, g.rk, g.nr, i0, lo + g.row0, cnt + g.row0, sm, err);
 }
 
 __global__ void __launch_bounds__(kBlock) bjoin_scan_kernel(const JoinSeg* __restrict__ js,
@@ -418,7 +409,7 @@ void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<
     if (l[j]->ncols + r[j]->ncols - 1 > VG_MAX_COLS) fail(VG_ERR_UNSUPPORTED, "join output has more than 9 columns");
     js[j] = {l[j]->cols[0], r[j]->cols[0], l[j]->nrows, r[j]->nrows, rows};
     rows += l[j]->nrows;
-    bstart[j + 1] = bstart[j] + div_up(l[j]->nrows, kBlock);
+    bstart[j + 1] = bstart[j] + div_up(l[j]->nrows, kJcTile);
     tstart[j + 1] = tstart[j] + div_up(l[j]->nrows, kTileRows);
     cbytes += 4.0 * (l[j]->nrows + r[j]->nrows);
   }
@@ -431,7 +422,8 @@ void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<
   VG_CUDA(cudaMemsetAsync(status.get(), 0, tstart[J] * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(uint32_t), ctx.stream));
   ctx.launch("join_count", cbytes, [&] {
-    bjoin_count_kernel<<<static_cast<unsigned>(bstart[J]), kBlock, 0, ctx.stream>>>(djs, dbs, J, lo.get(), cnt.get());
+    bjoin_count_kernel<<<static_cast<unsigned>(bstart[J]), kJcBlock, 0, ctx.stream>>>(djs, dbs, J, lo.get(),
+                                                                                    cnt.get(), ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
   ctx.launch("join_scan", 12.0 * rows, [&] {

@@ -47,6 +47,8 @@ class WaveEngine {
   explicit WaveEngine(Ctx& ctx) : ctx_(ctx) {}
   void add(PlannedQuery* pq);
   size_t active() const { return active_.size(); }
+  // Forgets every query in flight (after a device-level failure).
+  void reset() { active_.clear(); }
   void wave(std::vector<PlannedQuery*>& completed);
   uint32_t waves() const { return waves_; }
   BatchProfile prof;

@@ -8,6 +8,7 @@
 #include "vg_batch.h"
 #include "vg_batch_host.h"
 #include "vg_ctx.h"
+#include "vg_serve.h"
 #include "vg_index.h"
 #include "vg_relops.h"
 
@@ -22,6 +23,10 @@ struct vg_index {
 
 struct vg_batch {
   vg::BatchResult r;
+};
+
+struct vg_server {
+  std::unique_ptr<vg::Server> srv;
 };
 
 struct vg_result {
@@ -548,6 +553,93 @@ void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint6
 vg_status vg_batch_free(vg_batch* b) {
   delete b;
   return VG_OK;
+}
+
+vg_status vg_serve_start(vg_ctx* ctx, vg_index* ix, size_t budget_bytes, vg_server** out) {
+  if (!ctx || !ix || !out) return VG_ERR_INVALID;
+  *out = nullptr;
+  auto s = std::make_unique<vg_server>();
+  vg_status st = guard([&] { s->srv = std::make_unique<vg::Server>(ctx->c, ix->st.get(), budget_bytes); });
+  if (st == VG_OK) *out = s.release();
+  return st;
+}
+
+vg_status vg_serve_submit(vg_server* s, const char* sparql, uint64_t* ticket) {
+  if (!s || !sparql || !ticket) return VG_ERR_INVALID;
+  return guard([&] { *ticket = s->srv->submit(sparql); });
+}
+
+vg_status vg_serve_wait(vg_server* s, uint64_t ticket, double timeout_s, int* done) {
+  if (!s || !done) return VG_ERR_INVALID;
+  return guard([&] { *done = s->srv->wait(ticket, timeout_s) ? 1 : 0; });
+}
+
+vg_status vg_serve_query_status(vg_server* s, uint64_t ticket) {
+  if (!s) return VG_ERR_INVALID;
+  vg_status qs = VG_OK;
+  vg_status st = guard([&] {
+    vg::ServeItem* it = s->srv->get(ticket);
+    if (!it->done) vg::fail(VG_ERR_INVALID, "query still running");
+    qs = it->q.status;
+    if (qs != VG_OK) g_last_error = it->q.error;
+  });
+  return st != VG_OK ? st : qs;
+}
+
+uint32_t vg_serve_ncols(vg_server* s, uint64_t ticket) {
+  uint32_t n = 0;
+  if (s) guard([&] { n = static_cast<uint32_t>(s->srv->get(ticket)->q.headers.size()); });
+  return n;
+}
+
+uint64_t vg_serve_nrows(vg_server* s, uint64_t ticket) {
+  uint64_t n = 0;
+  if (s) guard([&] { n = s->srv->get(ticket)->q.rel.nrows; });
+  return n;
+}
+
+const char* vg_serve_header(vg_server* s, uint64_t ticket, uint32_t c) {
+  const char* h = nullptr;
+  if (s)
+    guard([&] {
+      vg::ServeItem* it = s->srv->get(ticket);
+      if (c < it->q.headers.size()) h = it->q.headers[c].c_str();
+    });
+  return h;
+}
+
+vg_status vg_serve_download(vg_server* s, uint64_t ticket, uint32_t c, uint32_t* host) {
+  if (!s) return VG_ERR_INVALID;
+  return guard([&] { s->srv->download(ticket, c, host); });
+}
+
+vg_status vg_serve_latency(vg_server* s, uint64_t ticket, double* queued_s, double* total_s) {
+  if (!s) return VG_ERR_INVALID;
+  return guard([&] {
+    vg::ServeItem* it = s->srv->get(ticket);
+    if (!it->done) vg::fail(VG_ERR_INVALID, "query still running");
+    const bool admitted = it->t_admit.time_since_epoch().count() != 0;
+    if (queued_s)
+      *queued_s = admitted ? std::chrono::duration<double>(it->t_admit - it->t_submit).count() : 0.0;
+    if (total_s) *total_s = std::chrono::duration<double>(it->t_done - it->t_submit).count();
+  });
+}
+
+vg_status vg_serve_release(vg_server* s, uint64_t ticket) {
+  if (!s) return VG_ERR_INVALID;
+  return guard([&] { s->srv->release(ticket); });
+}
+
+vg_status vg_serve_stats(vg_server* s, uint64_t out6[6]) {
+  if (!s || !out6) return VG_ERR_INVALID;
+  return guard([&] { s->srv->stats(out6); });
+}
+
+vg_status vg_serve_stop(vg_server* s) {
+  if (!s) return VG_OK;
+  vg_status st = guard([&] { s->srv.reset(); });
+  delete s;
+  return st;
 }
 
 }  // extern "C"

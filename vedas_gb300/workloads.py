@@ -59,13 +59,18 @@ def _zipf_probs(k: int, s: float) -> np.ndarray:
     return w / w.sum()
 
 
+def _bits(x) -> int:
+    m = int(x.max(initial=0))
+    return max(1, m.bit_length())
+
+
 def _dedup(s, p, o, n_target):
     """Remove duplicate triples keeping first occurrences, then cut to n_target."""
-    key = (p.astype(np.uint64) << np.uint64(58)) ^ (s.astype(np.uint64) << np.uint64(29)) \
-        ^ o.astype(np.uint64)
-    # key is injective for s < 2^29, o < 2^29, p < 2^6; fall back to a
-    # structured unique otherwise.
-    if s.max(initial=0) < (1 << 29) and o.max(initial=0) < (1 << 29) and p.max(initial=0) < 64:
+    bs, bp, bo = _bits(s), _bits(p), _bits(o)
+    if bs + bp + bo <= 64:
+        # (p, s, o) packed at their bit widths: injective
+        key = (p.astype(np.uint64) << np.uint64(bs + bo)) | (s.astype(np.uint64) << np.uint64(bo)) \
+            | o.astype(np.uint64)
         _, first = np.unique(key, return_index=True)
     else:
         rec = np.rec.fromarrays([s, p, o])
@@ -225,6 +230,57 @@ def query_mix(g: Graph, n_queries: int, seed: int = 0, cs: ConstantSampler | Non
         ts = by_shape[sh]
         out.append(instantiate(ts[rng.integers(0, len(ts))], cs, rng))
     return out
+
+
+def graph_hub(n: int = 500_000_000, n_entities: int = 10_000_000, n_predicates: int = 86,
+              zipf_s: float = 1.0, mean_degree: float = 3.0, hub_frac: float = 0.01,
+              hub_share: float = 0.3, alpha: float = 2.1, literal_frac: float = 0.2,
+              seed: int = 0, dedup: bool = True) -> Graph:
+    """The 500M-triple graph of the large-query and serving workloads.
+
+    Like graph_chain, plus heavy-tailed in-degree: hub_frac of the entities
+    are hubs that receive hub_share of all object slots, hub k of rank r with
+    weight r^(-1/(alpha-1)) (a power law of in-degree with exponent alpha).
+    Remaining objects are literal_frac literals and uniform entities.
+    dedup=False keeps repeated triples, as the reference's loader does
+    (src/loader.cu:19-53); it spares the 500M-element host sort.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pairs = int(n / mean_degree * 1.03) + 1024
+    ps = rng.integers(1, n_entities + 1, size=pairs, dtype=np.uint32)
+    pp = (rng.choice(n_predicates, size=pairs, p=_zipf_probs(n_predicates, zipf_s)) + 1).astype(np.uint32)
+    deg = rng.geometric(1.0 / mean_degree, size=pairs).astype(np.int64)
+    csum = np.cumsum(deg)
+    take = int(np.searchsorted(csum, int(n * 1.005) + 1024)) + 1
+    s = np.repeat(ps[:take], deg[:take])
+    p = np.repeat(pp[:take], deg[:take])
+    del ps, pp, deg, csum
+    m = s.shape[0]
+    n_hubs = max(1, int(n_entities * hub_frac))
+    hubs = (rng.choice(n_entities, size=n_hubs, replace=False) + 1).astype(np.uint32)
+    w = np.arange(1, n_hubs + 1, dtype=np.float64) ** (-1.0 / (alpha - 1.0))
+    w /= w.sum()
+    u = rng.random(m, dtype=np.float32)
+    o = rng.integers(1, n_entities + 1, size=m, dtype=np.uint32)
+    lit = u >= 1.0 - literal_frac
+    o[lit] = rng.integers(LITERAL_START_ID, LITERAL_START_ID + max(1, n_entities // 10),
+                          size=int(lit.sum()), dtype=np.uint32)
+    hub = u < hub_share
+    o[hub] = hubs[rng.choice(n_hubs, size=int(hub.sum()), p=w)]
+    del u, lit, hub
+    if dedup:
+        s, p, o = _dedup(s, p, o, n)
+    else:
+        s, p, o = s[:n], p[:n], o[:n]
+    return Graph(s, p, o, f"hub_n{n}")
+
+
+def snowflake_query(preds=(1, 2, 3, 4, 5, 6, 7)) -> str:
+    """Seven-pattern snowflake: two three-pattern stars (?x, ?y) joined by one
+    object-subject edge (?x p4 ?y)."""
+    a, b, c, d, e, f, g = preds
+    return (f"SELECT * WHERE {{ ?x <{a}> ?a . ?x <{b}> ?b . ?x <{c}> ?c . ?x <{d}> ?y . "
+            f"?y <{e}> ?e . ?y <{f}> ?f . ?y <{g}> ?g . }}")
 
 
 def star_query(pa: int = 3, pb: int = 7) -> str:
