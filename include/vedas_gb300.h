@@ -144,6 +144,29 @@ vg_status vg_select(vg_ctx* ctx, vg_index* ix, const vg_select_desc* d, vg_ir* o
  * first_last receives out column 0's first and last value when rows > 0. */
 vg_status vg_join(vg_ctx* ctx, const vg_ir* l, const vg_ir* r, vg_ir* out,
                   uint32_t first_last[2]);
+/* The join above for callers that cannot allocate device memory: it takes
+ * no vg_ctx and allocates nothing (no cudaMalloc, cudaFree or allocating
+ * library call).  This entry point has no counterpart in the reference.
+ * Hosts that have divided all HBM among their own pools, or serving threads
+ * that may only launch work, cannot give the core an arena; this variant
+ * keeps its scratch in a fixed file-scope device array instead, which caps
+ * l_rows at 2,097,152 (larger inputs return VG_ERR_OVERFLOW) and costs about
+ * 32 MiB on every GPU that loads the library, until the process exits.
+ * Columns are device pointers, column 0 of each side its sorted join key;
+ * out_cols are l_ncols + r_ncols - 1 caller-allocated device buffers of
+ * out_capacity rows.  *out_rows receives the result row count; when it
+ * exceeds out_capacity nothing is written and VG_ERR_OVERFLOW is returned.
+ * Runs on `stream` (a cudaStream_t, 0 = default) and returns after the join
+ * finished.  The first call on each device looks up the scratch address
+ * (make it before any stream capture).  All calls share the scratch: calls
+ * that overlap on the GPU race.  Errors are described by
+ * vg_noalloc_last_error(). */
+vg_status vg_join_noalloc(const uint32_t* const* l_cols, uint32_t l_ncols, uint64_t l_rows,
+                          const uint32_t* const* r_cols, uint32_t r_ncols, uint64_t r_rows,
+                          uint32_t* const* out_cols, uint64_t out_capacity, uint64_t* out_rows,
+                          void* stream);
+const char* vg_noalloc_last_error(void);
+
 /* Two-variable join: keys are (column 0, column 1) of each side, both
  * sorted lexicographically by them; output column 0..1 = keys, then the
  * rest of l, then the rest of r (src/JoinQueryJob.cu:181-225, :360-377). */

@@ -378,6 +378,39 @@ void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
   VG_CUDA(cudaGetLastError());
 }
 
+uint64_t join_into(cudaStream_t stream, int num_sms, const Rel& l, const Rel& r, uint32_t* const* out_cols,
+                   uint64_t capacity, uint32_t* lo, uint32_t* cnt, uint64_t* offs, uint64_t* status,
+                   uint32_t* ticket, uint64_t* total, DeviceErrors* err) {
+  (void)num_sms;
+  if (l.nrows == 0 || r.nrows == 0) return 0;
+  const uint32_t ncols = l.ncols + r.ncols - 1;
+  KeyOf<false> kl{l.cols[0], nullptr}, kr{r.cols[0], nullptr};
+  join_count_kernel<false><<<static_cast<unsigned>(div_up(l.nrows, kBlock)), kBlock, 0, stream>>>(
+      kl, l.nrows, kr, r.nrows, lo, cnt);
+  VG_CUDA(cudaGetLastError());
+  const uint64_t tiles = div_up(l.nrows, kTileRows);
+  scan_counts_kernel<<<static_cast<unsigned>(tiles), kBlock, 0, stream>>>(cnt, offs, l.nrows, status, ticket,
+                                                                         total, tiles, err);
+  VG_CUDA(cudaGetLastError());
+  uint64_t t = 0;
+  VG_CUDA(cudaMemcpyAsync(&t, total, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+  VG_CUDA(cudaStreamSynchronize(stream));
+  if (t == 0 || t > capacity) return t;
+  JoinWriteArgs a{};
+  a.offs = offs;
+  a.lo = lo;
+  a.nl = l.nrows;
+  a.total = t;
+  for (uint32_t c = 0; c < l.ncols; ++c) a.lc[c] = l.cols[c];
+  for (uint32_t c = 1; c < r.ncols; ++c) a.rc[c - 1] = r.cols[c];
+  for (uint32_t c = 0; c < ncols; ++c) a.oc[c] = out_cols[c];
+  a.nlc = l.ncols;
+  a.nrc = r.ncols - 1;
+  join_write_kernel<<<static_cast<unsigned>(div_up(t, kTileRows)), kBlock, 0, stream>>>(a);
+  VG_CUDA(cudaGetLastError());
+  return t;
+}
+
 void gather_cols(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, uint32_t ncols,
                  const uint32_t* perm, uint64_t n) {
   if (n == 0 || ncols == 0) return;

@@ -35,6 +35,14 @@ uint64_t unique_rows(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, 
 // ordered by (left row, right row).  Allocates `out` from the arena.
 void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out);
 
+// The same join on a caller's stream with caller-provided scratch and output
+// columns (nothing is allocated): lo/cnt/offs hold l.nrows entries, status
+// div_up(l.nrows, 2048) words; status, ticket and err must be zero.  Returns
+// the result row count; the outputs are written only when it fits `capacity`.
+uint64_t join_into(cudaStream_t stream, int num_sms, const Rel& l, const Rel& r, uint32_t* const* out_cols,
+                   uint64_t capacity, uint32_t* lo, uint32_t* cnt, uint64_t* offs, uint64_t* status,
+                   uint32_t* ticket, uint64_t* total, DeviceErrors* err);
+
 // out[c][i] = in[c][perm[i]] for every column.
 void gather_cols(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, uint32_t ncols,
                  const uint32_t* perm, uint64_t n);
