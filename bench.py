@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=256, help="queries per CPU-baseline step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--arena-gb", type=float, default=0.0,
+                    help="HBM arena size (0: 90%% of free memory; profilers need room to replay)")
     return ap.parse_args()
 
 
@@ -264,7 +266,7 @@ def bench_ours(args, rank, world, local, pg):
     import vedas_gb300 as vg
 
     g, queries = make_workload(args, rank)
-    ctx = vg.Context(local, arena_bytes=0)
+    ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
     t0 = time.perf_counter()
     ix = vg.Index(ctx, g.s, g.p, g.o)
     ctx.sync()
@@ -388,7 +390,7 @@ def bench_serve(args, rank, world, local, pg):
                              mix={"S": 0.6, "C": 0.3, "F": 0.1})
     rng = np.random.Generator(np.random.PCG64(args.seed + 99 + rank))
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n_q))
-    ctx = vg.Context(local, arena_bytes=0)
+    ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
     ix = vg.Index(ctx, g.s, g.p, g.o)
     srv = vg.Server(ix, budget_bytes=int(args.budget_gb * (1 << 30)))
     for q in qs[:64]:                      # warm-up: first waves, host mirrors

@@ -13,6 +13,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <thread>
 
 #include "vg_batch.h"
@@ -27,22 +30,91 @@ double since(Clock::time_point t0) {
   return std::chrono::duration<double>(Clock::now() - t0).count();
 }
 
+// Persistent host workers for the per-query phases of a wave.  run() hands
+// out indices through one atomic counter; the calling thread works too.
+class WorkerPool {
+ public:
+  static WorkerPool& get() {
+    static WorkerPool pool;
+    return pool;
+  }
+
+  void run(size_t n, const std::function<void(size_t)>& f) {
+    std::lock_guard<std::mutex> serial(run_mu_);  // one parallel loop at a time
+    if (n < 64 || workers_.empty()) {
+      for (size_t i = 0; i < n; ++i) f(i);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &f;
+      n_ = n;
+      next_.store(0);
+      busy_ = workers_.size();
+      ++gen_;
+    }
+    cv_.notify_all();
+    drain(f, n);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return busy_ == 0; });
+    fn_ = nullptr;
+  }
+
+  ~WorkerPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+  }
+
+ private:
+  WorkerPool() {
+    unsigned hw = std::thread::hardware_concurrency();
+    unsigned nt = hw > 1 ? std::min<unsigned>(hw - 1, 31) : 0;
+    for (unsigned t = 0; t < nt; ++t) workers_.emplace_back([this] { loop(); });
+  }
+
+  void drain(const std::function<void(size_t)>& f, size_t n) {
+    for (size_t i = next_.fetch_add(1); i < n; i = next_.fetch_add(1)) f(i);
+  }
+
+  void loop() {
+    uint64_t seen = 0;
+    while (true) {
+      const std::function<void(size_t)>* f;
+      size_t n;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+        f = fn_;
+        n = n_;
+      }
+      if (f) drain(*f, n);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--busy_ == 0) done_cv_.notify_all();
+    }
+  }
+
+  std::vector<std::thread> workers_;
+  std::mutex mu_, run_mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(size_t)>* fn_ = nullptr;
+  size_t n_ = 0;
+  std::atomic<size_t> next_{0};
+  size_t busy_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
 template <typename F>
 void pfor(size_t n, F&& f) {
-  unsigned hw = std::thread::hardware_concurrency();
-  unsigned nt = hw ? std::min<unsigned>(hw, 32) : 4;
-  if (n < 128 || nt <= 1) {
-    for (size_t i = 0; i < n; ++i) f(i);
-    return;
-  }
-  nt = static_cast<unsigned>(std::min<size_t>(nt, (n + 63) / 64));
-  std::atomic<size_t> next{0};
-  std::vector<std::thread> th;
-  for (unsigned t = 0; t < nt; ++t)
-    th.emplace_back([&] {
-      for (size_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) f(i);
-    });
-  for (auto& t : th) t.join();
+  std::function<void(size_t)> fn = f;
+  WorkerPool::get().run(n, fn);
 }
 
 template <typename F>

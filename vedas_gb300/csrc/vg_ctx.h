@@ -7,16 +7,20 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "vg_common.cuh"
 
 namespace vg {
 
-// First-fit allocator over one cudaMalloc'd slab.  Allocation is host-side
-// bookkeeping only (no device call), so intermediate relations never pay a
-// cudaMalloc.  All work on the slab is ordered on the context stream, so a
-// block may be handed out again as soon as the work that last used it has
+// Allocator over one cudaMalloc'd slab.  Allocation is host-side bookkeeping
+// only (no device call), so intermediate relations never pay a cudaMalloc.
+// Blocks up to kSmallMax come from per-size-class free lists (power-of-two
+// classes carved from chunks of the slab): O(1), which matters when thousands
+// of queries allocate their relations at once.  Larger blocks are best-fit
+// with coalescing.  All work on the slab is ordered on the context stream, so
+// a block may be handed out again as soon as the work that last used it has
 // been enqueued.
 class Arena {
  public:
@@ -28,7 +32,8 @@ class Arena {
   void* alloc(size_t bytes);      // throws VG_ERR_OOM
   void* try_alloc(size_t bytes);  // nullptr when it does not fit
   void free(void* p);
-  // Returns the tail of a live block beyond new_bytes to the free list.
+  // Returns the tail of a live large block beyond new_bytes to the free list
+  // (small blocks keep their class).
   void shrink(void* p, size_t new_bytes);
   size_t capacity() const { return cap_; }
   size_t used() const { return used_; }
@@ -37,11 +42,21 @@ class Arena {
 
  private:
   static constexpr size_t kAlign = 256;
+  static constexpr int kClasses = 13;                  // 256 B .. 1 MiB
+  static constexpr size_t kSmallMax = kAlign << (kClasses - 1);
+  static constexpr size_t kChunk = 4u << 20;           // small-class chunk
   char* base_ = nullptr;
   size_t cap_ = 0, used_ = 0, peak_ = 0;
-  std::map<size_t, size_t> free_;   // offset -> size
-  std::map<size_t, size_t> live_;   // offset -> size
+  std::map<size_t, size_t> free_;                      // offset -> size (large free blocks)
+  std::multimap<size_t, size_t> by_size_;              // size -> offset (same blocks)
+  std::unordered_map<size_t, size_t> live_;            // offset -> size (large live blocks)
+  std::vector<size_t> small_free_[kClasses];           // offsets of free small blocks
+  std::unordered_map<size_t, int> small_live_;         // offset -> class
   mutable std::mutex mu_;
+
+  size_t big_alloc(size_t bytes);                      // SIZE_MAX when it does not fit
+  void big_free(size_t off, size_t sz);
+  void erase_by_size(size_t sz, size_t off);
 };
 
 // Per-kernel accounting: launches, algorithmic bytes (the bytes the

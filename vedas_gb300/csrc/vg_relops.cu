@@ -4,6 +4,7 @@
 
 #include <algorithm>
 
+#include "vg_join_tile.cuh"
 #include "vg_prims.cuh"
 #include "vg_sort.h"
 
@@ -168,6 +169,16 @@ __global__ void __launch_bounds__(kBlock) join_count_kernel(KeyOf<TWO> L, uint64
   const uint64_t hi = key_upper_bound(R, lo, s_win[1], k);
   lo_out[i] = static_cast<uint32_t>(lo);
   cnt_out[i] = static_cast<uint32_t>(hi - lo);
+}
+
+// One block per 2048 left keys; the right-key window is staged in shared
+// memory by a bulk copy (vg_join_tile.cuh).
+__global__ void __launch_bounds__(kJcBlock) join_count_tiled_kernel(const uint32_t* __restrict__ L, uint64_t nl,
+                                                                    const uint32_t* __restrict__ R, uint64_t nr,
+                                                                    uint32_t* __restrict__ lo,
+                                                                    uint32_t* __restrict__ cnt, DeviceErrors* err) {
+  __shared__ JoinCountSmem sm;
+  join_count_tile(L, nl, R, nr, static_cast<uint64_t>(blockIdx.x) * kJcTile, lo, cnt, sm, err);
 }
 
 // Exclusive scan of uint32 counts into uint64 offsets (+ total).
@@ -340,9 +351,9 @@ void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
       join_count_kernel<true><<<cgrid, kBlock, 0, ctx.stream>>>(kl, l.nrows, kr, r.nrows, lo.get(), cnt.get());
     });
   } else {
-    KeyOf<false> kl{l.cols[0], nullptr}, kr{r.cols[0], nullptr};
     ctx.launch("join_count", cbytes, [&] {
-      join_count_kernel<false><<<cgrid, kBlock, 0, ctx.stream>>>(kl, l.nrows, kr, r.nrows, lo.get(), cnt.get());
+      join_count_tiled_kernel<<<static_cast<unsigned>(div_up(l.nrows, kJcTile)), kJcBlock, 0, ctx.stream>>>(
+          l.cols[0], l.nrows, r.cols[0], r.nrows, lo.get(), cnt.get(), ctx.d_err);
     });
   }
   VG_CUDA(cudaGetLastError());
