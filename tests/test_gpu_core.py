@@ -90,7 +90,11 @@ def test_unique_adjacent(ctx):
 
 
 @pytest.mark.parametrize("nl,nr,keys", [(1, 1, 3), (1000, 5000, 50), (70_000, 90_000, 30_000),
-                                        (5000, 300_000, 3)])
+                                        (5000, 300_000, 3),
+                                        # windows of right keys larger than shared memory: lockstep
+                                        # searches in global memory
+                                        (20_000, 3_000_000, 1_000_000), (3, 2_000_000, 10),
+                                        (50_000, 4_000_000, 1 << 31)])
 def test_join_matches_oracle(ctx, nl, nr, keys):
     import vedas_gb300 as vg
     rng = np.random.Generator(np.random.PCG64(nl + nr))

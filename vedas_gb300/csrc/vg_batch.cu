@@ -38,34 +38,65 @@ unsigned grid_cap(const Ctx& ctx, uint64_t units, int per_thread) {
 }
 
 // ---------------------------------------------------------------------------
+constexpr int kCopyPer = 4;                                   // 16-byte chunks per thread per tile
+constexpr uint64_t kCopyTile = static_cast<uint64_t>(kBlock) * kCopyPer;
+
+// Copies every piece; destination chunks are 16-byte aligned (head and tail
+// elements are copied by the piece's first chunk).  Blocks take tiles of
+// kCopyTile consecutive chunks; the pieces a tile covers are found once per
+// tile, so a thread's piece lookup is a search over those few pieces only.
 __global__ void __launch_bounds__(kBlock) bcopy_kernel(const CopyPiece* __restrict__ p,
                                                        const uint64_t* __restrict__ cstart, uint32_t P) {
+  __shared__ uint32_t s_k[2];
   const uint64_t total = cstart[P];
-  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
-  for (uint64_t q = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; q < total; q += stride) {
-    const uint32_t k = seg_of(cstart, P, q);
-    const CopyPiece pc = p[k];
-    const uint64_t c = q - cstart[k];
-    const uint64_t head = (4 - ((reinterpret_cast<uintptr_t>(pc.dst) >> 2) & 3)) & 3;
-    const uint64_t h = head < pc.len ? head : pc.len;
-    if (c == 0) {
-      for (uint64_t e = 0; e < h; ++e) pc.dst[e] = pc.src[e];
-      const uint64_t body = (pc.len - h) / 4 * 4;
-      for (uint64_t e = h + body; e < pc.len; ++e) pc.dst[e] = pc.src[e];
+  const uint64_t ntiles = (total + kCopyTile - 1) / kCopyTile;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint64_t q0 = t * kCopyTile;
+    const uint64_t q1 = (q0 + kCopyTile < total) ? q0 + kCopyTile : total;
+    if (threadIdx.x == 0) s_k[0] = seg_of(cstart, P, q0);
+    if (threadIdx.x == 32) s_k[1] = seg_of(cstart, P, q1 - 1);
+    __syncthreads();
+    const uint32_t k0 = s_k[0], k1 = s_k[1];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kCopyPer; ++i) {
+      const uint64_t q = q0 + static_cast<uint64_t>(i) * kBlock + threadIdx.x;
+      if (q >= q1) break;
+      uint32_t k = k0;
+      if (k1 > k0) {
+        uint32_t lo = k0, hi = k1;   // last k in [k0, k1] with cstart[k] <= q
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi + 1) >> 1;
+          if (cstart[mid] <= q) lo = mid;
+          else hi = mid - 1;
+        }
+        k = lo;
+      }
+      const CopyPiece pc = p[k];
+      const uint64_t c = q - cstart[k];
+      const uint64_t head = (4 - ((reinterpret_cast<uintptr_t>(pc.dst) >> 2) & 3)) & 3;
+      const uint64_t h = head < pc.len ? head : pc.len;
+      if (c == 0) {
+        for (uint64_t e = 0; e < h; ++e) pc.dst[e] = pc.src[e];
+        const uint64_t body = (pc.len - h) / 4 * 4;
+        for (uint64_t e = h + body; e < pc.len; ++e) pc.dst[e] = pc.src[e];
+      }
+      const uint64_t e0 = h + c * 4;
+      if (e0 + 4 > pc.len) continue;
+      const uint32_t* s = pc.src + e0;
+      uint4 v;
+      // vectors [s - sh, s - sh + 8) stay inside the piece for every chunk
+      // but the first and the last
+      if (c > 0 && e0 + 8 <= pc.len) {
+        v = load4_realigned(s);
+      } else {
+        v.x = s[0];
+        v.y = s[1];
+        v.z = s[2];
+        v.w = s[3];
+      }
+      *reinterpret_cast<uint4*>(pc.dst + e0) = v;
     }
-    const uint64_t e0 = h + c * 4;
-    if (e0 + 4 > pc.len) continue;
-    const uint32_t* s = pc.src + e0;
-    uint4 v;
-    if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
-      v = *reinterpret_cast<const uint4*>(s);
-    } else {
-      v.x = s[0];
-      v.y = s[1];
-      v.z = s[2];
-      v.w = s[3];
-    }
-    *reinterpret_cast<uint4*>(pc.dst + e0) = v;
   }
 }
 
@@ -158,7 +189,7 @@ struct JoinSeg {
 
 // One block per tile of kJcTile left keys of one join (block -> join by the
 // per-join tile prefix); the right-key window is staged by a bulk copy.
-__global__ void __launch_bounds__(kJcBlock) bjoin_count_kernel(const JoinSeg* __restrict__ js,
+__global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_kernel(const JoinSeg* __restrict__ js,
                                                                const uint64_t* __restrict__ bstart, uint32_t J,
                                                                uint32_t* __restrict__ lo, uint32_t* __restrict__ cnt,
                                                                DeviceErrors* err) {
@@ -295,7 +326,7 @@ void batched_copy(Ctx& ctx, const std::vector<CopyPiece>& pieces) {
   uint64_t* dc = upload(ctx, cstart);
   const uint32_t P = static_cast<uint32_t>(p.size());
   ctx.launch("select_copy", bytes, [&] {
-    bcopy_kernel<<<grid_cap(ctx, cstart.back(), 2), kBlock, 0, ctx.stream>>>(dp, dc, P);
+    bcopy_kernel<<<grid_cap(ctx, cstart.back(), kCopyPer), kBlock, 0, ctx.stream>>>(dp, dc, P);
   });
   VG_CUDA(cudaGetLastError());
   ctx.free(dp);

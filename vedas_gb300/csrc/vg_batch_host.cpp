@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
+#include <cstdlib>
 #include <functional>
 #include <mutex>
 #include <thread>
@@ -71,9 +72,15 @@ class WorkerPool {
   }
 
  private:
+  // VG_HOST_THREADS sets the number of host threads of a parallel phase,
+  // the calling thread included (default: the hardware threads, at most 32).
   WorkerPool() {
-    unsigned hw = std::thread::hardware_concurrency();
-    unsigned nt = hw > 1 ? std::min<unsigned>(hw - 1, 31) : 0;
+    unsigned total = std::thread::hardware_concurrency();
+    if (const char* e = std::getenv("VG_HOST_THREADS")) {
+      const long v = std::strtol(e, nullptr, 10);
+      if (v >= 1) total = static_cast<unsigned>(v);
+    }
+    const unsigned nt = total > 1 ? std::min<unsigned>(total - 1, 31) : 0;
     for (unsigned t = 0; t < nt; ++t) workers_.emplace_back([this] { loop(); });
   }
 
@@ -338,56 +345,67 @@ void WaveEngine::wave(std::vector<PlannedQuery*>& completed) {
     finalize(done, completed);
     prof.final_s += since(t0);
   }
+  for (PlannedQuery* q : done) q->retired = true;
   std::vector<PlannedQuery*> still;
   for (PlannedQuery* q : active_)
-    if (std::find(done.begin(), done.end(), q) == done.end()) still.push_back(q);
+    if (!q->retired) still.push_back(q);
   active_.swap(still);
 }
 
 // Projection and the final adjacent-unique pass (QueryPlan::execute, after
 // its job loop) of every query that just finished, in one batched launch.
 void WaveEngine::finalize(std::vector<PlannedQuery*>& done, std::vector<PlannedQuery*>& completed) {
-  std::vector<SegRows> fin;
-  std::vector<PlannedQuery*> fq;
-  std::vector<vedas::FullRelationIR*> fres;
-  for (PlannedQuery* q : done) {
+  // 1. projection and output buffers, per query on the host pool
+  std::vector<SegRows> seg(done.size());
+  std::vector<vedas::FullRelationIR*> res(done.size(), nullptr);
+  pfor(done.size(), [&](size_t k) {
+    PlannedQuery* q = done[k];
     BatchQuery* out = q->out;
-    if (out->status != VG_OK || !q->plan) continue;
+    if (out->status != VG_OK || !q->plan) return;
     guarded(out, [&] {
-      vedas::FullRelationIR* res = q->plan->project();
-      SegRows s;
-      s.ncols = static_cast<uint32_t>(res->getColumnNum());
-      s.n = res->size();
+      vedas::FullRelationIR* r = q->plan->project();
+      SegRows& s = seg[k];
+      s.ncols = static_cast<uint32_t>(r->getColumnNum());
+      s.n = r->size();
       for (uint32_t c = 0; c < s.ncols; ++c) {
-        s.in[c] = res->getRelationRawPointer(c);
+        s.in[c] = r->getRelationRawPointer(c);
         s.out[c] = ctx_.alloc<uint32_t>(s.n);
       }
-      fin.push_back(s);
-      fq.push_back(q);
-      fres.push_back(res);
+      res[k] = r;
     });
-  }
-  std::vector<uint64_t> kept = batched_unique(ctx_, fin);
-  for (size_t m = 0; m < fq.size(); ++m) {
-    BatchQuery* out = fq[m]->out;
-    vedas::FullRelationIR* res = fres[m];
-    for (size_t c = 0; c < res->getColumnNum(); ++c) out->headers.push_back(res->getHeader(c));
-    Rel r = res->release();
-    rel_free(ctx_, r);
-    Rel o;
-    o.ncols = fin[m].ncols;
-    o.nrows = kept[m];
-    for (uint32_t c = 0; c < o.ncols; ++c) {
-      o.cols[c] = fin[m].out[c];
-      ctx_.arena.shrink(o.cols[c], o.nrows * sizeof(uint32_t));
+  });
+  // 2. one batched adjacent-unique pass over all of them
+  std::vector<SegRows> fin;
+  std::vector<size_t> who;
+  for (size_t k = 0; k < done.size(); ++k)
+    if (res[k]) {
+      fin.push_back(seg[k]);
+      who.push_back(k);
     }
-    out->rel = o;
-  }
-  for (PlannedQuery* q : done) {
-    if (q->ex) q->out->log = q->ex->exe_log;
+  std::vector<uint64_t> kept = batched_unique(ctx_, fin);
+  std::vector<uint64_t> kept_of(done.size(), 0);
+  for (size_t m = 0; m < who.size(); ++m) kept_of[who[m]] = kept[m];
+  // 3. results handed over, intermediates freed, per query on the host pool
+  pfor(done.size(), [&](size_t k) {
+    PlannedQuery* q = done[k];
+    BatchQuery* out = q->out;
+    if (vedas::FullRelationIR* r = res[k]) {
+      for (size_t c = 0; c < r->getColumnNum(); ++c) out->headers.push_back(r->getHeader(c));
+      Rel in = r->release();
+      rel_free(ctx_, in);
+      Rel o;
+      o.ncols = seg[k].ncols;
+      o.nrows = kept_of[k];
+      for (uint32_t c = 0; c < o.ncols; ++c) {
+        o.cols[c] = seg[k].out[c];
+        ctx_.arena.shrink(o.cols[c], o.nrows * sizeof(uint32_t));
+      }
+      out->rel = o;
+    }
+    if (q->ex) out->log = std::move(q->ex->exe_log);
     q->plan.reset();  // frees every intermediate relation of the query
-    completed.push_back(q);
-  }
+  });
+  for (PlannedQuery* q : done) completed.push_back(q);
 }
 
 void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts, BatchResult& out) {

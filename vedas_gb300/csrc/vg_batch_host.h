@@ -31,6 +31,7 @@ struct PlannedQuery {
   size_t next = 0;
   uint64_t est_bytes = 0;   // estimated HBM for its relations (admission)
   BatchQuery* out = nullptr;
+  bool retired = false;     // handed back by the wave engine
 };
 
 // Plans one query on the host (thread-safe across queries once the storage's

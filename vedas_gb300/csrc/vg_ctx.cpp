@@ -15,7 +15,7 @@ void Arena::init(size_t bytes) {
   small_live_.clear();
   for (auto& v : small_free_) v.clear();
   free_[0] = bytes;
-  by_size_.emplace(bytes, 0);
+  by_size_.emplace(bytes, size_t{0});
   used_ = peak_ = 0;
 }
 
@@ -30,18 +30,11 @@ void Arena::release() {
   for (auto& v : small_free_) v.clear();
 }
 
-void Arena::erase_by_size(size_t sz, size_t off) {
-  auto r = by_size_.equal_range(sz);
-  for (auto it = r.first; it != r.second; ++it)
-    if (it->second == off) {
-      by_size_.erase(it);
-      return;
-    }
-}
+void Arena::erase_by_size(size_t sz, size_t off) { by_size_.erase({sz, off}); }
 
 // Best fit among the large free blocks; the remainder stays free.
 size_t Arena::big_alloc(size_t bytes) {
-  auto it = by_size_.lower_bound(bytes);
+  auto it = by_size_.lower_bound({bytes, size_t{0}});
   if (it == by_size_.end()) return SIZE_MAX;
   const size_t sz = it->first, off = it->second;
   by_size_.erase(it);

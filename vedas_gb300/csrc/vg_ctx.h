@@ -6,6 +6,7 @@
 
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -48,7 +49,7 @@ class Arena {
   char* base_ = nullptr;
   size_t cap_ = 0, used_ = 0, peak_ = 0;
   std::map<size_t, size_t> free_;                      // offset -> size (large free blocks)
-  std::multimap<size_t, size_t> by_size_;              // size -> offset (same blocks)
+  std::set<std::pair<size_t, size_t>> by_size_;        // (size, offset) of the same blocks
   std::unordered_map<size_t, size_t> live_;            // offset -> size (large live blocks)
   std::vector<size_t> small_free_[kClasses];           // offsets of free small blocks
   std::unordered_map<size_t, int> small_live_;         // offset -> class

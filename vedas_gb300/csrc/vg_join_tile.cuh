@@ -39,23 +39,92 @@ __device__ __forceinline__ uint64_t smem_upper(const uint32_t* keys, uint64_t ba
   return lo;
 }
 
+// First index in R[lo, hi) whose key is not below `key` (kUpper: above it),
+// found by one warp: each round 31 lanes probe evenly spaced keys and the
+// ballot of their comparisons narrows the range 32-fold, so a search over
+// 10^8 keys takes six rounds of parallel loads instead of 27 dependent ones.
+// Every lane of the warp must call it with the same arguments.
+template <bool kUpper>
+__device__ __forceinline__ uint64_t warp_bound(const uint32_t* __restrict__ R, uint64_t lo, uint64_t hi,
+                                               uint32_t key) {
+  const uint32_t lane = threadIdx.x & 31;
+  while (hi - lo > 32) {
+    const uint64_t step = (hi - lo + 31) >> 5;
+    const uint64_t p = lo + static_cast<uint64_t>(lane + 1) * step;
+    bool below = false;
+    if (lane < 31 && p < hi) {
+      const uint32_t a = __ldg(R + p);
+      below = kUpper ? (a <= key) : (a < key);
+    }
+    const uint32_t c = __popc(__ballot_sync(0xffffffffu, below));
+    const uint64_t nlo = c ? lo + static_cast<uint64_t>(c) * step + 1 : lo;
+    const uint64_t cap = lo + static_cast<uint64_t>(c + 1) * step;
+    hi = cap < hi ? cap : hi;
+    lo = nlo;
+  }
+  bool below = false;
+  if (lo + lane < hi) {
+    const uint32_t a = __ldg(R + lo + lane);
+    below = kUpper ? (a <= key) : (a < key);
+  }
+  return lo + __popc(__ballot_sync(0xffffffffu, below));
+}
+
+// Lower and upper bounds of K keys in R[w0, w1) at once: branchless binary
+// searches advanced in lockstep, so each round has 2K independent loads in
+// flight instead of one dependent chain per key.
+template <int K>
+__device__ __forceinline__ void lockstep_bounds(const uint32_t* __restrict__ R, uint64_t w0, uint64_t w1,
+                                                const uint32_t (&key)[K], uint64_t (&lo)[K], uint64_t (&hi)[K]) {
+  if (w1 <= w0) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) lo[j] = hi[j] = w0;
+    return;
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) lo[j] = hi[j] = w0;
+  uint64_t n = w1 - w0;
+  while (n > 1) {
+    const uint64_t half = n >> 1;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const uint32_t a = __ldg(R + lo[j] + half);
+      const uint32_t b = __ldg(R + hi[j] + half);
+      lo[j] = (a < key[j]) ? lo[j] + half : lo[j];
+      hi[j] = (b <= key[j]) ? hi[j] + half : hi[j];
+    }
+    n -= half;
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    lo[j] += (__ldg(R + lo[j]) < key[j]) ? 1 : 0;
+    hi[j] += (__ldg(R + hi[j]) <= key[j]) ? 1 : 0;
+  }
+}
+
 // Lower bound (in R) and match count of L[i0, min(i0 + kJcTile, nl)).  R is
 // sorted; the window of R that can match the tile, [lower(L[i0]),
-// upper(L[last])), is staged in shared memory when it fits: its 16-byte
-// aligned middle by one cp.async.bulk completed on an mbarrier, its ragged
-// ends by plain loads.  A window that does not fit (a heavy key, or a right
-// side much larger than the left) is searched in global memory instead.
+// upper(L[last])), is found by two warps at once and staged in shared memory
+// when it fits: its 16-byte aligned middle by one cp.async.bulk completed on
+// an mbarrier, its ragged ends by plain loads.  A window that does not fit (a
+// heavy key, or a right side much larger than the left) is searched in global
+// memory with lockstep bounds instead.
 __device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, uint64_t nl,
                                                 const uint32_t* __restrict__ R, uint64_t nr, uint64_t i0,
                                                 uint32_t* __restrict__ lo_out, uint32_t* __restrict__ cnt_out,
                                                 JoinCountSmem& sm, DeviceErrors* err) {
   const uint32_t tid = threadIdx.x;
   const uint64_t i_end = (i0 + kJcTile < nl) ? i0 + kJcTile : nl;
+  if (tid < 32) {
+    const uint64_t w0 = warp_bound<false>(R, 0, nr, L[i0]);
+    if (tid == 0) sm.w0 = w0;
+  } else if (tid < 64) {
+    const uint64_t w1 = warp_bound<true>(R, 0, nr, L[i_end - 1]);
+    if (tid == 32) sm.w1 = w1;
+  }
+  __syncthreads();
   if (tid == 0) {
-    const uint64_t w0 = lower_bound_dev(R, 0, nr, L[i0]);
-    const uint64_t w1 = upper_bound_dev(R, w0, nr, L[i_end - 1]);
-    sm.w0 = w0;
-    sm.w1 = w1;
+    const uint64_t w0 = sm.w0, w1 = sm.w1;
     sm.staged = 0;
     sm.failed = 0;
     if (w1 > w0 && w1 - w0 <= kJcWindow) {
@@ -73,7 +142,7 @@ __device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, 
     }
   }
   __syncthreads();
-  const uint64_t w0 = sm.w0, w1 = sm.w1;
+  const uint64_t w0 = sm.w0, w1 = sm.w1 > sm.w0 ? sm.w1 : sm.w0;
   const uint32_t staged = sm.staged;
   const uint64_t base = w0 & ~3ull;
   if (staged) {
@@ -91,21 +160,36 @@ __device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, 
   }
   __syncthreads();
   const bool use_smem = staged != 0 && sm.failed == 0;
+  const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
+  if (first >= i_end) return;
 
+  if (!use_smem) {
+    uint32_t key[kJcKeys];
+    uint64_t lo[kJcKeys], hi[kJcKeys];
+#pragma unroll
+    for (int j = 0; j < kJcKeys; ++j) {
+      const uint64_t i = first + j;
+      key[j] = L[i < i_end ? i : i_end - 1];
+    }
+    lockstep_bounds<kJcKeys>(R, w0, w1, key, lo, hi);
+#pragma unroll
+    for (int j = 0; j < kJcKeys; ++j) {
+      const uint64_t i = first + j;
+      if (i < i_end) {
+        lo_out[i] = static_cast<uint32_t>(lo[j]);
+        cnt_out[i] = static_cast<uint32_t>(hi[j] - lo[j]);
+      }
+    }
+    return;
+  }
   uint64_t prev = w0;
 #pragma unroll
   for (int j = 0; j < kJcKeys; ++j) {
-    const uint64_t i = i0 + static_cast<uint64_t>(tid) * kJcKeys + j;
+    const uint64_t i = first + j;
     if (i >= i_end) break;
     const uint32_t key = L[i];
-    uint64_t lo, hi;
-    if (use_smem) {
-      lo = smem_lower(sm.keys, base, prev, w1, key);
-      hi = smem_upper(sm.keys, base, lo, w1, key);
-    } else {
-      lo = lower_bound_dev(R, prev, w1, key);
-      hi = upper_bound_dev(R, lo, w1, key);
-    }
+    const uint64_t lo = smem_lower(sm.keys, base, prev, w1, key);
+    const uint64_t hi = smem_upper(sm.keys, base, lo, w1, key);
     prev = lo;
     lo_out[i] = static_cast<uint32_t>(lo);
     cnt_out[i] = static_cast<uint32_t>(hi - lo);

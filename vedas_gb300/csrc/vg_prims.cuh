@@ -225,4 +225,20 @@ __device__ __forceinline__ uint64_t upper_bound_dev(const T* a, uint64_t lo, uin
   return lo;
 }
 
+// Four source elements starting at s, read as aligned 16-byte vectors: the
+// vector holding s and, when s is not 16-byte aligned, the next one.  Only
+// called where both vectors lie inside the piece.
+__device__ __forceinline__ uint4 load4_realigned(const uint32_t* s) {
+  const uint32_t sh = static_cast<uint32_t>(reinterpret_cast<uintptr_t>(s) >> 2) & 3u;
+  const uint4* a = reinterpret_cast<const uint4*>(s - sh);
+  const uint4 x = __ldg(a);
+  if (sh == 0) return x;
+  const uint4 y = __ldg(a + 1);
+  uint4 v;
+  if (sh == 1) v = make_uint4(x.y, x.z, x.w, y.x);
+  else if (sh == 2) v = make_uint4(x.z, x.w, y.x, y.y);
+  else v = make_uint4(x.w, y.x, y.y, y.z);
+  return v;
+}
+
 }  // namespace vg

@@ -53,8 +53,8 @@ __global__ void __launch_bounds__(kBlock) multi_copy_kernel(CopyArgs a) {
     if (e0 + 4 > pc.len) continue;
     uint4 v;
     const uint32_t* s = pc.src + e0;
-    if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
-      v = *reinterpret_cast<const uint4*>(s);
+    if (c > 0 && e0 + 8 <= pc.len) {
+      v = load4_realigned(s);   // both aligned vectors inside the piece
     } else {
       v.x = s[0];
       v.y = s[1];
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kBlock) join_count_kernel(KeyOf<TWO> L, uint64
 
 // One block per 2048 left keys; the right-key window is staged in shared
 // memory by a bulk copy (vg_join_tile.cuh).
-__global__ void __launch_bounds__(kJcBlock) join_count_tiled_kernel(const uint32_t* __restrict__ L, uint64_t nl,
+__global__ void __launch_bounds__(kJcBlock, 4) join_count_tiled_kernel(const uint32_t* __restrict__ L, uint64_t nl,
                                                                     const uint32_t* __restrict__ R, uint64_t nr,
                                                                     uint32_t* __restrict__ lo,
                                                                     uint32_t* __restrict__ cnt, DeviceErrors* err) {
