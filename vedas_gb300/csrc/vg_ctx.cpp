@@ -1,5 +1,7 @@
 #include "vg_ctx.h"
 
+#include <algorithm>
+
 namespace vg {
 
 void Arena::init(size_t bytes) {
@@ -7,43 +9,105 @@ void Arena::init(size_t bytes) {
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, bytes);
   if (e != cudaSuccess) fail(VG_ERR_OOM, std::string("arena cudaMalloc: ") + cudaGetErrorString(e));
-  base_ = static_cast<char*>(p);
+  setup(static_cast<char*>(p), bytes, true);
+}
+
+void Arena::init_at(void* base, size_t bytes) {
+  setup(static_cast<char*>(base), bytes / kAlign * kAlign, false);
+}
+
+void Arena::setup(char* base, size_t bytes, bool owned) {
+  release();
+  base_ = base;
+  owned_ = owned;
   cap_ = bytes;
-  free_.clear();
-  by_size_.clear();
-  live_.clear();
-  small_live_.clear();
-  for (auto& v : small_free_) v.clear();
-  free_[0] = bytes;
-  by_size_.emplace(bytes, size_t{0});
-  used_ = peak_ = 0;
+  nchunks_ = bytes / kChunk + 1;
+  chunk_class_.reset(new std::atomic<int8_t>[nchunks_]);
+  for (size_t k = 0; k < nchunks_; ++k) chunk_class_[k].store(-1, std::memory_order_relaxed);
+  shards_.reset(new Shard[kShards]);
+  if (bytes) add_free(0, bytes);
+  used_.store(0);
+  peak_.store(0);
 }
 
 void Arena::release() {
-  if (base_) cudaFree(base_);
+  if (base_ && owned_) cudaFree(base_);
   base_ = nullptr;
-  cap_ = used_ = 0;
+  owned_ = false;
+  cap_ = 0;
   free_.clear();
   by_size_.clear();
   live_.clear();
-  small_live_.clear();
   for (auto& v : small_free_) v.clear();
+  chunk_class_.reset();
+  nchunks_ = 0;
+  shards_.reset();
+}
+
+int Arena::my_shard() {
+  static std::atomic<int> next{0};
+  thread_local int idx = next.fetch_add(1, std::memory_order_relaxed) % kShards;
+  return idx;
+}
+
+int Arena::small_class(size_t off) const {
+  return chunk_class_[off / kChunk].load(std::memory_order_relaxed);
+}
+
+void Arena::note_used(size_t add) {
+  const size_t u = used_.fetch_add(add, std::memory_order_relaxed) + add;
+  size_t pk = peak_.load(std::memory_order_relaxed);
+  while (u > pk && !peak_.compare_exchange_weak(pk, u, std::memory_order_relaxed)) {
+  }
 }
 
 void Arena::erase_by_size(size_t sz, size_t off) { by_size_.erase({sz, off}); }
+
+void Arena::take_free(size_t off, size_t sz) {
+  by_size_.erase({sz, off});
+  free_.erase(off);
+}
+
+void Arena::add_free(size_t off, size_t sz) {
+  free_[off] = sz;
+  by_size_.emplace(sz, off);
+}
 
 // Best fit among the large free blocks; the remainder stays free.
 size_t Arena::big_alloc(size_t bytes) {
   auto it = by_size_.lower_bound({bytes, size_t{0}});
   if (it == by_size_.end()) return SIZE_MAX;
   const size_t sz = it->first, off = it->second;
-  by_size_.erase(it);
-  free_.erase(off);
-  if (sz > bytes) {
-    free_[off + bytes] = sz - bytes;
-    by_size_.emplace(sz - bytes, off + bytes);
-  }
+  take_free(off, sz);
+  if (sz > bytes) add_free(off + bytes, sz - bytes);
   return off;
+}
+
+// Small-class chunks are carved from the top of the slab (the highest free
+// block that holds a kChunk-aligned chunk, at its highest aligned position),
+// while large blocks are split from the low end of their best fit, so chunks
+// cluster at one end and do not fragment the space large relations need.
+size_t Arena::chunk_alloc() {
+  int tries = 0;
+  for (auto it = free_.rbegin(); it != free_.rend() && tries < 256; ++it, ++tries) {
+    const size_t off = it->first, sz = it->second;
+    if (sz < kChunk) continue;
+    const size_t a = (off + sz - kChunk) / kChunk * kChunk;
+    if (a < off) continue;
+    take_free(off, sz);
+    if (a > off) add_free(off, a - off);
+    if (a + kChunk < off + sz) add_free(a + kChunk, off + sz - (a + kChunk));
+    return a;
+  }
+  // none near the top: any block of 2 * kChunk - kAlign or more holds one
+  auto it = by_size_.lower_bound({2 * kChunk - kAlign, size_t{0}});
+  if (it == by_size_.end()) return SIZE_MAX;
+  const size_t sz = it->first, off = it->second;
+  const size_t a = (off + sz - kChunk) / kChunk * kChunk;
+  take_free(off, sz);
+  if (a > off) add_free(off, a - off);
+  if (a + kChunk < off + sz) add_free(a + kChunk, off + sz - (a + kChunk));
+  return a;
 }
 
 void Arena::big_free(size_t off, size_t sz) {
@@ -62,36 +126,67 @@ void Arena::big_free(size_t off, size_t sz) {
       return;
     }
   }
-  free_[off] = sz;
-  by_size_.emplace(sz, off);
+  add_free(off, sz);
 }
 
 void* Arena::try_alloc(size_t bytes) {
-  std::lock_guard<std::mutex> lk(mu_);
+  if (!base_) return nullptr;
   bytes = (bytes + kAlign - 1) / kAlign * kAlign;
   if (bytes == 0) bytes = kAlign;
   if (bytes <= kSmallMax) {
     int c = 0;
     while ((kAlign << c) < bytes) ++c;
     const size_t csz = kAlign << c;
-    if (small_free_[c].empty()) {
-      const size_t chunk = csz * 16 > kChunk ? csz * 16 : kChunk;
-      const size_t off = big_alloc(chunk);
-      if (off == SIZE_MAX) return nullptr;
-      for (size_t k = chunk / csz; k-- > 0;) small_free_[c].push_back(off + k * csz);
+    Shard& sh = shards_[my_shard()];
+    {
+      std::lock_guard<std::mutex> lk(sh.mu);
+      if (!sh.free[c].empty()) {
+        const size_t off = sh.free[c].back();
+        sh.free[c].pop_back();
+        note_used(csz);
+        return base_ + off;
+      }
     }
-    const size_t off = small_free_[c].back();
-    small_free_[c].pop_back();
-    small_live_[off] = c;
-    used_ += csz;
-    if (used_ > peak_) peak_ = used_;
+    // refill from the global list, or carve a new chunk; a quarter of a
+    // chunk's worth of blocks moves per refill
+    std::vector<size_t> got;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      std::vector<size_t>& g = small_free_[c];
+      if (!g.empty()) {
+        const size_t batch = std::max<size_t>(1, kChunk / csz / 4);
+        const size_t n = std::min(batch, g.size());
+        got.assign(g.end() - static_cast<long>(n), g.end());
+        g.resize(g.size() - n);
+      } else {
+        const size_t a = chunk_alloc();
+        if (a != SIZE_MAX) {
+          chunk_class_[a / kChunk].store(static_cast<int8_t>(c), std::memory_order_relaxed);
+          for (size_t k = kChunk / csz; k-- > 0;) got.push_back(a + k * csz);
+        } else {
+          // no aligned chunk left: serve it as a large block
+          const size_t off = big_alloc(bytes);
+          if (off == SIZE_MAX) return nullptr;
+          live_[off] = bytes;
+          note_used(bytes);
+          return base_ + off;
+        }
+      }
+    }
+    const size_t off = got.back();
+    got.pop_back();
+    if (!got.empty()) {
+      std::lock_guard<std::mutex> lk(sh.mu);
+      sh.free[c].insert(sh.free[c].end(), got.begin(), got.end());
+    }
+    note_used(csz);
     return base_ + off;
   }
+  std::lock_guard<std::mutex> lk(mu_);
   const size_t off = big_alloc(bytes);
   if (off == SIZE_MAX) return nullptr;
   live_[off] = bytes;
-  used_ += bytes;
-  if (used_ > peak_) peak_ = used_;
+  note_used(bytes);
   return base_ + off;
 }
 
@@ -99,27 +194,44 @@ void* Arena::alloc(size_t bytes) {
   void* p = try_alloc(bytes);
   if (!p)
     fail(VG_ERR_OOM, "arena exhausted: requested " + std::to_string(bytes) + " bytes, used " +
-                         std::to_string(used_) + " of " + std::to_string(cap_));
+                         std::to_string(used()) + " of " + std::to_string(cap_));
   return p;
 }
 
 void Arena::free(void* p) {
   if (!p) return;
-  std::lock_guard<std::mutex> lk(mu_);
   const size_t off = static_cast<size_t>(static_cast<char*>(p) - base_);
-  auto sm = small_live_.find(off);
-  if (sm != small_live_.end()) {
-    const int c = sm->second;
-    small_live_.erase(sm);
-    small_free_[c].push_back(off);
-    used_ -= kAlign << c;
+  if (!base_ || off >= cap_) fail(VG_ERR_INVALID, "arena free of a pointer outside the slab");
+  const int c = small_class(off);
+  if (c >= 0) {
+    const size_t csz = kAlign << c;
+    used_.fetch_sub(csz, std::memory_order_relaxed);
+    Shard& sh = shards_[my_shard()];
+    std::vector<size_t> spill;
+    {
+      std::lock_guard<std::mutex> lk(sh.mu);
+      std::vector<size_t>& v = sh.free[c];
+      v.push_back(off);
+      // a shard keeps up to one chunk's worth of a class; the older half of
+      // a longer list goes back to the global list
+      if (v.size() * csz > kChunk) {
+        const size_t half = v.size() / 2;
+        spill.assign(v.begin(), v.begin() + static_cast<long>(half));
+        v.erase(v.begin(), v.begin() + static_cast<long>(half));
+      }
+    }
+    if (!spill.empty()) {
+      std::lock_guard<std::mutex> lk(mu_);
+      small_free_[c].insert(small_free_[c].end(), spill.begin(), spill.end());
+    }
     return;
   }
+  std::lock_guard<std::mutex> lk(mu_);
   auto it = live_.find(off);
   if (it == live_.end()) fail(VG_ERR_INVALID, "arena free of an unknown block");
   const size_t sz = it->second;
   live_.erase(it);
-  used_ -= sz;
+  used_.fetch_sub(sz, std::memory_order_relaxed);
   big_free(off, sz);
 }
 
@@ -127,15 +239,16 @@ void Arena::shrink(void* p, size_t new_bytes) {
   if (!p) return;
   new_bytes = (new_bytes + kAlign - 1) / kAlign * kAlign;
   if (new_bytes == 0) new_bytes = kAlign;
-  std::lock_guard<std::mutex> lk(mu_);
   const size_t off = static_cast<size_t>(static_cast<char*>(p) - base_);
-  if (small_live_.count(off)) return;
+  if (!base_ || off >= cap_) fail(VG_ERR_INVALID, "arena shrink of a pointer outside the slab");
+  if (small_class(off) >= 0) return;
+  std::lock_guard<std::mutex> lk(mu_);
   auto it = live_.find(off);
   if (it == live_.end()) fail(VG_ERR_INVALID, "arena shrink of an unknown block");
   if (new_bytes >= it->second) return;
   const size_t tail = it->second - new_bytes;
   it->second = new_bytes;
-  used_ -= tail;
+  used_.fetch_sub(tail, std::memory_order_relaxed);
   big_free(off + new_bytes, tail);
 }
 

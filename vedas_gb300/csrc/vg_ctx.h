@@ -4,7 +4,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <set>
 #include <string>
@@ -17,18 +19,27 @@ namespace vg {
 
 // Allocator over one cudaMalloc'd slab.  Allocation is host-side bookkeeping
 // only (no device call), so intermediate relations never pay a cudaMalloc.
-// Blocks up to kSmallMax come from per-size-class free lists (power-of-two
-// classes carved from chunks of the slab): O(1), which matters when thousands
-// of queries allocate their relations at once.  Larger blocks are best-fit
-// with coalescing.  All work on the slab is ordered on the context stream, so
-// a block may be handed out again as soon as the work that last used it has
-// been enqueued.
+// All work on the slab is ordered on the context stream, so a block may be
+// handed out again as soon as the work that last used it has been enqueued.
+//
+// Blocks up to kSmallMax come from power-of-two size classes carved from
+// kChunk-aligned chunks of the slab.  A directory with one entry per chunk
+// position gives the class of any small block without a lock, and free lists
+// are sharded by host thread, so the parallel host phases of a batch (which
+// allocate and free relations of thousands of queries at once) almost never
+// wait on each other.  Shards hand surplus blocks back to a global list and
+// refill from it in batches.  Larger blocks are best-fit with coalescing
+// under one lock.
 class Arena {
  public:
   Arena() = default;
   Arena(const Arena&) = delete;
   Arena& operator=(const Arena&) = delete;
-  void init(size_t bytes);
+  ~Arena() { release(); }
+  void init(size_t bytes);                 // cudaMalloc's the slab
+  // Manages [base, base + bytes), owned by the caller; the arena never
+  // dereferences it (host-side tests use this).
+  void init_at(void* base, size_t bytes);
   void release();
   void* alloc(size_t bytes);      // throws VG_ERR_OOM
   void* try_alloc(size_t bytes);  // nullptr when it does not fit
@@ -37,27 +48,46 @@ class Arena {
   // (small blocks keep their class).
   void shrink(void* p, size_t new_bytes);
   size_t capacity() const { return cap_; }
-  size_t used() const { return used_; }
-  size_t peak() const { return peak_; }
+  size_t used() const { return used_.load(std::memory_order_relaxed); }
+  size_t peak() const { return peak_.load(std::memory_order_relaxed); }
   size_t largest_free() const;
 
- private:
   static constexpr size_t kAlign = 256;
   static constexpr int kClasses = 13;                  // 256 B .. 1 MiB
   static constexpr size_t kSmallMax = kAlign << (kClasses - 1);
-  static constexpr size_t kChunk = 4u << 20;           // small-class chunk
+  static constexpr size_t kChunk = 4u << 20;           // small-class chunk, kChunk-aligned in the slab
+
+ private:
+  static constexpr int kShards = 32;
+  struct alignas(64) Shard {
+    std::mutex mu;
+    std::vector<size_t> free[kClasses];
+  };
   char* base_ = nullptr;
-  size_t cap_ = 0, used_ = 0, peak_ = 0;
+  bool owned_ = false;
+  size_t cap_ = 0;
+  std::atomic<size_t> used_{0}, peak_{0};
+  // under mu_
   std::map<size_t, size_t> free_;                      // offset -> size (large free blocks)
   std::set<std::pair<size_t, size_t>> by_size_;        // (size, offset) of the same blocks
   std::unordered_map<size_t, size_t> live_;            // offset -> size (large live blocks)
-  std::vector<size_t> small_free_[kClasses];           // offsets of free small blocks
-  std::unordered_map<size_t, int> small_live_;         // offset -> class
+  std::vector<size_t> small_free_[kClasses];           // global lists of free small blocks
   mutable std::mutex mu_;
+  // chunk position -> size class, -1 where no small chunk lies (read without a lock)
+  std::unique_ptr<std::atomic<int8_t>[]> chunk_class_;
+  size_t nchunks_ = 0;
+  std::unique_ptr<Shard[]> shards_;
 
+  void setup(char* base, size_t bytes, bool owned);
   size_t big_alloc(size_t bytes);                      // SIZE_MAX when it does not fit
+  size_t chunk_alloc();                                // a kChunk-aligned chunk, or SIZE_MAX
   void big_free(size_t off, size_t sz);
   void erase_by_size(size_t sz, size_t off);
+  void take_free(size_t off, size_t sz);               // removes a free block from both indexes
+  void add_free(size_t off, size_t sz);
+  void note_used(size_t add);
+  int small_class(size_t off) const;
+  static int my_shard();
 };
 
 // Per-kernel accounting: launches, algorithmic bytes (the bytes the
