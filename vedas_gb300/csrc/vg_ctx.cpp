@@ -84,30 +84,29 @@ size_t Arena::big_alloc(size_t bytes) {
 }
 
 // Small-class chunks are carved from the top of the slab (the highest free
-// block that holds a kChunk-aligned chunk, at its highest aligned position),
-// while large blocks are split from the low end of their best fit, so chunks
-// cluster at one end and do not fragment the space large relations need.
-size_t Arena::chunk_alloc() {
-  int tries = 0;
-  for (auto it = free_.rbegin(); it != free_.rend() && tries < 256; ++it, ++tries) {
-    const size_t off = it->first, sz = it->second;
-    if (sz < kChunk) continue;
-    const size_t a = (off + sz - kChunk) / kChunk * kChunk;
-    if (a < off) continue;
+// block that holds a kChunk-aligned chunk of `bytes`, at its highest aligned
+// position), while large blocks are split from the low end of their best fit,
+// so chunks cluster at one end and do not fragment the space large relations
+// need.
+size_t Arena::chunk_alloc(size_t bytes) {
+  auto carve = [&](size_t off, size_t sz) {
+    if (sz < bytes) return SIZE_MAX;
+    const size_t a = (off + sz - bytes) / kChunk * kChunk;
+    if (a < off) return SIZE_MAX;
     take_free(off, sz);
     if (a > off) add_free(off, a - off);
-    if (a + kChunk < off + sz) add_free(a + kChunk, off + sz - (a + kChunk));
+    if (a + bytes < off + sz) add_free(a + bytes, off + sz - (a + bytes));
     return a;
+  };
+  int tries = 0;
+  for (auto it = free_.rbegin(); it != free_.rend() && tries < 256; ++it, ++tries) {
+    const size_t a = carve(it->first, it->second);
+    if (a != SIZE_MAX) return a;
   }
-  // none near the top: any block of 2 * kChunk - kAlign or more holds one
-  auto it = by_size_.lower_bound({2 * kChunk - kAlign, size_t{0}});
+  // none near the top: any block of bytes + kChunk - kAlign or more holds one
+  auto it = by_size_.lower_bound({bytes + kChunk - kAlign, size_t{0}});
   if (it == by_size_.end()) return SIZE_MAX;
-  const size_t sz = it->first, off = it->second;
-  const size_t a = (off + sz - kChunk) / kChunk * kChunk;
-  take_free(off, sz);
-  if (a > off) add_free(off, a - off);
-  if (a + kChunk < off + sz) add_free(a + kChunk, off + sz - (a + kChunk));
-  return a;
+  return carve(it->second, it->first);
 }
 
 void Arena::big_free(size_t off, size_t sz) {
@@ -147,22 +146,24 @@ void* Arena::try_alloc(size_t bytes) {
         return base_ + off;
       }
     }
-    // refill from the global list, or carve a new chunk; a quarter of a
-    // chunk's worth of blocks moves per refill
+    // refill from the global list (a quarter of a chunk's worth of blocks,
+    // at least two), or carve a new chunk
     std::vector<size_t> got;
     {
       std::lock_guard<std::mutex> lk(mu_);
       std::vector<size_t>& g = small_free_[c];
       if (!g.empty()) {
-        const size_t batch = std::max<size_t>(1, kChunk / csz / 4);
+        const size_t batch = std::max<size_t>(2, kChunk / csz / 4);
         const size_t n = std::min(batch, g.size());
         got.assign(g.end() - static_cast<long>(n), g.end());
         g.resize(g.size() - n);
       } else {
-        const size_t a = chunk_alloc();
+        const size_t cb = chunk_bytes(c);
+        const size_t a = chunk_alloc(cb);
         if (a != SIZE_MAX) {
-          chunk_class_[a / kChunk].store(static_cast<int8_t>(c), std::memory_order_relaxed);
-          for (size_t k = kChunk / csz; k-- > 0;) got.push_back(a + k * csz);
+          for (size_t k = 0; k < cb / kChunk; ++k)
+            chunk_class_[a / kChunk + k].store(static_cast<int8_t>(c), std::memory_order_relaxed);
+          for (size_t k = cb / csz; k-- > 0;) got.push_back(a + k * csz);
         } else {
           // no aligned chunk left: serve it as a large block
           const size_t off = big_alloc(bytes);
@@ -212,9 +213,9 @@ void Arena::free(void* p) {
       std::lock_guard<std::mutex> lk(sh.mu);
       std::vector<size_t>& v = sh.free[c];
       v.push_back(off);
-      // a shard keeps up to one chunk's worth of a class; the older half of
-      // a longer list goes back to the global list
-      if (v.size() * csz > kChunk) {
+      // a shard keeps up to a chunk's worth of a class (at least 8 blocks);
+      // the older half of a longer list goes back to the global list
+      if (v.size() > std::max<size_t>(8, kChunk / csz)) {
         const size_t half = v.size() / 2;
         spill.assign(v.begin(), v.begin() + static_cast<long>(half));
         v.erase(v.begin(), v.begin() + static_cast<long>(half));

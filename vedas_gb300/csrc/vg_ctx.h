@@ -23,8 +23,8 @@ namespace vg {
 // handed out again as soon as the work that last used it has been enqueued.
 //
 // Blocks up to kSmallMax come from power-of-two size classes carved from
-// kChunk-aligned chunks of the slab.  A directory with one entry per chunk
-// position gives the class of any small block without a lock, and free lists
+// kChunk-aligned chunks of the slab.  A directory with one entry per kChunk
+// of the slab gives the class of any small block without a lock, and free lists
 // are sharded by host thread, so the parallel host phases of a batch (which
 // allocate and free relations of thousands of queries at once) almost never
 // wait on each other.  Shards hand surplus blocks back to a global list and
@@ -53,9 +53,13 @@ class Arena {
   size_t largest_free() const;
 
   static constexpr size_t kAlign = 256;
-  static constexpr int kClasses = 13;                  // 256 B .. 1 MiB
+  static constexpr int kClasses = 16;                  // 256 B .. 8 MiB
   static constexpr size_t kSmallMax = kAlign << (kClasses - 1);
-  static constexpr size_t kChunk = 4u << 20;           // small-class chunk, kChunk-aligned in the slab
+  static constexpr size_t kChunk = 4u << 20;           // directory granularity; chunks are kChunk-aligned
+  // A class's chunk: 4 MiB, or two blocks for classes above 2 MiB.
+  static constexpr size_t chunk_bytes(int c) {
+    return (kAlign << c) * 2 > kChunk ? (kAlign << c) * 2 : kChunk;
+  }
 
  private:
   static constexpr int kShards = 32;
@@ -80,7 +84,7 @@ class Arena {
 
   void setup(char* base, size_t bytes, bool owned);
   size_t big_alloc(size_t bytes);                      // SIZE_MAX when it does not fit
-  size_t chunk_alloc();                                // a kChunk-aligned chunk, or SIZE_MAX
+  size_t chunk_alloc(size_t bytes);                    // a kChunk-aligned chunk, or SIZE_MAX
   void big_free(size_t off, size_t sz);
   void erase_by_size(size_t sz, size_t off);
   void take_free(size_t off, size_t sz);               // removes a free block from both indexes
