@@ -242,6 +242,8 @@ vg_status vg_batch_query_status(const vg_batch* b, uint32_t q);
 const char* vg_batch_query_error(const vg_batch* b, uint32_t q);
 uint32_t vg_batch_ncols(const vg_batch* b, uint32_t q);
 uint64_t vg_batch_nrows(const vg_batch* b, uint32_t q);
+/* Row counts of every query at once: nrows[q] for q < vg_batch_size(b). */
+vg_status vg_batch_rows(const vg_batch* b, uint64_t* nrows);
 const char* vg_batch_header(const vg_batch* b, uint32_t q, uint32_t c);
 const uint32_t* vg_batch_column_device(const vg_batch* b, uint32_t q, uint32_t c);
 vg_status vg_batch_download(const vg_batch* b, uint32_t q, uint32_t c, uint32_t* host);

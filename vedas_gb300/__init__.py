@@ -98,6 +98,7 @@ def lib():
             "vg_batch_query_error": (ctypes.c_char_p, [vp, u32]),
             "vg_batch_ncols": (u32, [vp, u32]),
             "vg_batch_nrows": (u64, [vp, u32]),
+            "vg_batch_rows": (i32, [vp, vp]),
             "vg_batch_header": (ctypes.c_char_p, [vp, u32, u32]),
             "vg_batch_column_device": (vp, [vp, u32, u32]),
             "vg_batch_download": (i32, [vp, u32, u32, pu32]),
@@ -301,8 +302,14 @@ class Batch:
 
     def run(self) -> int:
         """Total result rows (the batch already ran in the constructor)."""
-        L = lib()
-        return sum(int(L.vg_batch_nrows(self.h, q)) for q in range(self.n))
+        return int(self.rows().sum())
+
+    def rows(self) -> np.ndarray:
+        """Row count of every query (one call)."""
+        out = np.zeros(self.n, dtype=np.uint64)
+        if self.n:
+            check(lib().vg_batch_rows(self.h, out.ctypes.data))
+        return out
 
     @property
     def waves(self) -> int:

@@ -570,19 +570,8 @@ int SelectQueryJob::startJob(int gpu) {
   gpuId = gpu;
   SelectWork w;
   prepare(w);
-  if (w.unique) {
-    const uint32_t* in[1] = {w.uniq_src};
-    uint32_t* out[1] = {w.ir->getRelationRawPointer(0)};
-    finishUnique(w, vg::unique_rows(*ex->ctx, in, out, 1, w.uniq_n));
-  } else if (!w.pieces.empty()) {
-    vg::multi_copy(*ex->ctx, w.pieces.data(), static_cast<int>(w.pieces.size()));
-  }
+  if (!w.pieces.empty()) vg::multi_copy(*ex->ctx, w.pieces.data(), static_cast<int>(w.pieces.size()));
   return 0;
-}
-
-void SelectQueryJob::finishUnique(SelectWork& w, uint64_t kept) {
-  w.ir->ctx()->arena.shrink(w.ir->getRelationRawPointer(0), kept * sizeof(uint32_t));
-  w.ir->rel().nrows = kept;
 }
 
 void SelectQueryJob::prepare(SelectWork& w) {
@@ -637,16 +626,23 @@ void SelectQueryJob::prepare(SelectWork& w) {
   if (!is_second_var_used) {
     if (first > second) throw ReferenceUB("select row count underflows");
     const size_t row = second - first;
-    auto* ir = new FullRelationIR(ctx, 1, row);
+    // The reference uploads l2d[first, second) and removes adjacent
+    // duplicates.  first and second are boundaries of runs of equal keys (the
+    // predicate's range, narrowed by a lower and an upper bound on the key),
+    // so the distinct keys are exactly the level-2 index keys of the runs
+    // that start in [first, second): a contiguous slice of the level-2 values.
+    TYPEID_HOST_VEC* l2o = pos_index ? st->getPredicateObjectIndexOffsets() : st->getPredicateSubjectIndexOffsets();
+    const TYPEID* dl2v = st->dev(pos_index ? "po_o_idx_values" : "ps_s_idx_values");
+    const size_t ra = static_cast<size_t>(std::lower_bound(l2o->begin(), l2o->end(), first) - l2o->begin());
+    const size_t rb = static_cast<size_t>(std::lower_bound(l2o->begin(), l2o->end(), second) - l2o->begin());
+    if (row > 0 && (ra >= l2o->size() || (*l2o)[ra] != first || rb < ra))
+      throw vg::Error(VG_ERR_INVALID, "select range does not start a level-2 run");
+    const size_t kept = row > 0 ? rb - ra : 0;
+    auto* ir = new FullRelationIR(ctx, 1, kept);
     ir->setHeader(0, variables[0], false);
     intermediateResult = ir;
     w.ir = ir;
-    if (row > 0) {
-      // copy + adjacent unique fused: compact straight from the index slice
-      w.unique = true;
-      w.uniq_src = dl2d + first;
-      w.uniq_n = row;
-    }
+    if (kept > 0) w.pieces.push_back({dl2v + ra, ir->getRelationRawPointer(0), kept});
     ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), row, 1));
     return;
   }

@@ -209,15 +209,11 @@ class QueryJob {
   IR* intermediateResult = nullptr;
 };
 
-// Device work a select needs once its host-side lookups are done: either
-// copies of index slices into the new relation, or an adjacent-unique
-// compaction of one slice into its single column.
+// Device work a select needs once its host-side lookups are done: copies of
+// index slices into the new relation.
 struct SelectWork {
   FullRelationIR* ir = nullptr;
   std::vector<vg::CopyPiece> pieces;
-  bool unique = false;
-  const TYPEID* uniq_src = nullptr;
-  size_t uniq_n = 0;
 };
 
 // Host state of a join between its phases: operands (possibly swapped),
@@ -242,11 +238,9 @@ class SelectQueryJob : public QueryJob {
   int startJob(int gpuId) override;
   IR* getIR() override { return intermediateResult; }
   std::string jobTypeName() const override { return "Upload Job"; }
-  // Phase 1 (host): index lookups, bounds, empty intervals; allocates the
-  // relation and describes the device work.
+  // Host part: index lookups, bounds, empty intervals; allocates the
+  // relation and describes the copies that fill it.
   void prepare(SelectWork& w);
-  // Phase 2 (after the device work): the unique compaction's row count.
-  static void finishUnique(SelectWork& w, uint64_t kept);
 
  private:
   QueryExecutor* ex;

@@ -25,8 +25,7 @@ __device__ __forceinline__ uint32_t seg_of(const uint64_t* start, uint32_t S, ui
 template <typename T>
 T* upload(Ctx& ctx, const std::vector<T>& v) {
   T* d = static_cast<T*>(ctx.arena.alloc((v.empty() ? 1 : v.size()) * sizeof(T)));
-  if (!v.empty())
-    VG_CUDA(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx.stream));
+  if (!v.empty()) ctx.upload_bytes(d, v.data(), v.size() * sizeof(T));
   return d;
 }
 
@@ -153,14 +152,16 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
 }
 
 // ---------------------------------------------------------------------------
+// (segment, key) composite sort keys: the segment sits above the key's
+// key_bits bits, so one sort orders rows by segment and, within it, by key.
 __global__ void __launch_bounds__(kBlock) composite_keys_kernel(const uint32_t* const* __restrict__ col0,
                                                                 const uint64_t* __restrict__ rstart, uint32_t S,
-                                                                uint64_t* __restrict__ keys) {
+                                                                uint32_t key_bits, uint64_t* __restrict__ keys) {
   const uint64_t total = rstart[S];
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
   for (uint64_t r = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; r < total; r += stride) {
     const uint32_t s = seg_of(rstart, S, r);
-    keys[r] = (static_cast<uint64_t>(s) << 32) | col0[s][r - rstart[s]];
+    keys[r] = (static_cast<uint64_t>(s) << key_bits) | col0[s][r - rstart[s]];
   }
 }
 
@@ -333,10 +334,9 @@ void batched_copy(Ctx& ctx, const std::vector<CopyPiece>& pieces) {
   ctx.free(dc);
 }
 
-std::vector<uint64_t> batched_unique(Ctx& ctx, const std::vector<SegRows>& segs) {
+void batched_unique_enqueue(Ctx& ctx, const std::vector<SegRows>& segs, uint64_t* counts_host) {
   const uint32_t S = static_cast<uint32_t>(segs.size());
-  std::vector<uint64_t> counts(S, 0);
-  if (S == 0) return counts;
+  if (S == 0) return;
   std::vector<uint64_t> tstart(S + 1, 0);
   double bytes = 0;
   for (uint32_t s = 0; s < S; ++s) {
@@ -344,7 +344,10 @@ std::vector<uint64_t> batched_unique(Ctx& ctx, const std::vector<SegRows>& segs)
     bytes += 4.0 * segs[s].n * segs[s].ncols;
   }
   const uint64_t tiles = tstart[S];
-  if (tiles == 0) return counts;
+  if (tiles == 0) {
+    for (uint32_t s = 0; s < S; ++s) counts_host[s] = 0;
+    return;
+  }
   SegRows* ds = upload(ctx, segs);
   uint64_t* dt = upload(ctx, tstart);
   Scratch<uint64_t> status(ctx, tiles), dcount(ctx, S);
@@ -357,17 +360,29 @@ std::vector<uint64_t> batched_unique(Ctx& ctx, const std::vector<SegRows>& segs)
                                                                            dcount.get(), ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
-  VG_CUDA(cudaMemcpyAsync(counts.data(), dcount.get(), S * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
-  ctx.sync();
-  double wb = 0;
-  for (uint32_t s = 0; s < S; ++s) wb += 4.0 * counts[s] * segs[s].ncols;
-  ctx.kstats["unique_compact"].bytes += wb;
+  VG_CUDA(cudaMemcpyAsync(counts_host, dcount.get(), S * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.free(ds);
   ctx.free(dt);
+}
+
+void note_unique_writes(Ctx& ctx, const std::vector<SegRows>& segs, const uint64_t* counts) {
+  double wb = 0;
+  for (size_t s = 0; s < segs.size(); ++s) wb += 4.0 * counts[s] * segs[s].ncols;
+  ctx.kstats["unique_compact"].bytes += wb;
+}
+
+std::vector<uint64_t> batched_unique(Ctx& ctx, const std::vector<SegRows>& segs) {
+  std::vector<uint64_t> counts(segs.size(), 0);
+  if (segs.empty()) return counts;
+  PinnedWords h;
+  batched_unique_enqueue(ctx, segs, h.reserve(segs.size()));
+  ctx.sync();
+  std::copy(h.data(), h.data() + segs.size(), counts.begin());
+  note_unique_writes(ctx, segs, counts.data());
   return counts;
 }
 
-void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in) {
+void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in, int key_bits) {
   std::vector<Rel*> rels;
   for (Rel* r : rels_in)
     if (r->nrows > 1 && r->ncols > 0) rels.push_back(r);
@@ -381,6 +396,8 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in) {
   }
   const uint64_t N = rstart[S];
   if (N > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "batched sort is limited to 2^32 rows");
+  const bool known = key_bits > 0 && key_bits <= 32;
+  const int kb = known ? key_bits : 32;
   uint64_t* drs = upload(ctx, rstart);
   const uint32_t** dc0 = upload(ctx, col0);
   uint64_t* keys = ctx.alloc<uint64_t>(N);
@@ -388,10 +405,12 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in) {
   uint32_t* vals = ctx.alloc<uint32_t>(N);
   uint32_t* vals_alt = ctx.alloc<uint32_t>(N);
   ctx.launch("sort_keys", 12.0 * N, [&] {
-    composite_keys_kernel<<<grid_cap(ctx, N, 4), kBlock, 0, ctx.stream>>>(dc0, drs, S, keys);
+    composite_keys_kernel<<<grid_cap(ctx, N, 4), kBlock, 0, ctx.stream>>>(dc0, drs, S, static_cast<uint32_t>(kb),
+                                                                          keys);
   });
   VG_CUDA(cudaGetLastError());
-  const bool alt = radix_sort_u64(ctx, keys, keys_alt, vals, vals_alt, N, 32 + bits_for_segments(S), true);
+  // with the key width known the passes are fixed and nothing waits on the device
+  const bool alt = radix_sort_u64(ctx, keys, keys_alt, vals, vals_alt, N, kb + bits_for_segments(S), true, !known);
   uint32_t* perm = alt ? vals_alt : vals;
   ctx.free(keys);
   ctx.free(keys_alt);
@@ -423,22 +442,26 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in) {
   ctx.free(const_cast<uint32_t**>(dc0));
 }
 
-void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r,
-                  std::vector<Rel>& out, std::vector<uint32_t>& first_last) {
+void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r, JoinBatch& jb,
+                        uint64_t* totals_host) {
   const uint32_t J = static_cast<uint32_t>(l.size());
-  out.assign(J, Rel());
-  first_last.assign(2 * J, 0);
+  jb = JoinBatch();
+  jb.J = J;
+  jb.l = l;
+  jb.r = r;
   if (J == 0) return;
   std::vector<JoinSeg> js(J);
   std::vector<uint64_t> bstart(J + 1, 0), tstart(J + 1, 0);
   uint64_t rows = 0;
   double cbytes = 0;
+  jb.row0.resize(J);
   for (uint32_t j = 0; j < J; ++j) {
     if (l[j]->nrows == 0 || r[j]->nrows == 0) fail(VG_ERR_INVALID, "batched join of an empty relation");
     if (l[j]->nrows > 0xFFFFFFFFull || r[j]->nrows > 0xFFFFFFFFull)
       fail(VG_ERR_OVERFLOW, "join inputs are limited to 2^32 rows");
     if (l[j]->ncols + r[j]->ncols - 1 > VG_MAX_COLS) fail(VG_ERR_UNSUPPORTED, "join output has more than 9 columns");
     js[j] = {l[j]->cols[0], r[j]->cols[0], l[j]->nrows, r[j]->nrows, rows};
+    jb.row0[j] = rows;
     rows += l[j]->nrows;
     bstart[j + 1] = bstart[j] + div_up(l[j]->nrows, kJcTile);
     tstart[j + 1] = tstart[j] + div_up(l[j]->nrows, kTileRows);
@@ -447,47 +470,66 @@ void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<
   JoinSeg* djs = upload(ctx, js);
   uint64_t* dbs = upload(ctx, bstart);
   uint64_t* dts = upload(ctx, tstart);
-  Scratch<uint32_t> lo(ctx, rows), cnt(ctx, rows);
-  Scratch<uint64_t> offs(ctx, rows), status(ctx, tstart[J]), totals(ctx, J);
-  Scratch<uint32_t> ticket(ctx, 1);
-  VG_CUDA(cudaMemsetAsync(status.get(), 0, tstart[J] * sizeof(uint64_t), ctx.stream));
-  VG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(uint32_t), ctx.stream));
+  jb.lo = ctx.alloc<uint32_t>(rows);
+  uint32_t* cnt = ctx.alloc<uint32_t>(rows);
+  jb.offs = ctx.alloc<uint64_t>(rows);
+  uint64_t* status = ctx.alloc<uint64_t>(tstart[J]);
+  uint64_t* totals = ctx.alloc<uint64_t>(J);
+  uint32_t* ticket = ctx.alloc<uint32_t>(1);
+  VG_CUDA(cudaMemsetAsync(status, 0, tstart[J] * sizeof(uint64_t), ctx.stream));
+  VG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), ctx.stream));
   ctx.launch("join_count", cbytes, [&] {
-    bjoin_count_kernel<<<static_cast<unsigned>(bstart[J]), kJcBlock, 0, ctx.stream>>>(djs, dbs, J, lo.get(),
-                                                                                    cnt.get(), ctx.d_err);
+    bjoin_count_kernel<<<static_cast<unsigned>(bstart[J]), kJcBlock, 0, ctx.stream>>>(djs, dbs, J, jb.lo, cnt,
+                                                                                    ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
   ctx.launch("join_scan", 12.0 * rows, [&] {
-    bjoin_scan_kernel<<<static_cast<unsigned>(tstart[J]), kBlock, 0, ctx.stream>>>(
-        djs, dts, J, cnt.get(), offs.get(), status.get(), ticket.get(), totals.get(), ctx.d_err);
+    bjoin_scan_kernel<<<static_cast<unsigned>(tstart[J]), kBlock, 0, ctx.stream>>>(djs, dts, J, cnt, jb.offs, status,
+                                                                                 ticket, totals, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
-  std::vector<uint64_t> tot(J);
-  VG_CUDA(cudaMemcpyAsync(tot.data(), totals.get(), J * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
-  ctx.sync();
+  VG_CUDA(cudaMemcpyAsync(totals_host, totals, J * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  // the stream orders every later use of these blocks after the kernels above
+  ctx.free(cnt);
+  ctx.free(status);
+  ctx.free(totals);
+  ctx.free(ticket);
+  ctx.free(djs);
+  ctx.free(dbs);
+  ctx.free(dts);
+}
+
+void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::vector<Rel>& out,
+                        uint32_t* first_last_host) {
+  const uint32_t J = jb.J;
+  out.assign(J, Rel());
+  if (J == 0) return;
   std::vector<JoinOut> jo(J);
   std::vector<uint64_t> ostart(J + 1, 0);
   double wbytes = 0;
   for (uint32_t j = 0; j < J; ++j) {
-    if (tot[j] > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
-    const uint32_t ncols = l[j]->ncols + r[j]->ncols - 1;
-    out[j] = rel_alloc(ctx, ncols, tot[j]);
+    if (totals[j] > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
+    const Rel* l = jb.l[j];
+    const Rel* r = jb.r[j];
+    const uint32_t ncols = l->ncols + r->ncols - 1;
+    out[j] = rel_alloc(ctx, ncols, totals[j]);
     JoinOut& o = jo[j];
     std::memset(&o, 0, sizeof(o));
-    o.offs = offs.get() + js[j].row0;
-    o.lo = lo.get() + js[j].row0;
-    o.nl = l[j]->nrows;
-    o.total = tot[j];
-    for (uint32_t c = 0; c < l[j]->ncols; ++c) o.lc[c] = l[j]->cols[c];
-    for (uint32_t c = 1; c < r[j]->ncols; ++c) o.rc[c - 1] = r[j]->cols[c];
+    o.offs = jb.offs + jb.row0[j];
+    o.lo = jb.lo + jb.row0[j];
+    o.nl = l->nrows;
+    o.total = totals[j];
+    for (uint32_t c = 0; c < l->ncols; ++c) o.lc[c] = l->cols[c];
+    for (uint32_t c = 1; c < r->ncols; ++c) o.rc[c - 1] = r->cols[c];
     for (uint32_t c = 0; c < ncols; ++c) o.oc[c] = out[j].cols[c];
-    o.nlc = l[j]->ncols;
-    o.nrc = r[j]->ncols - 1;
-    ostart[j + 1] = ostart[j] + div_up(tot[j], kTileRows);
-    wbytes += 4.0 * tot[j] * (2.0 * ncols - 1);
+    o.nlc = l->ncols;
+    o.nrc = r->ncols - 1;
+    ostart[j + 1] = ostart[j] + div_up(totals[j], kTileRows);
+    wbytes += 4.0 * totals[j] * (2.0 * ncols - 1);
   }
   JoinOut* djo = upload(ctx, jo);
-  Scratch<uint32_t> dfl(ctx, 2 * J);
+  uint32_t* dfl = ctx.alloc<uint32_t>(2 * J);
+  VG_CUDA(cudaMemsetAsync(dfl, 0, 2 * J * sizeof(uint32_t), ctx.stream));
   if (ostart[J] > 0) {
     uint64_t* dos = upload(ctx, ostart);
     ctx.launch("join_write", wbytes, [&] {
@@ -497,21 +539,42 @@ void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<
     ctx.free(dos);
   }
   ctx.launch("join_first_last", 8.0 * J, [&] {
-    first_last_kernel<<<static_cast<unsigned>(div_up(J, 128)), 128, 0, ctx.stream>>>(djo, J, dfl.get());
+    first_last_kernel<<<static_cast<unsigned>(div_up(J, 128)), 128, 0, ctx.stream>>>(djo, J, dfl);
   });
   VG_CUDA(cudaGetLastError());
-  VG_CUDA(cudaMemcpyAsync(first_last.data(), dfl.get(), 2 * J * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                          ctx.stream));
-  ctx.sync();
+  VG_CUDA(cudaMemcpyAsync(first_last_host, dfl, 2 * J * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.free(dfl);
   ctx.free(djo);
-  ctx.free(djs);
-  ctx.free(dbs);
-  ctx.free(dts);
+  ctx.free(jb.lo);
+  ctx.free(jb.offs);
+  jb.lo = nullptr;
+  jb.offs = nullptr;
 }
 
-void batched_col0(Ctx& ctx, const std::vector<const Rel*>& rels, std::vector<std::vector<uint32_t>>& out) {
+void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r,
+                  std::vector<Rel>& out, std::vector<uint32_t>& first_last) {
+  const uint32_t J = static_cast<uint32_t>(l.size());
+  out.assign(J, Rel());
+  first_last.assign(2 * J, 0);
+  if (J == 0) return;
+  PinnedWords tot, fl;
+  JoinBatch jb;
+  batched_join_count(ctx, l, r, jb, tot.reserve(J));
+  ctx.sync();
+  batched_join_write(ctx, jb, tot.data(), out, reinterpret_cast<uint32_t*>(fl.reserve(J)));
+  ctx.sync();
+  const uint32_t* f = reinterpret_cast<const uint32_t*>(fl.data());
+  std::copy(f, f + 2 * J, first_last.begin());
+}
+
+uint64_t col0_words(const std::vector<const Rel*>& rels) {
+  uint64_t t = 0;
+  for (const Rel* r : rels) t += r->nrows;
+  return t;
+}
+
+void batched_col0_enqueue(Ctx& ctx, const std::vector<const Rel*>& rels, uint32_t* host) {
   const uint32_t R = static_cast<uint32_t>(rels.size());
-  out.assign(R, {});
   if (R == 0) return;
   std::vector<Col0Req> rq(R);
   uint64_t total = 0;
@@ -521,16 +584,46 @@ void batched_col0(Ctx& ctx, const std::vector<const Rel*>& rels, std::vector<std
   }
   if (total == 0) return;
   Col0Req* drq = upload(ctx, rq);
-  Scratch<uint32_t> buf(ctx, total);
+  uint32_t* buf = ctx.alloc<uint32_t>(total);
   ctx.launch("col0_stage", 8.0 * total, [&] {
-    col0_kernel<<<R < 1024 ? R : 1024, 128, 0, ctx.stream>>>(drq, R, buf.get());
+    col0_kernel<<<R < 1024 ? R : 1024, 128, 0, ctx.stream>>>(drq, R, buf);
   });
   VG_CUDA(cudaGetLastError());
-  std::vector<uint32_t> h(total);
-  VG_CUDA(cudaMemcpyAsync(h.data(), buf.get(), total * 4, cudaMemcpyDeviceToHost, ctx.stream));
-  ctx.sync();
-  for (uint32_t q = 0; q < R; ++q) out[q].assign(h.begin() + rq[q].dst, h.begin() + rq[q].dst + rq[q].n);
+  VG_CUDA(cudaMemcpyAsync(host, buf, total * 4, cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.free(buf);
   ctx.free(drq);
+}
+
+void batched_col0(Ctx& ctx, const std::vector<const Rel*>& rels, std::vector<std::vector<uint32_t>>& out) {
+  const uint32_t R = static_cast<uint32_t>(rels.size());
+  out.assign(R, {});
+  const uint64_t total = col0_words(rels);
+  if (R == 0 || total == 0) return;
+  PinnedWords h;
+  uint32_t* p = reinterpret_cast<uint32_t*>(h.reserve((total + 1) / 2));
+  batched_col0_enqueue(ctx, rels, p);
+  ctx.sync();
+  uint64_t off = 0;
+  for (uint32_t q = 0; q < R; ++q) {
+    out[q].assign(p + off, p + off + rels[q]->nrows);
+    off += rels[q]->nrows;
+  }
+}
+
+PinnedWords::~PinnedWords() {
+  if (p_) cudaFreeHost(p_);
+}
+
+uint64_t* PinnedWords::reserve(size_t words) {
+  if (words <= cap_ && p_) return p_;
+  size_t cap = cap_ ? cap_ : 4096;
+  while (cap < words) cap *= 2;
+  if (p_) VG_CUDA(cudaFreeHost(p_));
+  p_ = nullptr;
+  cap_ = 0;
+  VG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&p_), cap * sizeof(uint64_t), cudaHostAllocDefault));
+  cap_ = cap;
+  return p_;
 }
 
 }  // namespace vg

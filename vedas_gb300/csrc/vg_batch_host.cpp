@@ -186,226 +186,317 @@ void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text,
 }
 
 BatchResult::~BatchResult() {
-  if (ctx)
-    for (auto& q : queries) rel_free(*ctx, q.rel);
+  // results, headers and logs of thousands of queries are released on the pool
+  pfor(queries.size(), [&](size_t i) {
+    BatchQuery& q = queries[i];
+    if (ctx) rel_free(*ctx, q.rel);
+    std::vector<std::string>().swap(q.headers);
+    std::vector<vedas::ExecuteLogRecord>().swap(q.log);
+    std::string().swap(q.error);
+  });
+}
+
+WaveEngine::WaveEngine(Ctx& ctx, int key_bits) : ctx_(ctx), key_bits_(key_bits) {
+  VG_CUDA(cudaEventCreateWithFlags(&ev_a_, cudaEventDisableTiming));
+  VG_CUDA(cudaEventCreateWithFlags(&ev_b_, cudaEventDisableTiming));
+}
+
+WaveEngine::~WaveEngine() {
+  if (a_pending_ || b_pending_) cudaStreamSynchronize(ctx_.stream);
+  for (auto& r : jouts_) rel_free(ctx_, r);
+  if (ev_a_) cudaEventDestroy(ev_a_);
+  if (ev_b_) cudaEventDestroy(ev_b_);
 }
 
 void WaveEngine::add(PlannedQuery* pq) { active_.push_back(pq); }
 
-void WaveEngine::wave(std::vector<PlannedQuery*>& completed) {
-  // Queries that failed while planning, or have no job left, finish now.
-  std::vector<PlannedQuery*> run, done;
+void WaveEngine::reset() {
+  cudaStreamSynchronize(ctx_.stream);
+  a_pending_ = b_pending_ = false;
+  for (auto& r : jouts_) rel_free(ctx_, r);
+  jouts_.clear();
+  jb_ = JoinBatch();
+  active_.clear();
+  run_.clear();
+  items_.clear();
+  final_.clear();
+  fin_seg_.clear();
+  fin_res_.clear();
+  next_is_a_ = true;
+}
+
+void WaveEngine::step(std::vector<PlannedQuery*>& completed) {
+  if (next_is_a_) stage_a(completed);
+  else stage_b(completed);
+  next_is_a_ = !next_is_a_;
+}
+
+void WaveEngine::retire_failed(PlannedQuery* q, std::vector<PlannedQuery*>& completed) {
+  if (q->ex) q->out->log = std::move(q->ex->exe_log);
+  q->plan.reset();
+  completed.push_back(q);
+}
+
+// Host finishing of every job of the wave in flight (its device results are
+// in: stage B's event has passed).
+void WaveEngine::finish_wave() {
+  auto t0 = Clock::now();
+  const uint32_t* jfl = nullptr;
+  if (!joins_.empty()) {
+    const uint64_t* hb = h_b_.data();
+    jfl = reinterpret_cast<const uint32_t*>(hb + off_fl_);
+    const uint32_t* c0 = reinterpret_cast<const uint32_t*>(hb + off_jc0_);
+    uint64_t off = 0;
+    for (size_t m : jsmall_) {
+      Item& it = items_[joins_[m]];
+      const uint64_t n = jouts_[m].nrows;
+      it.c0.assign(c0 + off, c0 + off + n);
+      it.has_c0 = true;
+      off += n;
+    }
+  }
+  pfor(items_.size(), [&](size_t k) {
+    Item& it = items_[k];
+    BatchQuery* out = run_[k]->out;
+    if (it.kind == Item::kSwap) {
+      guarded(out, [&] { it.xj->finish(it.has_c0 ? &it.c0 : nullptr); });
+    } else if (it.kind == Item::kJoin) {
+      const size_t m = static_cast<size_t>(it.join);
+      if (!guarded(out, [&] {
+            it.jj->finish(it.jw, jouts_[m], jfl[2 * m], jfl[2 * m + 1], it.has_c0 ? &it.c0 : nullptr);
+          }))
+        rel_free(ctx_, jouts_[m]);
+    }
+  });
+  jouts_.clear();
+  joins_.clear();
+  jsmall_.clear();
+  for (PlannedQuery* q : run_) {
+    ++q->next;
+    active_.push_back(q);   // sorted into "next job" or "finished" by the next stage A
+  }
+  run_.clear();
+  items_.clear();
+  prof.finish_s += since(t0);
+}
+
+void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
+  if (b_pending_) {
+    auto t0 = Clock::now();
+    VG_CUDA(cudaEventSynchronize(ev_b_));
+    b_pending_ = false;
+    prof.device_s += since(t0);
+  }
+  if (!run_.empty()) finish_wave();
+
+  // queries with a next job run it; the others finish (or have failed)
+  std::vector<PlannedQuery*> done;
   for (PlannedQuery* q : active_) {
     if (q->out->status != VG_OK || !q->plan || q->next >= q->plan->jobNum()) done.push_back(q);
-    else run.push_back(q);
+    else run_.push_back(q);
   }
-  if (!run.empty()) {
+  active_.clear();
+
+  auto t0 = Clock::now();
+  items_.assign(run_.size(), Item());
+  if (!run_.empty()) {
     ++waves_;
-    enum Kind { kNone, kSelect, kJoin, kSwap };
-    struct Item {
-      Kind kind = kNone;
-      vedas::SelectWork sw;
-      vedas::JoinQueryJob* jj = nullptr;
-      vedas::JoinWork jw;
-      vedas::IndexSwapJob* xj = nullptr;
-      vedas::FullRelationIR* xir = nullptr;
-    };
-    std::vector<Item> items(run.size());
-    auto t0 = Clock::now();
-    pfor(run.size(), [&](size_t k) {
-      PlannedQuery* q = run[k];
+    pfor(run_.size(), [&](size_t k) {
+      PlannedQuery* q = run_[k];
       vedas::QueryJob* job = q->plan->getJob(q->next);
-      Item& it = items[k];
+      Item& it = items_[k];
       guarded(q->out, [&] {
-        if (auto* s = dynamic_cast<vedas::SelectQueryJob*>(job)) {
-          s->prepare(it.sw);
-          it.kind = kSelect;
+        if (auto* sj = dynamic_cast<vedas::SelectQueryJob*>(job)) {
+          sj->prepare(it.sw);
+          it.kind = Item::kSelect;
         } else if (auto* j = dynamic_cast<vedas::JoinQueryJob*>(job)) {
           j->prepare(it.jw);
           it.jj = j;
-          it.kind = it.jw.empty ? kNone : kJoin;
+          it.kind = it.jw.empty ? Item::kNone : Item::kJoin;
         } else if (auto* x = dynamic_cast<vedas::IndexSwapJob*>(job)) {
           it.xj = x;
           it.xir = x->prepare();
-          it.kind = kSwap;
+          it.kind = Item::kSwap;
         } else {
           job->startJob(0);  // transfer: a pass-through on one device
         }
       });
-      if (q->out->status != VG_OK) it.kind = kNone;
+      if (q->out->status != VG_OK) it.kind = Item::kNone;
     });
-    prof.prepare_s += since(t0);
-
-    // 1. every stable re-sort by column 0 of this wave in one segmented sort
-    t0 = Clock::now();
-    std::vector<Rel*> to_sort;
-    for (auto& it : items) {
-      if (it.kind == kJoin) {
-        if (it.jw.sortL) to_sort.push_back(&it.jw.lir->rel());
-        if (it.jw.sortR) to_sort.push_back(&it.jw.rir->rel());
-      } else if (it.kind == kSwap) {
-        to_sort.push_back(&it.xir->rel());
-      }
-    }
-    batched_sort_by_first(ctx_, to_sort);
-
-    // 2. empty-interval scans of swapped relations need column 0 of the small ones
-    std::vector<std::vector<uint32_t>> swap_c0;
-    std::vector<const std::vector<uint32_t>*> swap_c0_of(items.size(), nullptr);
-    {
-      std::vector<const Rel*> small;
-      std::vector<size_t> who;
-      for (size_t k = 0; k < items.size(); ++k)
-        if (items[k].kind == kSwap && items[k].xir->size() > 2 && items[k].xir->size() < 100) {
-          small.push_back(&items[k].xir->rel());
-          who.push_back(k);
-        }
-      batched_col0(ctx_, small, swap_c0);
-      for (size_t m = 0; m < who.size(); ++m) swap_c0_of[who[m]] = &swap_c0[m];
-    }
-
-    // 3. selects: all copies in one launch, all unique compactions in one
-    std::vector<uint64_t> kept_of(items.size(), 0);
-    {
-      std::vector<CopyPiece> pieces;
-      std::vector<SegRows> useg;
-      std::vector<size_t> uwho;
-      for (size_t k = 0; k < items.size(); ++k) {
-        if (items[k].kind != kSelect) continue;
-        auto& w = items[k].sw;
-        if (w.unique) {
-          SegRows s;
-          s.ncols = 1;
-          s.n = w.uniq_n;
-          s.in[0] = w.uniq_src;
-          s.out[0] = w.ir->getRelationRawPointer(0);
-          useg.push_back(s);
-          uwho.push_back(k);
-        } else {
-          pieces.insert(pieces.end(), w.pieces.begin(), w.pieces.end());
-        }
-      }
-      batched_copy(ctx_, pieces);
-      std::vector<uint64_t> kept = batched_unique(ctx_, useg);
-      for (size_t m = 0; m < uwho.size(); ++m) kept_of[uwho[m]] = kept[m];
-    }
-
-    // 4. joins: one count / scan / write chain for all of them
-    std::vector<size_t> jwho;
-    std::vector<Rel> jouts;
-    std::vector<uint32_t> jfl;
-    std::vector<std::vector<uint32_t>> join_c0;
-    std::vector<const std::vector<uint32_t>*> join_c0_of(items.size(), nullptr);
-    {
-      std::vector<const Rel*> L, R;
-      for (size_t k = 0; k < items.size(); ++k)
-        if (items[k].kind == kJoin) {
-          L.push_back(&items[k].jw.lir->rel());
-          R.push_back(&items[k].jw.rir->rel());
-          jwho.push_back(k);
-        }
-      batched_join(ctx_, L, R, jouts, jfl);
-      std::vector<const Rel*> small;
-      std::vector<size_t> who;
-      for (size_t m = 0; m < jwho.size(); ++m)
-        if (!items[jwho[m]].jj->isLastJoinForVar() && jouts[m].nrows > 2 && jouts[m].nrows < 100) {
-          small.push_back(&jouts[m]);
-          who.push_back(jwho[m]);
-        }
-      batched_col0(ctx_, small, join_c0);
-      for (size_t m = 0; m < who.size(); ++m) join_c0_of[who[m]] = &join_c0[m];
-    }
-    prof.device_s += since(t0);
-
-    // 5. host finishing of every job of the wave
-    t0 = Clock::now();
-    std::vector<size_t> jpos(items.size(), 0);
-    for (size_t m = 0; m < jwho.size(); ++m) jpos[jwho[m]] = m;
-    pfor(items.size(), [&](size_t k) {
-      Item& it = items[k];
-      BatchQuery* out = run[k]->out;
-      if (it.kind == kSwap) {
-        guarded(out, [&] { it.xj->finish(swap_c0_of[k]); });
-      } else if (it.kind == kSelect) {
-        if (it.sw.unique) vedas::SelectQueryJob::finishUnique(it.sw, kept_of[k]);
-      } else if (it.kind == kJoin) {
-        const size_t m = jpos[k];
-        if (!guarded(out, [&] { it.jj->finish(it.jw, jouts[m], jfl[2 * m], jfl[2 * m + 1], join_c0_of[k]); }))
-          rel_free(ctx_, jouts[m]);
-      }
-    });
-    for (PlannedQuery* q : run) {
-      ++q->next;
-      if (q->out->status != VG_OK || q->next >= q->plan->jobNum()) done.push_back(q);
-    }
-    prof.finish_s += since(t0);
   }
-  if (!done.empty()) {
-    auto t0 = Clock::now();
-    finalize(done, completed);
-    prof.final_s += since(t0);
-  }
-  for (PlannedQuery* q : done) q->retired = true;
-  std::vector<PlannedQuery*> still;
-  for (PlannedQuery* q : active_)
-    if (!q->retired) still.push_back(q);
-  active_.swap(still);
-}
+  prof.prepare_s += since(t0);
 
-// Projection and the final adjacent-unique pass (QueryPlan::execute, after
-// its job loop) of every query that just finished, in one batched launch.
-void WaveEngine::finalize(std::vector<PlannedQuery*>& done, std::vector<PlannedQuery*>& completed) {
-  // 1. projection and output buffers, per query on the host pool
-  std::vector<SegRows> seg(done.size());
-  std::vector<vedas::FullRelationIR*> res(done.size(), nullptr);
-  pfor(done.size(), [&](size_t k) {
-    PlannedQuery* q = done[k];
-    BatchQuery* out = q->out;
-    if (out->status != VG_OK || !q->plan) return;
-    guarded(out, [&] {
+  // projection of the queries that finished; failed ones go back at once
+  t0 = Clock::now();
+  std::vector<PlannedQuery*> fin;
+  for (PlannedQuery* q : done) {
+    if (q->out->status != VG_OK || !q->plan) retire_failed(q, completed);
+    else fin.push_back(q);
+  }
+  std::vector<SegRows> seg(fin.size());
+  std::vector<vedas::FullRelationIR*> res(fin.size(), nullptr);
+  pfor(fin.size(), [&](size_t k) {
+    PlannedQuery* q = fin[k];
+    guarded(q->out, [&] {
       vedas::FullRelationIR* r = q->plan->project();
-      SegRows& s = seg[k];
-      s.ncols = static_cast<uint32_t>(r->getColumnNum());
-      s.n = r->size();
-      for (uint32_t c = 0; c < s.ncols; ++c) {
-        s.in[c] = r->getRelationRawPointer(c);
-        s.out[c] = ctx_.alloc<uint32_t>(s.n);
+      SegRows& sr = seg[k];
+      sr.ncols = static_cast<uint32_t>(r->getColumnNum());
+      sr.n = r->size();
+      for (uint32_t c = 0; c < sr.ncols; ++c) {
+        sr.in[c] = r->getRelationRawPointer(c);
+        sr.out[c] = ctx_.alloc<uint32_t>(sr.n);
       }
       res[k] = r;
     });
   });
-  // 2. one batched adjacent-unique pass over all of them
-  std::vector<SegRows> fin;
-  std::vector<size_t> who;
-  for (size_t k = 0; k < done.size(); ++k)
+  for (size_t k = 0; k < fin.size(); ++k) {
     if (res[k]) {
-      fin.push_back(seg[k]);
-      who.push_back(k);
+      final_.push_back(fin[k]);
+      fin_seg_.push_back(seg[k]);
+      fin_res_.push_back(res[k]);
+    } else {
+      retire_failed(fin[k], completed);
     }
-  std::vector<uint64_t> kept = batched_unique(ctx_, fin);
-  std::vector<uint64_t> kept_of(done.size(), 0);
-  for (size_t m = 0; m < who.size(); ++m) kept_of[who[m]] = kept[m];
-  // 3. results handed over, intermediates freed, per query on the host pool
-  pfor(done.size(), [&](size_t k) {
-    PlannedQuery* q = done[k];
-    BatchQuery* out = q->out;
-    if (vedas::FullRelationIR* r = res[k]) {
+  }
+  prof.final_s += since(t0);
+
+  // device half 1
+  t0 = Clock::now();
+  std::vector<Rel*> to_sort;
+  std::vector<const Rel*> swap_rels;
+  swap_small_.clear();
+  joins_.clear();
+  std::vector<CopyPiece> pieces;
+  std::vector<const Rel*> jl, jr;
+  for (size_t k = 0; k < items_.size(); ++k) {
+    Item& it = items_[k];
+    if (it.kind == Item::kJoin) {
+      if (it.jw.sortL) to_sort.push_back(&it.jw.lir->rel());
+      if (it.jw.sortR) to_sort.push_back(&it.jw.rir->rel());
+      it.join = static_cast<int64_t>(joins_.size());
+      joins_.push_back(k);
+      jl.push_back(&it.jw.lir->rel());
+      jr.push_back(&it.jw.rir->rel());
+    } else if (it.kind == Item::kSwap) {
+      to_sort.push_back(&it.xir->rel());
+      if (it.xir->size() > 2 && it.xir->size() < 100) {
+        swap_small_.push_back(k);
+        swap_rels.push_back(&it.xir->rel());
+      }
+    } else if (it.kind == Item::kSelect) {
+      pieces.insert(pieces.end(), it.sw.pieces.begin(), it.sw.pieces.end());
+    }
+  }
+  const size_t c0_words = (col0_words(swap_rels) + 1) / 2;
+  off_tot_ = 0;
+  off_fin_ = off_tot_ + jl.size();
+  off_c0_ = off_fin_ + fin_seg_.size();
+  uint64_t* ha = h_a_.reserve(off_c0_ + c0_words + 1);
+  bool any = false;
+  if (!to_sort.empty()) {
+    batched_sort_by_first(ctx_, to_sort, key_bits_);
+    any = true;
+  }
+  if (!swap_rels.empty()) {
+    batched_col0_enqueue(ctx_, swap_rels, reinterpret_cast<uint32_t*>(ha + off_c0_));
+    any = true;
+  }
+  if (!pieces.empty()) {
+    batched_copy(ctx_, pieces);
+    any = true;
+  }
+  if (!jl.empty()) {
+    batched_join_count(ctx_, jl, jr, jb_, ha + off_tot_);
+    any = true;
+  }
+  if (!fin_seg_.empty()) {
+    batched_unique_enqueue(ctx_, fin_seg_, ha + off_fin_);
+    any = true;
+  }
+  if (any) {
+    VG_CUDA(cudaEventRecord(ev_a_, ctx_.stream));
+    a_pending_ = true;
+  }
+  prof.device_s += since(t0);
+}
+
+void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
+  if (!a_pending_) return;
+  auto t0 = Clock::now();
+  VG_CUDA(cudaEventSynchronize(ev_a_));
+  a_pending_ = false;
+  prof.device_s += since(t0);
+  const uint64_t* ha = h_a_.data();
+
+  // staged columns of the wave in flight
+  {
+    const uint32_t* c0 = reinterpret_cast<const uint32_t*>(ha + off_c0_);
+    uint64_t off = 0;
+    for (size_t k : swap_small_) {
+      Item& it = items_[k];
+      const uint64_t n = it.xir->size();
+      it.c0.assign(c0 + off, c0 + off + n);
+      it.has_c0 = true;
+      off += n;
+    }
+  }
+
+  // queries that finished: results handed back
+  t0 = Clock::now();
+  if (!final_.empty()) {
+    const uint64_t* kept = ha + off_fin_;
+    note_unique_writes(ctx_, fin_seg_, kept);
+    pfor(final_.size(), [&](size_t k) {
+      PlannedQuery* q = final_[k];
+      BatchQuery* out = q->out;
+      vedas::FullRelationIR* r = fin_res_[k];
       for (size_t c = 0; c < r->getColumnNum(); ++c) out->headers.push_back(r->getHeader(c));
       Rel in = r->release();
       rel_free(ctx_, in);
       Rel o;
-      o.ncols = seg[k].ncols;
-      o.nrows = kept_of[k];
+      o.ncols = fin_seg_[k].ncols;
+      o.nrows = kept[k];
       for (uint32_t c = 0; c < o.ncols; ++c) {
-        o.cols[c] = seg[k].out[c];
+        o.cols[c] = fin_seg_[k].out[c];
         ctx_.arena.shrink(o.cols[c], o.nrows * sizeof(uint32_t));
       }
       out->rel = o;
+      if (q->ex) out->log = std::move(q->ex->exe_log);
+      q->plan.reset();  // frees every intermediate relation of the query
+    });
+    for (PlannedQuery* q : final_) completed.push_back(q);
+    final_.clear();
+    fin_seg_.clear();
+    fin_res_.clear();
+  }
+  prof.final_s += since(t0);
+
+  // device half 2: join outputs
+  t0 = Clock::now();
+  if (!joins_.empty()) {
+    const uint64_t* tot = ha + off_tot_;
+    std::vector<const Rel*> small;
+    std::vector<size_t> who;
+    for (size_t m = 0; m < joins_.size(); ++m) {
+      Item& it = items_[joins_[m]];
+      if (!it.jj->isLastJoinForVar() && tot[m] > 2 && tot[m] < 100) who.push_back(m);
     }
-    if (q->ex) out->log = std::move(q->ex->exe_log);
-    q->plan.reset();  // frees every intermediate relation of the query
-  });
-  for (PlannedQuery* q : done) completed.push_back(q);
+    const size_t J = joins_.size();
+    uint64_t small_rows = 0;
+    for (size_t m : who) small_rows += tot[m];
+    off_fl_ = 0;
+    off_jc0_ = (2 * J + 1) / 2;
+    uint64_t* hb = h_b_.reserve(off_jc0_ + (small_rows + 1) / 2 + 1);
+    batched_join_write(ctx_, jb_, tot, jouts_, reinterpret_cast<uint32_t*>(hb + off_fl_));
+    for (size_t m : who) small.push_back(&jouts_[m]);
+    batched_col0_enqueue(ctx_, small, reinterpret_cast<uint32_t*>(hb + off_jc0_));
+    jsmall_ = std::move(who);
+    VG_CUDA(cudaEventRecord(ev_b_, ctx_.stream));
+    b_pending_ = true;
+  } else {
+    jsmall_.clear();
+  }
+  prof.device_s += since(t0);
 }
 
 void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts, BatchResult& out) {
@@ -420,15 +511,39 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
     pq[i].out = &out.queries[i];
     plan_query(ctx, storage, texts[i], pq[i]);
   });
-  WaveEngine eng(ctx);
-  eng.prof.plan_s = since(t0);
-  for (auto& q : pq) eng.add(&q);
+  const double plan_s = since(t0);
+  // two engines take turns on the stream: while the device runs one
+  // engine's half-wave, the host runs the other's stages
+  const int kb = key_bits_for(storage);
+  WaveEngine e0(ctx, kb), e1(ctx, kb);
+  for (size_t i = 0; i < pq.size(); ++i) (i % 2 ? e1 : e0).add(&pq[i]);
   std::vector<PlannedQuery*> completed;
-  while (eng.active() > 0) eng.wave(completed);
-  out.waves = eng.waves();
-  out.prof = eng.prof;
+  while (e0.active() > 0 || e1.active() > 0) {
+    if (e0.active() > 0) e0.step(completed);
+    if (e1.active() > 0) e1.step(completed);
+  }
+  out.waves = std::max(e0.waves(), e1.waves());
+  out.prof = e0.prof;
+  out.prof.prepare_s += e1.prof.prepare_s;
+  out.prof.device_s += e1.prof.device_s;
+  out.prof.finish_s += e1.prof.finish_s;
+  out.prof.final_s += e1.prof.final_s;
+  out.prof.plan_s = plan_s;
   ctx.check_device_errors();
+  // parsed queries and executors (bounds, empty intervals, logs) go on the pool
+  pfor(pq.size(), [&](size_t i) {
+    pq[i].plan.reset();
+    pq[i].ex.reset();
+    pq[i].sq.reset();
+  });
   out.prof.total_s = since(t_all);
+}
+
+int key_bits_for(vedas::VedasStorage* storage) {
+  const uint32_t m = storage->index().max_id;
+  int b = 1;
+  while (b < 32 && (uint64_t{1} << b) <= m) ++b;
+  return b;
 }
 
 }  // namespace vg

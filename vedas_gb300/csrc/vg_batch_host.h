@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "compat/vedas_compat.h"
+#include "vg_batch.h"
 #include "vg_relops.h"
 
 namespace vg {
@@ -31,7 +32,6 @@ struct PlannedQuery {
   size_t next = 0;
   uint64_t est_bytes = 0;   // estimated HBM for its relations (admission)
   BatchQuery* out = nullptr;
-  bool retired = false;     // handed back by the wave engine
 };
 
 // Plans one query on the host (thread-safe across queries once the storage's
@@ -40,25 +40,81 @@ void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text,
 void prepare_mirrors(vedas::VedasStorage* storage);
 
 // Advances every added query by one job per wave; the device work of a wave
-// is issued as batched launches.  Queries that finish (or fail) are projected,
-// de-duplicated in one batched pass, have their intermediates freed and are
-// handed back.
+// is issued as batched launches.  A wave has two stages:
+//  A: finish the previous wave's jobs on the host, prepare every query's next
+//     job, and enqueue the first device half (sorts, select copies, join
+//     counts and scans, and the final compaction of queries that just
+//     finished);
+//  B: wait for that half, hand finished queries back, allocate the join
+//     outputs and enqueue the join writes.
+// Nothing else waits on the device.  Two engines on one stream that take
+// turns (A of one, then A of the other, then B of each) keep the device busy
+// with one engine's work while the host runs the other's stages.
 class WaveEngine {
  public:
-  explicit WaveEngine(Ctx& ctx) : ctx_(ctx) {}
+  // key_bits bounds every relation value (< 2^key_bits), so the segmented
+  // sorts run without a host round trip; 0 when unknown.
+  explicit WaveEngine(Ctx& ctx, int key_bits = 0);
+  ~WaveEngine();
+  WaveEngine(const WaveEngine&) = delete;
+  WaveEngine& operator=(const WaveEngine&) = delete;
   void add(PlannedQuery* pq);
-  size_t active() const { return active_.size(); }
+  // Queries added and not yet handed back (waiting, in flight or finishing).
+  size_t active() const { return active_.size() + run_.size() + final_.size(); }
   // Forgets every query in flight (after a device-level failure).
-  void reset() { active_.clear(); }
-  void wave(std::vector<PlannedQuery*>& completed);
+  void reset();
+  // Stage A then stage B.
+  void wave(std::vector<PlannedQuery*>& completed) {
+    stage_a(completed);
+    stage_b(completed);
+  }
+  // The next stage (A and B alternate).
+  void step(std::vector<PlannedQuery*>& completed);
   uint32_t waves() const { return waves_; }
   BatchProfile prof;
 
+  // Host state of one job of the wave in flight.
+  struct Item {
+    enum Kind { kNone, kSelect, kJoin, kSwap } kind = kNone;
+    vedas::SelectWork sw;
+    vedas::JoinQueryJob* jj = nullptr;
+    vedas::JoinWork jw;
+    vedas::IndexSwapJob* xj = nullptr;
+    vedas::FullRelationIR* xir = nullptr;
+    int64_t join = -1;                  // index among the wave's joins
+    std::vector<uint32_t> c0;           // staged column 0 (small swapped relations, small join outputs)
+    bool has_c0 = false;
+  };
+
  private:
+  void stage_a(std::vector<PlannedQuery*>& completed);
+  void stage_b(std::vector<PlannedQuery*>& completed);
+  void finish_wave();
+  void retire_failed(PlannedQuery* q, std::vector<PlannedQuery*>& completed);
+
   Ctx& ctx_;
-  std::vector<PlannedQuery*> active_;
+  int key_bits_ = 0;
   uint32_t waves_ = 0;
-  void finalize(std::vector<PlannedQuery*>& done, std::vector<PlannedQuery*>& completed);
+  bool next_is_a_ = true;
+  std::vector<PlannedQuery*> active_;   // queries waiting for their next job
+  // the wave in flight
+  std::vector<PlannedQuery*> run_;
+  std::vector<Item> items_;
+  std::vector<size_t> swap_small_;      // items whose swapped relation stages column 0
+  std::vector<size_t> joins_;           // items with a join, in batch order
+  std::vector<size_t> jsmall_;          // joins (by batch index) whose small output stages column 0
+  JoinBatch jb_;
+  std::vector<Rel> jouts_;
+  // queries whose last job finished: compacted in stage A, handed back in stage B
+  std::vector<PlannedQuery*> final_;
+  std::vector<SegRows> fin_seg_;
+  std::vector<vedas::FullRelationIR*> fin_res_;
+  // device -> host results of each stage and the events that mark them
+  PinnedWords h_a_, h_b_;
+  size_t off_tot_ = 0, off_fin_ = 0, off_c0_ = 0;   // words into h_a_
+  size_t off_fl_ = 0, off_jc0_ = 0;                               // words into h_b_
+  cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;
+  bool a_pending_ = false, b_pending_ = false;
 };
 
 struct BatchResult {
@@ -68,6 +124,9 @@ struct BatchResult {
   BatchProfile prof;
   ~BatchResult();
 };
+
+// Bits that hold every id of the storage's index (for WaveEngine's key_bits).
+int key_bits_for(vedas::VedasStorage* storage);
 
 // Runs every query to completion together; per-query failures are recorded
 // in their BatchQuery and do not stop the others.

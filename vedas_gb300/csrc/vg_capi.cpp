@@ -132,6 +132,7 @@ vg_status vg_ctx_destroy(vg_ctx* ctx) {
   if (!ctx) return VG_OK;
   vg::Ctx& c = ctx->c;
   if (c.stream) cudaStreamSynchronize(c.stream);
+  c.release_upload_ring();
   c.arena.release();
   if (c.d_err) cudaFree(c.d_err);
   if (c.h_small) cudaFreeHost(c.h_small);
@@ -494,6 +495,11 @@ uint32_t vg_batch_ncols(const vg_batch* b, uint32_t q) {
 }
 uint64_t vg_batch_nrows(const vg_batch* b, uint32_t q) {
   return (b && q < b->r.queries.size()) ? b->r.queries[q].rel.nrows : 0;
+}
+vg_status vg_batch_rows(const vg_batch* b, uint64_t* nrows) {
+  if (!b || (!nrows && !b->r.queries.empty())) return VG_ERR_INVALID;
+  for (size_t q = 0; q < b->r.queries.size(); ++q) nrows[q] = b->r.queries[q].rel.nrows;
+  return VG_OK;
 }
 const char* vg_batch_header(const vg_batch* b, uint32_t q, uint32_t c) {
   if (!b || q >= b->r.queries.size() || c >= b->r.queries[q].headers.size()) return nullptr;

@@ -1,6 +1,7 @@
 #include "vg_ctx.h"
 
 #include <algorithm>
+#include <cstring>
 
 namespace vg {
 
@@ -258,6 +259,60 @@ size_t Arena::largest_free() const {
   size_t m = 0;
   for (auto& kv : free_) m = kv.second > m ? kv.second : m;
   return m;
+}
+
+void Ctx::upload_bytes(void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return;
+  constexpr size_t kRingMin = size_t{16} << 20;
+  const size_t need = (bytes + 255) / 256 * 256;
+  if (need > ring_cap_) {
+    // grow: wait for every copy out of the old ring, then replace it
+    for (RingUse& u : ring_used_) {
+      VG_CUDA(cudaEventSynchronize(u.done));
+      event_pool.push_back(u.done);
+    }
+    ring_used_.clear();
+    if (ring_) VG_CUDA(cudaFreeHost(ring_));
+    ring_ = nullptr;
+    ring_cap_ = 0;
+    size_t cap = kRingMin;
+    while (cap < 4 * need) cap *= 2;
+    VG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&ring_), cap, cudaHostAllocDefault));
+    ring_cap_ = cap;
+    ring_head_ = 0;
+  }
+  if (ring_head_ + need > ring_cap_) ring_head_ = 0;
+  const size_t b = ring_head_, e = ring_head_ + need;
+  // regions are reused in FIFO order: retire the oldest copies until [b, e) is free
+  while (!ring_used_.empty()) {
+    const RingUse& u = ring_used_.front();
+    const bool overlaps = u.begin < e && b < u.end;
+    if (!overlaps && cudaEventQuery(u.done) != cudaSuccess) break;
+    VG_CUDA(cudaEventSynchronize(u.done));
+    event_pool.push_back(u.done);
+    ring_used_.pop_front();
+  }
+  for (const RingUse& u : ring_used_)
+    if (u.begin < e && b < u.end) fail(VG_ERR_CUDA, "upload ring bookkeeping");
+  std::memcpy(ring_ + b, src, bytes);
+  VG_CUDA(cudaMemcpyAsync(dst, ring_ + b, bytes, cudaMemcpyHostToDevice, stream));
+  cudaEvent_t ev = take_event();
+  VG_CUDA(cudaEventRecord(ev, stream));
+  ring_used_.push_back({b, e, ev});
+  ring_head_ = e;
+}
+
+void Ctx::release_upload_ring() {
+  for (RingUse& u : ring_used_) {
+    cudaEventSynchronize(u.done);
+    cudaEventDestroy(u.done);
+  }
+  ring_used_.clear();
+  if (ring_) cudaFreeHost(ring_);
+  ring_ = nullptr;
+  ring_cap_ = ring_head_ = 0;
+  for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+  event_pool.clear();
 }
 
 cudaEvent_t Ctx::take_event() {

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -116,6 +117,14 @@ struct Ctx {
 
   bool timing = false;
   uint64_t launches = 0;
+  // page-locked upload ring: [ring_, ring_ + ring_cap_), regions in flight in FIFO order
+  char* ring_ = nullptr;
+  size_t ring_cap_ = 0, ring_head_ = 0;
+  struct RingUse {
+    size_t begin, end;
+    cudaEvent_t done;
+  };
+  std::deque<RingUse> ring_used_;
   std::map<std::string, KernelStat> kstats;
   std::vector<cudaEvent_t> event_pool;
 
@@ -140,6 +149,13 @@ struct Ctx {
   // Converts recorded event pairs into milliseconds (synchronizes).
   void collect_timing();
   void reset_stats();
+
+  // Copies `bytes` from host memory to device memory `dst` on the stream,
+  // through a page-locked ring, so the copy never waits for earlier work
+  // (a copy from pageable memory may).  The caller's buffer is free to reuse
+  // on return.
+  void upload_bytes(void* dst, const void* src, size_t bytes);
+  void release_upload_ring();
 
   template <typename T>
   T* alloc(uint64_t n) {

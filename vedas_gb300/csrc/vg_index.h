@@ -40,6 +40,7 @@ struct Index {
   Ctx* ctx = nullptr;
   bool full = false;
   uint64_t n = 0;
+  uint32_t max_id = 0;   // largest subject, predicate or object id (bounds relation values)
   std::map<std::string, DevArray> dev;
   std::map<std::string, std::vector<uint32_t>> host;  // mirrors, made on request
 

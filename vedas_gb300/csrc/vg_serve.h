@@ -36,7 +36,8 @@ struct ServeItem {
 
 class Server {
  public:
-  Server(Ctx& ctx, vedas::VedasStorage* st, uint64_t budget) : ctx_(ctx), st_(st), budget_(budget), eng_(ctx) {
+  Server(Ctx& ctx, vedas::VedasStorage* st, uint64_t budget)
+      : ctx_(ctx), st_(st), budget_(budget), eng_(ctx, key_bits_for(st)) {
     prepare_mirrors(st_);
     VG_CUDA(cudaStreamCreateWithFlags(&dl_stream_, cudaStreamNonBlocking));
     worker_ = std::thread([this] { loop(); });

@@ -6,7 +6,9 @@
 // sort is stable; tiles take their index from an atomic ticket in launch
 // order, which guarantees that every look-back predecessor is running.
 // Passes whose digit is the same for every key are skipped (the permutation
-// would be the identity).
+// would be the identity), unless the caller asks for the variant without a
+// host round trip, which scans the bucket bases on the device and runs every
+// pass over [0, end_bit).
 #include "vg_sort.h"
 
 #include <vector>
@@ -38,6 +40,22 @@ __global__ void __launch_bounds__(kBlock) radix_hist_kernel(const K* __restrict_
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < passes * kRadix; i += kBlock)
     if (sh[i]) atomicAdd(&hist[i], static_cast<unsigned long long>(sh[i]));
+}
+
+// Exclusive scan of each pass's 256 digit counts (one block per pass).
+__global__ void __launch_bounds__(kRadix) radix_bases_kernel(const unsigned long long* __restrict__ hist,
+                                                              uint64_t* __restrict__ bases) {
+  __shared__ uint64_t s[kRadix];
+  const uint32_t p = blockIdx.x, d = threadIdx.x;
+  s[d] = hist[p * kRadix + d];
+  __syncthreads();
+  for (uint32_t off = 1; off < kRadix; off <<= 1) {
+    const uint64_t v = d >= off ? s[d - off] : 0;
+    __syncthreads();
+    s[d] += v;
+    __syncthreads();
+  }
+  bases[p * kRadix + d] = s[d] - hist[p * kRadix + d];
 }
 
 __global__ void iota_kernel(uint32_t* out, uint64_t n) {
@@ -167,7 +185,7 @@ void launch_pass(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uint32_t*
 
 template <typename K>
 bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* vals_alt, uint64_t n,
-                     int end_bit, bool vals_iota) {
+                     int end_bit, bool vals_iota, bool host_skip) {
   const bool has_v = vals != nullptr;
   if (n == 0) return false;
   if (n > 0xFFFFFFFFull && has_v) fail(VG_ERR_OVERFLOW, "radix sort values are 32-bit row ids");
@@ -185,34 +203,42 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
     radix_hist_kernel<K><<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(keys, n, passes, hist.get());
   });
   VG_CUDA(cudaGetLastError());
-  std::vector<unsigned long long> h(passes * kRadix);
-  VG_CUDA(cudaMemcpyAsync(h.data(), hist.get(), h.size() * sizeof(unsigned long long),
-                          cudaMemcpyDeviceToHost, ctx.stream));
-  ctx.sync();
-
-  std::vector<uint64_t> bases(passes * kRadix);
-  std::vector<int> todo;
-  for (int p = 0; p < passes; ++p) {
-    uint64_t run = 0;
-    bool trivial = false;
-    for (int d = 0; d < kRadix; ++d) {
-      const uint64_t c = h[p * kRadix + d];
-      if (c == n) trivial = true;
-      bases[p * kRadix + d] = run;
-      run += c;
-    }
-    if (!trivial) todo.push_back(p);
-  }
-  if (todo.empty()) {
-    if (has_v && vals_iota) {
-      ctx.launch("iota", 4.0 * n, [&] { iota_kernel<<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(vals, n); });
-      VG_CUDA(cudaGetLastError());
-    }
-    return false;
-  }
   Scratch<uint64_t> d_bases(ctx, passes * kRadix);
-  VG_CUDA(cudaMemcpyAsync(d_bases.get(), bases.data(), bases.size() * sizeof(uint64_t),
-                          cudaMemcpyHostToDevice, ctx.stream));
+  std::vector<int> todo;
+  if (host_skip) {
+    std::vector<unsigned long long> h(passes * kRadix);
+    VG_CUDA(cudaMemcpyAsync(h.data(), hist.get(), h.size() * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+    std::vector<uint64_t> bases(passes * kRadix);
+    for (int p = 0; p < passes; ++p) {
+      uint64_t run = 0;
+      bool trivial = false;
+      for (int d = 0; d < kRadix; ++d) {
+        const uint64_t c = h[p * kRadix + d];
+        if (c == n) trivial = true;
+        bases[p * kRadix + d] = run;
+        run += c;
+      }
+      if (!trivial) todo.push_back(p);
+    }
+    if (todo.empty()) {
+      if (has_v && vals_iota) {
+        ctx.launch("iota", 4.0 * n, [&] { iota_kernel<<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(vals, n); });
+        VG_CUDA(cudaGetLastError());
+      }
+      return false;
+    }
+    VG_CUDA(cudaMemcpyAsync(d_bases.get(), bases.data(), bases.size() * sizeof(uint64_t),
+                            cudaMemcpyHostToDevice, ctx.stream));
+  } else {
+    // no host round trip: bases scanned on the device and every pass runs
+    ctx.launch("radix_bases", 0.0, [&] {
+      radix_bases_kernel<<<static_cast<unsigned>(passes), kRadix, 0, ctx.stream>>>(hist.get(), d_bases.get());
+    });
+    VG_CUDA(cudaGetLastError());
+    for (int p = 0; p < passes; ++p) todo.push_back(p);
+  }
   const uint64_t tiles = div_up(n, kTile);
   Scratch<uint64_t> status(ctx, tiles * kRadix);
   Scratch<uint32_t> ticket(ctx, todo.size());
@@ -245,13 +271,13 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
 }  // namespace
 
 bool radix_sort_u32(Ctx& ctx, uint32_t* keys, uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
-                    uint64_t n, int end_bit, bool vals_iota) {
-  return radix_sort_impl<uint32_t>(ctx, keys, keys_alt, vals, vals_alt, n, end_bit, vals_iota);
+                    uint64_t n, int end_bit, bool vals_iota, bool host_skip) {
+  return radix_sort_impl<uint32_t>(ctx, keys, keys_alt, vals, vals_alt, n, end_bit, vals_iota, host_skip);
 }
 
 bool radix_sort_u64(Ctx& ctx, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
-                    uint64_t n, int end_bit, bool vals_iota) {
-  return radix_sort_impl<uint64_t>(ctx, keys, keys_alt, vals, vals_alt, n, end_bit, vals_iota);
+                    uint64_t n, int end_bit, bool vals_iota, bool host_skip) {
+  return radix_sort_impl<uint64_t>(ctx, keys, keys_alt, vals, vals_alt, n, end_bit, vals_iota, host_skip);
 }
 
 void fill_iota(Ctx& ctx, uint32_t* out, uint64_t n) {

@@ -1,4 +1,5 @@
 // Resident index: build orchestration, host mirrors and the .vds format.
+#include <algorithm>
 #include <cstdio>
 #include <fstream>
 
@@ -45,6 +46,7 @@ void build_index(Ctx& ctx, const uint32_t* s, const uint32_t* p, const uint32_t*
   uint32_t mx[3];
   column_max3(ctx, s, p, o, n, mx);
   const uint32_t ms = mx[0], mp = mx[1], mo = mx[2];
+  ix.max_id = std::max(ms, std::max(mp, mo));
   auto put = [&](const char* name, const DevArray& a) { ix.dev[name] = a; };
   {
     PermOutputs pso;
@@ -150,6 +152,10 @@ void open_vds(Ctx& ctx, const char* path, bool full, Index& ix) {
   if (full)
     for (const char* n : kVdsFullOrder) r(n);
   ix.n = ix.get("pso_data").len;
+  // subjects and objects are the level-2 keys and data of PSO; predicates the level-1 keys
+  ix.max_id = 0;
+  for (const char* name : {"ps_data", "pso_data", "p_idx_values"})
+    for (uint32_t v : ix.host[name]) ix.max_id = std::max(ix.max_id, v);
   ctx.sync();
 }
 
