@@ -181,28 +181,15 @@ def run_plain(ix, queries, download=False):
     return rows, d2h
 
 
-_PINNED = {}
-
-
-def pinned_buffer(nbytes: int):
-    """A reusable page-locked host buffer (torch only allocates it)."""
-    import torch
-    buf = _PINNED.get("b")
-    if buf is None or buf.numel() < nbytes:
-        buf = torch.empty(max(nbytes, 1), dtype=torch.uint8, pin_memory=True)
-        _PINNED["b"] = buf
-    return buf
-
-
 def run_batch(ix, queries, download=False, profile=None):
+    """One batched step; with download every result also lands in host
+    memory (copied while the batch runs, complete when it returns)."""
     import vedas_gb300 as vg
-    b = vg.Batch(ix, queries)
+    b = vg.Batch(ix, queries, to_host=download)
     rows = b.run()
     d2h = 0
     if download:
-        words = b.result_words()
-        buf = pinned_buffer(4 * words)
-        d2h = b.download_all(buf.data_ptr())
+        d2h = 4 * b.result_words()
     if profile is not None:
         for k, v in b.profile().items():
             profile[k] = profile.get(k, 0.0) + v

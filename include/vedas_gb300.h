@@ -233,6 +233,16 @@ typedef struct vg_batch vg_batch;
  * own status; the others complete. */
 vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq,
                        vg_batch** out);
+/* vg_batch_run, and every query's result columns are also copied to
+ * page-locked host memory owned by the batch as the query finishes, on a
+ * second stream, so the transfers overlap the rest of the batch.  The copies
+ * are complete when the call returns; vg_batch_host_column gives them (valid
+ * until vg_batch_free; vg_batch_nrows(b, q) words; NULL for a failed query).
+ * The reference has no batched execution; this is the batch counterpart of
+ * reading a SparqlResult on the host (src/SparqlResult.cu). */
+vg_status vg_batch_run_host(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq,
+                            vg_batch** out);
+const uint32_t* vg_batch_host_column(const vg_batch* b, uint32_t q, uint32_t c);
 uint32_t vg_batch_size(const vg_batch* b);
 uint32_t vg_batch_waves(const vg_batch* b);
 /* Seconds spent: out6 = {host planning, host job preparation, batched device

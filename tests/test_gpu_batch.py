@@ -77,3 +77,31 @@ def test_batch_empty_and_single(ctx):
         np.testing.assert_array_equal(a, c)
     b.close()
     ix.close()
+
+
+def test_batch_host_copies_equal_device_results(ctx):
+    """Results copied to host memory while the batch runs equal the device
+    results, query by query, over two batches that reuse the host chunks."""
+    import vedas_gb300 as vg
+    g = workloads.graph_chain(n=300_000, n_entities=30_000, seed=14)
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    for seed in (15, 16):
+        qs = workloads.query_mix(g, 500, seed=seed)
+        b = vg.Batch(ix, qs, to_host=True)
+        plain = vg.Batch(ix, qs)
+        total = 0
+        for i in range(len(qs)):
+            assert b.status(i) == plain.status(i)
+            if b.status(i) != 0:
+                continue
+            dev = plain.columns(i)
+            host = b.host_columns(i)
+            assert len(dev) == len(host)
+            for a, c in zip(host, dev):
+                np.testing.assert_array_equal(a, c)
+            total += sum(a.shape[0] for a in host)
+        assert total > 0
+        assert 4 * b.result_words() == 4 * plain.result_words()
+        plain.close()
+        b.close()
+    ix.close()

@@ -148,3 +148,37 @@ def test_mixed_queries_match_oracle(ctx, graph):
         checked += 1
     assert checked > 150
     ix.close()
+
+
+def test_select_results_own_their_columns(ctx):
+    """Selects read index slices without copying them; a select handed to the
+    caller must still own (and free) every column, with the reference's rows."""
+    import vedas_gb300 as vg
+    g = workloads.graph_small_star(n=120_000, n_subjects=6_000, seed=12)
+    used0 = ctx.memory()[0]
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    order = np.lexsort((g.o, g.s, g.p))            # PSO order
+    ps, pso, pp = g.s[order], g.o[order], g.p[order]
+    for p in (1, 5, 9):
+        b, e = np.searchsorted(pp, p, "left"), np.searchsorted(pp, p, "right")
+        # two variables, both used: (subject, object) rows of predicate p
+        rel, _ = vg.select(ctx, ix, 3, p, index_pos=False, second_used=True)
+        got = rel.to_host()
+        np.testing.assert_array_equal(got[0], ps[b:e])
+        np.testing.assert_array_equal(got[1], pso[b:e])
+        rel.free()
+        # second variable unused: the distinct subjects, in order
+        rel, _ = vg.select(ctx, ix, 3, p, index_pos=False, second_used=False)
+        sub = ps[b:e]
+        keep = np.ones(sub.shape[0], dtype=bool)
+        keep[1:] = sub[1:] != sub[:-1]
+        np.testing.assert_array_equal(rel.to_host()[0], sub[keep])
+        rel.free()
+        # one variable: subjects of (?, p, o)
+        o = int(pso[b + (e - b) // 2])
+        rel, _ = vg.select(ctx, ix, 1, p, constant=o)
+        exp = np.sort(g.s[(g.p == p) & (g.o == o)], kind="stable")
+        np.testing.assert_array_equal(rel.to_host()[0], exp)
+        rel.free()
+    ix.close()
+    assert ctx.memory()[0] == used0               # every column freed exactly once

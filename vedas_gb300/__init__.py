@@ -92,6 +92,8 @@ def lib():
                                      ctypes.POINTER(u64)]),
             "vg_result_free": (i32, [vp]),
             "vg_batch_run": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(vp)]),
+            "vg_batch_run_host": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(vp)]),
+            "vg_batch_host_column": (vp, [vp, u32, u32]),
             "vg_batch_size": (u32, [vp]),
             "vg_batch_waves": (u32, [vp]),
             "vg_batch_query_status": (i32, [vp, u32]),
@@ -292,13 +294,33 @@ class Batch:
 
     OPS = Result.OPS
 
-    def __init__(self, ix: "Index", queries):
+    def __init__(self, ix: "Index", queries, to_host: bool = False):
+        """Runs the queries; with to_host every result is also copied to
+        page-locked host memory while the batch runs (host_columns)."""
         self.ix = ix
         self.n = len(queries)
-        arr = (ctypes.c_char_p * self.n)(*[q.encode() for q in queries])
+        self.to_host = to_host
+        arr = (ctypes.c_char_p * self.n)(*[q if isinstance(q, bytes) else q.encode() for q in queries])
         h = ctypes.c_void_p()
-        check(lib().vg_batch_run(ix.ctx.h, ix.h, arr, self.n, ctypes.byref(h)))
+        run = lib().vg_batch_run_host if to_host else lib().vg_batch_run
+        check(run(ix.ctx.h, ix.h, arr, self.n, ctypes.byref(h)))
         self.h = h
+
+    def host_columns(self, q: int):
+        """Query q's result columns from the batch's host copies (to_host)."""
+        if not self.to_host:
+            raise VgError(1, "the batch was run without host copies")
+        L = lib()
+        n = self.nrows(q)
+        out = []
+        for c in range(L.vg_batch_ncols(self.h, q)):
+            p = L.vg_batch_host_column(self.h, q, c)
+            if n == 0 or not p:
+                out.append(np.zeros(n, dtype=np.uint32))
+            else:
+                buf = (ctypes.c_uint32 * n).from_address(p)
+                out.append(np.frombuffer(buf, dtype=np.uint32).copy())
+        return out
 
     def run(self) -> int:
         """Total result rows (the batch already ran in the constructor)."""

@@ -48,6 +48,17 @@ FullRelationIR::FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSi
   is_predicates.resize(columnNum);
 }
 
+FullRelationIR::FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSize, const TYPEID* const* views)
+    : ctx_(ctx) {
+  if (columnNum > VG_MAX_COLS) throw vg::Error(VG_ERR_UNSUPPORTED, "more than 9 columns");
+  r_.ncols = static_cast<uint32_t>(columnNum);
+  r_.nrows = relationSize;
+  for (size_t c = 0; c < columnNum; ++c) r_.cols[c] = const_cast<TYPEID*>(views[c]);
+  r_.borrowed = (1u << columnNum) - 1u;
+  headers.resize(columnNum);
+  is_predicates.resize(columnNum);
+}
+
 FullRelationIR::~FullRelationIR() { vg::rel_free(*ctx_, r_); }
 
 void FullRelationIR::adopt(vg::Rel& r) {
@@ -88,6 +99,8 @@ void FullRelationIR::sortByFirstColumn() { vg::sort_by_first(*ctx_, r_); }
 void FullRelationIR::swapColumn(size_t i, size_t j) {  // src/FullRelationIR.cu:715-727
   if (i == j) return;
   std::swap(r_.cols[i], r_.cols[j]);
+  const uint32_t bi = r_.borrowed >> i & 1u, bj = r_.borrowed >> j & 1u;
+  r_.borrowed = (r_.borrowed & ~((1u << i) | (1u << j))) | (bi << j) | (bj << i);
   bool t = is_predicates[i];
   is_predicates[i] = is_predicates[j];
   is_predicates[j] = t;
@@ -97,7 +110,10 @@ void FullRelationIR::swapColumn(size_t i, size_t j) {  // src/FullRelationIR.cu:
 }
 
 void FullRelationIR::removeColumn(size_t i) {  // src/FullRelationIR.cu:729-736
-  ctx_->free(r_.cols[i]);
+  vg::rel_drop_col(*ctx_, r_, static_cast<uint32_t>(i));
+  // columns above i move down one place, with their ownership bits
+  const uint32_t low = r_.borrowed & ((1u << i) - 1u);
+  r_.borrowed = low | ((r_.borrowed >> (i + 1)) << i);
   for (size_t k = i; k + 1 < r_.ncols; ++k) r_.cols[k] = r_.cols[k + 1];
   r_.cols[r_.ncols - 1] = nullptr;
   r_.ncols -= 1;
@@ -590,11 +606,12 @@ void SelectQueryJob::prepare(SelectWork& w) {
                                                   static_cast<TYPEID>(r1.second), dataid[1]);
     if (r2.first > r2.second) r2.second = r2.first;
     const size_t rows = r2.second - r2.first;
-    auto* ir = new FullRelationIR(ctx, 1, rows);
+    // the uploaded slice is read, never written: the relation views it
+    const TYPEID* view[1] = {ddata + r2.first};
+    auto* ir = rows ? new FullRelationIR(ctx, 1, rows, view) : new FullRelationIR(ctx, 1, 0);
     ir->setHeader(0, variables[0], false);
     intermediateResult = ir;
     w.ir = ir;
-    if (rows) w.pieces.push_back({ddata + r2.first, ir->getRelationRawPointer(0), rows});
     ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), rows, 1));
     if (ex->variables_bound.count(variables[0]) > 0) {
       if (rows == 0) QueryExecutor::updateBoundDict(&ex->variables_bound, variables[0], 0, 0);
@@ -627,7 +644,8 @@ void SelectQueryJob::prepare(SelectWork& w) {
     if (first > second) throw ReferenceUB("select row count underflows");
     const size_t row = second - first;
     // The reference uploads l2d[first, second) and removes adjacent
-    // duplicates.  first and second are boundaries of runs of equal keys (the
+    // duplicates (src/SelectQueryJob.cu:151-166).  first and second are
+    // boundaries of runs of equal keys (the
     // predicate's range, narrowed by a lower and an upper bound on the key),
     // so the distinct keys are exactly the level-2 index keys of the runs
     // that start in [first, second): a contiguous slice of the level-2 values.
@@ -638,11 +656,11 @@ void SelectQueryJob::prepare(SelectWork& w) {
     if (row > 0 && (ra >= l2o->size() || (*l2o)[ra] != first || rb < ra))
       throw vg::Error(VG_ERR_INVALID, "select range does not start a level-2 run");
     const size_t kept = row > 0 ? rb - ra : 0;
-    auto* ir = new FullRelationIR(ctx, 1, kept);
+    const TYPEID* view[1] = {dl2v + ra};
+    auto* ir = kept ? new FullRelationIR(ctx, 1, kept, view) : new FullRelationIR(ctx, 1, 0);
     ir->setHeader(0, variables[0], false);
     intermediateResult = ir;
     w.ir = ir;
-    if (kept > 0) w.pieces.push_back({dl2v + ra, ir->getRelationRawPointer(0), kept});
     ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), row, 1));
     return;
   }
@@ -650,6 +668,18 @@ void SelectQueryJob::prepare(SelectWork& w) {
   std::vector<std::pair<size_t, size_t>> up;
   std::vector<size_t> offs;
   ex->empty_interval_dict.getUploadRelationData(variables[0], l2d->data(), ds, de, total, up, offs);
+  // one whole interval: the relation views the two index slices
+  if (up.size() == 1 && offs[0] == 0 && up[0].second >= up[0].first && up[0].second - up[0].first == total &&
+      total > 0) {
+    const TYPEID* view[2] = {dl2d + up[0].first, ddata + up[0].first};
+    auto* ir = new FullRelationIR(ctx, 2, total, view);
+    ir->setHeader(0, variables[0], false);
+    ir->setHeader(1, variables[1], false);
+    intermediateResult = ir;
+    w.ir = ir;
+    ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), total, 2));
+    return;
+  }
   auto* ir = new FullRelationIR(ctx, 2, total);
   ir->setHeader(0, variables[0], false);
   ir->setHeader(1, variables[1], false);

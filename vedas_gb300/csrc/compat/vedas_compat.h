@@ -93,6 +93,9 @@ class VedasStorage {
 class FullRelationIR : public IR {
  public:
   FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSize);
+  // A relation whose columns are views of index slices (not copied); see
+  // vg::Rel::borrowed.
+  FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSize, const TYPEID* const* views);
   ~FullRelationIR() override;
   void sort();
   void removeDuplicate();

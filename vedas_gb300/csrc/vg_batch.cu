@@ -432,7 +432,7 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in, int key_b
   VG_CUDA(cudaGetLastError());
   for (uint32_t s = 0; s < S; ++s)
     for (uint32_t c = 0; c < rels[s]->ncols; ++c) {
-      ctx.free(rels[s]->cols[c]);
+      rel_drop_col(ctx, *rels[s], c);
       rels[s]->cols[c] = segs[s].out[c];
     }
   ctx.free(vals);

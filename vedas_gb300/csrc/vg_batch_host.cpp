@@ -32,7 +32,12 @@ double since(Clock::time_point t0) {
 }
 
 // Persistent host workers for the per-query phases of a wave.  run() hands
-// out indices through one atomic counter; the calling thread works too.
+// out indices through one atomic counter; the calling thread works too.  A
+// wave has several parallel phases a few hundred microseconds apart, so
+// idle workers poll for the next phase for a while (kSpin polls) before they
+// sleep on the condition variable, and the caller polls for the workers'
+// completion the same way: a sleeping thread takes tens of microseconds to
+// wake, which would add up over the hundreds of phases of a batch.
 class WorkerPool {
  public:
   static WorkerPool& get() {
@@ -46,32 +51,38 @@ class WorkerPool {
       for (size_t i = 0; i < n; ++i) f(i);
       return;
     }
+    fn_ = &f;
+    n_ = n;
+    next_.store(0, std::memory_order_relaxed);
+    busy_.store(workers_.size(), std::memory_order_relaxed);
     {
       std::lock_guard<std::mutex> lk(mu_);
-      fn_ = &f;
-      n_ = n;
-      next_.store(0);
-      busy_ = workers_.size();
-      ++gen_;
+      gen_.fetch_add(1, std::memory_order_release);
     }
     cv_.notify_all();
     drain(f, n);
-    std::unique_lock<std::mutex> lk(mu_);
-    done_cv_.wait(lk, [&] { return busy_ == 0; });
+    for (int i = 0; i < kSpin && busy_.load(std::memory_order_acquire) != 0; ++i) {
+    }
+    if (busy_.load(std::memory_order_acquire) != 0) {
+      std::unique_lock<std::mutex> lk(mu_);
+      done_cv_.wait(lk, [&] { return busy_.load(std::memory_order_acquire) == 0; });
+    }
     fn_ = nullptr;
   }
 
   ~WorkerPool() {
+    stop_.store(true);
     {
       std::lock_guard<std::mutex> lk(mu_);
-      stop_ = true;
-      ++gen_;
+      gen_.fetch_add(1, std::memory_order_release);
     }
     cv_.notify_all();
     for (auto& t : workers_) t.join();
   }
 
  private:
+  static constexpr int kSpin = 1 << 16;
+
   // VG_HOST_THREADS sets the number of host threads of a parallel phase,
   // the calling thread included (default: the hardware threads, at most 32).
   WorkerPool() {
@@ -91,31 +102,32 @@ class WorkerPool {
   void loop() {
     uint64_t seen = 0;
     while (true) {
-      const std::function<void(size_t)>* f;
-      size_t n;
-      {
+      uint64_t g = gen_.load(std::memory_order_acquire);
+      for (int i = 0; g == seen && i < kSpin; ++i) g = gen_.load(std::memory_order_acquire);
+      if (g == seen) {
         std::unique_lock<std::mutex> lk(mu_);
-        cv_.wait(lk, [&] { return gen_ != seen; });
-        seen = gen_;
-        if (stop_) return;
-        f = fn_;
-        n = n_;
+        cv_.wait(lk, [&] { return gen_.load(std::memory_order_acquire) != seen; });
+        g = gen_.load(std::memory_order_acquire);
       }
-      if (f) drain(*f, n);
-      std::lock_guard<std::mutex> lk(mu_);
-      if (--busy_ == 0) done_cv_.notify_all();
+      seen = g;
+      if (stop_.load()) return;
+      drain(*fn_, n_);
+      if (busy_.fetch_sub(1, std::memory_order_acq_rel) == 1) {
+        std::lock_guard<std::mutex> lk(mu_);
+        done_cv_.notify_all();
+      }
     }
   }
 
   std::vector<std::thread> workers_;
   std::mutex mu_, run_mu_;
   std::condition_variable cv_, done_cv_;
-  const std::function<void(size_t)>* fn_ = nullptr;
+  const std::function<void(size_t)>* fn_ = nullptr;   // published by gen_ (release/acquire)
   size_t n_ = 0;
   std::atomic<size_t> next_{0};
-  size_t busy_ = 0;
-  uint64_t gen_ = 0;
-  bool stop_ = false;
+  std::atomic<size_t> busy_{0};
+  std::atomic<uint64_t> gen_{0};
+  std::atomic<bool> stop_{false};
 };
 
 template <typename F>
@@ -465,6 +477,11 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
       q->plan.reset();  // frees every intermediate relation of the query
     });
     for (PlannedQuery* q : final_) completed.push_back(q);
+    if (host_) {
+      std::vector<BatchQuery*> outs;
+      for (PlannedQuery* q : final_) outs.push_back(q->out);
+      host_->add(outs);
+    }
     final_.clear();
     fin_seg_.clear();
     fin_res_.clear();
@@ -499,7 +516,71 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   prof.device_s += since(t0);
 }
 
-void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts, BatchResult& out) {
+HostResults::~HostResults() {
+  finish();
+  for (Chunk& c : chunks_) ctx_.give_pinned(c.p, c.cap);
+}
+
+void HostResults::retire_stages(bool all) {
+  // a staging block is freed once the main stream is ordered after its copy
+  // (a no-op wait when the copy is already done)
+  std::vector<Pending> keep;
+  for (Pending& p : pending_) {
+    if (!all && cudaEventQuery(p.done) != cudaSuccess) {
+      keep.push_back(p);
+      continue;
+    }
+    VG_CUDA(cudaStreamWaitEvent(ctx_.stream, p.done, 0));
+    ctx_.free(p.stage);
+    cudaEventDestroy(p.done);
+  }
+  pending_.swap(keep);
+}
+
+void HostResults::add(const std::vector<BatchQuery*>& qs) {
+  retire_stages(false);
+  uint64_t words = 0;
+  for (const BatchQuery* q : qs) words += q->rel.nrows * q->rel.ncols;
+  if (words == 0) return;
+  const size_t bytes = words * sizeof(uint32_t);
+  if (chunks_.empty() || chunks_.back().cap - chunks_.back().used < bytes) {
+    size_t got = 0;
+    void* p = ctx_.take_pinned(std::max<size_t>(bytes, size_t{256} << 20), &got);
+    chunks_.push_back({static_cast<char*>(p), got, 0});
+  }
+  Chunk& ch = chunks_.back();
+  uint32_t* host = reinterpret_cast<uint32_t*>(ch.p + ch.used);
+  uint32_t* stage = ctx_.alloc<uint32_t>(words);
+  std::vector<CopyPiece> pieces;
+  uint64_t off = 0;
+  for (BatchQuery* q : qs)
+    for (uint32_t c = 0; c < q->rel.ncols; ++c) {
+      pieces.push_back({q->rel.cols[c], stage + off, q->rel.nrows});
+      q->host[c] = host + off;
+      off += q->rel.nrows;
+    }
+  batched_copy(ctx_, pieces);
+  cudaEvent_t packed, done;
+  VG_CUDA(cudaEventCreateWithFlags(&packed, cudaEventDisableTiming));
+  VG_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+  VG_CUDA(cudaEventRecord(packed, ctx_.stream));
+  cudaStream_t dl = ctx_.dl_stream();
+  VG_CUDA(cudaStreamWaitEvent(dl, packed, 0));
+  VG_CUDA(cudaMemcpyAsync(host, stage, bytes, cudaMemcpyDeviceToHost, dl));
+  VG_CUDA(cudaEventRecord(done, dl));
+  cudaEventDestroy(packed);
+  pending_.push_back({stage, done});
+  ch.used += (bytes + 255) / 256 * 256;
+  bytes_ += bytes;
+}
+
+void HostResults::finish() {
+  if (ctx_.dl_stream_) VG_CUDA(cudaStreamSynchronize(ctx_.dl_stream_));
+  retire_stages(true);
+}
+
+void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts, BatchResult& out,
+               bool to_host) {
   auto t_all = Clock::now();
   out.ctx = &ctx;
   out.queries.clear();
@@ -516,6 +597,11 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   // engine's half-wave, the host runs the other's stages
   const int kb = key_bits_for(storage);
   WaveEngine e0(ctx, kb), e1(ctx, kb);
+  if (to_host) {
+    out.host = std::make_unique<HostResults>(ctx);
+    e0.set_host_results(out.host.get());
+    e1.set_host_results(out.host.get());
+  }
   for (size_t i = 0; i < pq.size(); ++i) (i % 2 ? e1 : e0).add(&pq[i]);
   std::vector<PlannedQuery*> completed;
   while (e0.active() > 0 || e1.active() > 0) {
@@ -529,6 +615,7 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   out.prof.finish_s += e1.prof.finish_s;
   out.prof.final_s += e1.prof.final_s;
   out.prof.plan_s = plan_s;
+  if (out.host) out.host->finish();
   ctx.check_device_errors();
   // parsed queries and executors (bounds, empty intervals, logs) go on the pool
   pfor(pq.size(), [&](size_t i) {

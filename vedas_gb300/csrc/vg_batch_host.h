@@ -17,6 +17,40 @@ struct BatchQuery {
   std::vector<std::string> headers;
   Rel rel;
   std::vector<vedas::ExecuteLogRecord> log;
+  const uint32_t* host[VG_MAX_COLS] = {nullptr};   // page-locked copies (HostResults)
+};
+
+// Page-locked host copies of finished queries' results, made while the batch
+// runs: each time queries finish, one gather packs their columns on the
+// device and one copy on a second stream brings them to host memory, so the
+// transfers overlap the rest of the batch.  Chunks of page-locked memory come
+// from the context's pool and go back to it with the HostResults.
+class HostResults {
+ public:
+  explicit HostResults(Ctx& ctx) : ctx_(ctx) {}
+  ~HostResults();
+  HostResults(const HostResults&) = delete;
+  HostResults& operator=(const HostResults&) = delete;
+  // Enqueues the copies of these queries' result columns.
+  void add(const std::vector<BatchQuery*>& qs);
+  // Waits for every copy.
+  void finish();
+  uint64_t bytes() const { return bytes_; }
+
+ private:
+  struct Chunk {
+    char* p;
+    size_t cap, used;
+  };
+  struct Pending {
+    uint32_t* stage;
+    cudaEvent_t done;
+  };
+  Ctx& ctx_;
+  std::vector<Chunk> chunks_;
+  std::vector<Pending> pending_;
+  uint64_t bytes_ = 0;
+  void retire_stages(bool all);
 };
 
 // Seconds spent in each part of a batched run.
@@ -70,6 +104,8 @@ class WaveEngine {
   }
   // The next stage (A and B alternate).
   void step(std::vector<PlannedQuery*>& completed);
+  // Copies each finished query's result to the host as it finishes.
+  void set_host_results(HostResults* h) { host_ = h; }
   uint32_t waves() const { return waves_; }
   BatchProfile prof;
 
@@ -94,6 +130,7 @@ class WaveEngine {
 
   Ctx& ctx_;
   int key_bits_ = 0;
+  HostResults* host_ = nullptr;
   uint32_t waves_ = 0;
   bool next_is_a_ = true;
   std::vector<PlannedQuery*> active_;   // queries waiting for their next job
@@ -122,6 +159,7 @@ struct BatchResult {
   std::vector<BatchQuery> queries;
   uint32_t waves = 0;
   BatchProfile prof;
+  std::unique_ptr<HostResults> host;   // with run_batch(..., to_host)
   ~BatchResult();
 };
 
@@ -130,7 +168,9 @@ int key_bits_for(vedas::VedasStorage* storage);
 
 // Runs every query to completion together; per-query failures are recorded
 // in their BatchQuery and do not stop the others.
+// With to_host, every result is also copied to page-locked host memory
+// while the batch runs (BatchQuery::host).
 void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts,
-               BatchResult& out);
+               BatchResult& out, bool to_host = false);
 
 }  // namespace vg

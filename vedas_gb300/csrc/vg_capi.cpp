@@ -132,6 +132,8 @@ vg_status vg_ctx_destroy(vg_ctx* ctx) {
   if (!ctx) return VG_OK;
   vg::Ctx& c = ctx->c;
   if (c.stream) cudaStreamSynchronize(c.stream);
+  c.release_dl_stream();
+  c.release_pinned();
   c.release_upload_ring();
   c.arena.release();
   if (c.d_err) cudaFree(c.d_err);
@@ -276,7 +278,9 @@ vg_status vg_select(vg_ctx* ctx, vg_index* ix, const vg_select_desc* d, vg_ir* o
       job.reset(new vedas::SelectQueryJob(&ex, d->kind == 1, v0, d->pred, d->constant));
     job->startJob(0);
     auto* ir = dynamic_cast<vedas::FullRelationIR*>(job->getIR());
-    from_rel(ir->release(), out);
+    vg::Rel r = ir->release();
+    vg::rel_own(ctx->c, r);   // the caller owns (and frees) every column
+    from_rel(r, out);
     if (bu) {
       bu[2] = 0;
       if (d->has_bound && d->kind != 3) {
@@ -375,6 +379,7 @@ vg_status vg_query(vg_ctx* ctx, vg_index* ix, const char* sparql, vg_result** ou
     vedas::FullRelationIR* ir = sr.getResultIR();
     for (size_t c = 0; c < ir->getColumnNum(); ++c) res->headers.push_back(ir->getHeader(c));
     res->rel = ir->release();
+    vg::rel_own(ctx->c, res->rel);   // a result never refers to index memory
     res->ctx = ctx;
     res->log = ex.exe_log;
     ctx->c.check_device_errors();
@@ -457,7 +462,9 @@ vg_status vg_eid_sequence(const uint64_t* quads, uint32_t n, uint64_t out4[4]) {
   });
 }
 
-vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, vg_batch** out) {
+namespace {
+vg_status batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, bool to_host,
+                    vg_batch** out) {
   if (!ctx || !ix || !out || (nq && !queries)) return VG_ERR_INVALID;
   *out = nullptr;
   auto b = std::make_unique<vg_batch>();
@@ -465,10 +472,24 @@ vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, ui
     std::vector<std::string> texts;
     texts.reserve(nq);
     for (uint32_t i = 0; i < nq; ++i) texts.emplace_back(queries[i] ? queries[i] : "");
-    vg::run_batch(ctx->c, ix->st.get(), texts, b->r);
+    vg::run_batch(ctx->c, ix->st.get(), texts, b->r, to_host);
   });
   if (st == VG_OK) *out = b.release();
   return st;
+}
+}  // namespace
+
+vg_status vg_batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, vg_batch** out) {
+  return batch_run(ctx, ix, queries, nq, false, out);
+}
+
+vg_status vg_batch_run_host(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, vg_batch** out) {
+  return batch_run(ctx, ix, queries, nq, true, out);
+}
+
+const uint32_t* vg_batch_host_column(const vg_batch* b, uint32_t q, uint32_t c) {
+  if (!b || !b->r.host || q >= b->r.queries.size() || c >= b->r.queries[q].rel.ncols) return nullptr;
+  return b->r.queries[q].host[c];
 }
 
 uint32_t vg_batch_size(const vg_batch* b) { return b ? static_cast<uint32_t>(b->r.queries.size()) : 0; }

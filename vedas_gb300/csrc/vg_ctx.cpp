@@ -315,6 +315,45 @@ void Ctx::release_upload_ring() {
   event_pool.clear();
 }
 
+void* Ctx::take_pinned(size_t bytes, size_t* got) {
+  size_t best = SIZE_MAX;
+  for (size_t i = 0; i < pinned_free_.size(); ++i)
+    if (pinned_free_[i].second >= bytes && (best == SIZE_MAX || pinned_free_[i].second < pinned_free_[best].second))
+      best = i;
+  if (best != SIZE_MAX) {
+    auto pr = pinned_free_[best];
+    pinned_free_.erase(pinned_free_.begin() + static_cast<long>(best));
+    *got = pr.second;
+    return pr.first;
+  }
+  void* p = nullptr;
+  VG_CUDA(cudaHostAlloc(&p, bytes, cudaHostAllocDefault));
+  *got = bytes;
+  return p;
+}
+
+void Ctx::give_pinned(void* p, size_t bytes) {
+  if (p) pinned_free_.emplace_back(p, bytes);
+}
+
+void Ctx::release_pinned() {
+  for (auto& pr : pinned_free_) cudaFreeHost(pr.first);
+  pinned_free_.clear();
+}
+
+cudaStream_t Ctx::dl_stream() {
+  if (!dl_stream_) VG_CUDA(cudaStreamCreateWithFlags(&dl_stream_, cudaStreamNonBlocking));
+  return dl_stream_;
+}
+
+void Ctx::release_dl_stream() {
+  if (dl_stream_) {
+    cudaStreamSynchronize(dl_stream_);
+    cudaStreamDestroy(dl_stream_);
+  }
+  dl_stream_ = nullptr;
+}
+
 cudaEvent_t Ctx::take_event() {
   if (!event_pool.empty()) {
     cudaEvent_t e = event_pool.back();

@@ -150,6 +150,17 @@ struct Ctx {
   void collect_timing();
   void reset_stats();
 
+  // Page-locked host chunks kept for reuse (pinning memory is slow):
+  // take_pinned returns one of at least `bytes`, give_pinned returns it.
+  void* take_pinned(size_t bytes, size_t* got);
+  void give_pinned(void* p, size_t bytes);
+  void release_pinned();
+  std::vector<std::pair<void*, size_t>> pinned_free_;
+  // A second stream for result downloads (created on first use).
+  cudaStream_t dl_stream();
+  void release_dl_stream();
+  cudaStream_t dl_stream_ = nullptr;
+
   // Copies `bytes` from host memory to device memory `dst` on the stream,
   // through a page-locked ring, so the copy never waits for earlier work
   // (a copy from pageable memory may).  The caller's buffer is free to reuse

@@ -123,14 +123,19 @@ __device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, 
     if (tid == 32) sm.w1 = w1;
   }
   __syncthreads();
+  // R may start at any 4-byte boundary (a view of an index slice): element e
+  // sits on a 16-byte boundary when (e + mis) % 4 == 0, and the window is laid
+  // out in shared memory from `base`, the aligned element at or below w0
+  // (index arithmetic is modulo 2^64, so base may lie below element 0).
+  const uint64_t mis = (reinterpret_cast<uintptr_t>(R) >> 2) & 3u;
   if (tid == 0) {
     const uint64_t w0 = sm.w0, w1 = sm.w1;
     sm.staged = 0;
     sm.failed = 0;
     if (w1 > w0 && w1 - w0 <= kJcWindow) {
-      const uint64_t base = w0 & ~3ull;
-      const uint64_t a0 = (w0 + 3) & ~3ull, a1 = w1 & ~3ull;
-      if ((reinterpret_cast<uintptr_t>(R) & 15) == 0 && a1 > a0) {
+      const uint64_t base = ((w0 + mis) & ~3ull) - mis;
+      const uint64_t a0 = ((w0 + mis + 3) & ~3ull) - mis, a1 = ((w1 + mis) & ~3ull) - mis;
+      if (a1 > a0 && a1 <= w1) {
         mbar_init(&sm.bar, 1);
         const uint32_t bytes = static_cast<uint32_t>((a1 - a0) * 4);
         mbar_arrive_expect_tx(&sm.bar, bytes);
@@ -144,10 +149,10 @@ __device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, 
   __syncthreads();
   const uint64_t w0 = sm.w0, w1 = sm.w1 > sm.w0 ? sm.w1 : sm.w0;
   const uint32_t staged = sm.staged;
-  const uint64_t base = w0 & ~3ull;
+  const uint64_t base = ((w0 + mis) & ~3ull) - mis;
   if (staged) {
-    const uint64_t a0 = (staged == 2) ? ((w0 + 3) & ~3ull) : w1;
-    const uint64_t a1 = (staged == 2) ? (w1 & ~3ull) : w1;
+    const uint64_t a0 = (staged == 2) ? ((w0 + mis + 3) & ~3ull) - mis : w1;
+    const uint64_t a1 = (staged == 2) ? ((w1 + mis) & ~3ull) - mis : w1;
     for (uint64_t e = w0 + tid; e < a0; e += kJcBlock) sm.keys[e - base] = R[e];
     for (uint64_t e = a1 + tid; e < w1; e += kJcBlock) sm.keys[e - base] = R[e];
   }

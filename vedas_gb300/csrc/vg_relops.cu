@@ -273,11 +273,28 @@ Rel rel_alloc(Ctx& ctx, uint32_t ncols, uint64_t nrows) {
 
 void rel_free(Ctx& ctx, Rel& r) {
   for (uint32_t c = 0; c < r.ncols; ++c) {
-    ctx.free(r.cols[c]);
+    if (!(r.borrowed >> c & 1u)) ctx.free(r.cols[c]);
     r.cols[c] = nullptr;
   }
   r.ncols = 0;
   r.nrows = 0;
+  r.borrowed = 0;
+}
+
+void rel_drop_col(Ctx& ctx, Rel& r, uint32_t c) {
+  if (!(r.borrowed >> c & 1u)) ctx.free(r.cols[c]);
+  r.borrowed &= ~(1u << c);
+}
+
+void rel_own(Ctx& ctx, Rel& r) {
+  for (uint32_t c = 0; c < r.ncols; ++c) {
+    if (!(r.borrowed >> c & 1u)) continue;
+    uint32_t* o = ctx.alloc<uint32_t>(r.nrows);
+    if (r.nrows)
+      VG_CUDA(cudaMemcpyAsync(o, r.cols[c], r.nrows * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx.stream));
+    r.cols[c] = o;
+  }
+  r.borrowed = 0;
 }
 
 void multi_copy(Ctx& ctx, const CopyPiece* pieces, int np) {
@@ -440,6 +457,17 @@ void sort_by_first(Ctx& ctx, Rel& r) {
   const uint64_t n = r.nrows;
   if (n <= 1 || r.ncols == 0) return;
   if (n > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "relation sorts are limited to 2^32 rows");
+  if (r.borrowed & 1u) {
+    // the sort uses column 0 as its key buffer: take a copy of a view
+    Rel k0;
+    k0.ncols = 1;
+    k0.nrows = n;
+    k0.cols[0] = r.cols[0];
+    k0.borrowed = 1;
+    rel_own(ctx, k0);
+    r.cols[0] = k0.cols[0];
+    r.borrowed &= ~1u;
+  }
   uint32_t* keys_alt = ctx.alloc<uint32_t>(n);
   if (r.ncols == 1) {
     const bool alt = radix_sort_u32(ctx, r.cols[0], keys_alt, nullptr, nullptr, n, 32, false);
@@ -467,7 +495,7 @@ void sort_by_first(Ctx& ctx, Rel& r) {
     const uint32_t* in[1] = {r.cols[c]};
     uint32_t* out[1] = {nc};
     gather_cols(ctx, in, out, 1, perm, n);
-    ctx.free(r.cols[c]);
+    rel_drop_col(ctx, r, c);
     r.cols[c] = nc;
   }
   ctx.free(perm);
@@ -495,7 +523,7 @@ void sort_rows(Ctx& ctx, Rel& r) {
     const uint32_t* in[1] = {r.cols[c]};
     uint32_t* out[1] = {nc};
     gather_cols(ctx, in, out, 1, perm, n);
-    ctx.free(r.cols[c]);
+    rel_drop_col(ctx, r, c);
     r.cols[c] = nc;
   }
   ctx.free(perm);

@@ -7,14 +7,24 @@
 namespace vg {
 
 // A device relation: ncols uint32 columns of nrows rows (column-major).
+// Bit c of `borrowed` marks column c as a view into memory the relation does
+// not own (a slice of an index array): it is never freed or written through
+// the relation, and it may start at any 4-byte boundary.
 struct Rel {
   uint32_t ncols = 0;
   uint64_t nrows = 0;
   uint32_t* cols[VG_MAX_COLS] = {nullptr};
+  uint32_t borrowed = 0;
 };
 
 Rel rel_alloc(Ctx& ctx, uint32_t ncols, uint64_t nrows);
+// Frees the owned columns.
 void rel_free(Ctx& ctx, Rel& r);
+// Frees column c if the relation owns it, and marks the slot owned (the
+// caller stores an owned column there or drops it).
+void rel_drop_col(Ctx& ctx, Rel& r, uint32_t c);
+// Replaces every borrowed column by an owned copy (stream-ordered).
+void rel_own(Ctx& ctx, Rel& r);
 
 // One contiguous copy src[0, len) -> dst[0, len).
 struct CopyPiece {
