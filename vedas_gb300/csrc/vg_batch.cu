@@ -188,58 +188,47 @@ struct JoinSeg {
   uint64_t row0;   // offset of this join's left rows in the lo/cnt/offs arrays
 };
 
-// One block per tile of kJcTile left keys of one join (block -> join by the
-// per-join tile prefix); the right-key window is staged by a bulk copy.
-__global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_kernel(const JoinSeg* __restrict__ js,
-                                                               const uint64_t* __restrict__ bstart, uint32_t J,
-                                                               uint32_t* __restrict__ lo, uint32_t* __restrict__ cnt,
-                                                               DeviceErrors* err) {
+// One block per tile of kJcTile left keys of one join, tiles taken in ticket
+// order.  The tile's match counts stay in registers (the right-key window is
+// staged by a bulk copy when it fits); their block scan and a segmented
+// decoupled look-back over the join's earlier tiles give every left key its
+// output offset directly, and the join's last tile writes its total.
+__global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
+    const JoinSeg* __restrict__ js, const uint64_t* __restrict__ bstart, uint32_t J, uint32_t* __restrict__ lo,
+    uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket, uint64_t* __restrict__ totals,
+    DeviceErrors* err) {
   __shared__ JoinCountSmem sm;
-  __shared__ uint32_t s_j;
-  if (threadIdx.x == 0) s_j = seg_of(bstart, J, blockIdx.x);
-  __syncthreads();
-  const JoinSeg g = js[s_j];
-  const uint64_t i0 = (blockIdx.x - bstart[s_j]) * static_cast<uint64_t>(kJcTile);
-  join_count_tile(g.lk, g.nl, g.rk, g.nr, i0, lo + g.row0, cnt + g.row0, sm, err);
-}
-
-__global__ void __launch_bounds__(kBlock) bjoin_scan_kernel(const JoinSeg* __restrict__ js,
-                                                            const uint64_t* __restrict__ tstart, uint32_t J,
-                                                            const uint32_t* __restrict__ cnt,
-                                                            uint64_t* __restrict__ offs, uint64_t* status,
-                                                            uint32_t* ticket, uint64_t* totals, DeviceErrors* err) {
-  __shared__ uint64_t s_scan[kBlock / 32 + 1];
+  __shared__ uint64_t s_scan[kJcBlock / 32 + 1];
   __shared__ uint64_t s_b;
   __shared__ uint32_t s_tile, s_j;
   if (threadIdx.x == 0) {
     s_tile = atomicAdd(ticket, 1u);
-    s_j = seg_of(tstart, J, s_tile);
+    s_j = seg_of(bstart, J, s_tile);
   }
   __syncthreads();
   const uint64_t tile = s_tile;
   const uint32_t j = s_j;
   const JoinSeg g = js[j];
-  const uint64_t r0 = (tile - tstart[j]) * kTileRows + threadIdx.x * kRows;
-  uint32_t v[kRows];
+  const uint64_t i0 = (tile - bstart[j]) * static_cast<uint64_t>(kJcTile);
+  uint32_t cnt[kJcKeys];
+  join_count_tile_regs(g.lk, g.nl, g.rk, g.nr, i0, lo + g.row0, cnt, sm, err);
   uint64_t sum = 0;
 #pragma unroll
-  for (int i = 0; i < kRows; ++i) {
-    v[i] = (r0 + i < g.nl) ? cnt[g.row0 + r0 + i] : 0u;
-    sum += v[i];
-  }
+  for (int k = 0; k < kJcKeys; ++k) sum += cnt[k];
   uint64_t tot;
-  const uint64_t e = block_excl_scan64<kBlock>(sum, tot, s_scan);
+  const uint64_t e = block_excl_scan64<kJcBlock>(sum, tot, s_scan);
   if (threadIdx.x < 32) {
-    const uint64_t p = warp_lookback_seg(status, tile, tstart[j], tot, err);
+    const uint64_t p = warp_lookback_seg(status, tile, bstart[j], tot, err);
     if (threadIdx.x == 0) s_b = p;
   }
   __syncthreads();
-  if (tile == tstart[j + 1] - 1 && threadIdx.x == 0) totals[j] = s_b + tot;
+  if (tile == bstart[j + 1] - 1 && threadIdx.x == 0) totals[j] = s_b + tot;
   uint64_t run = s_b + e;
+  const uint64_t first = i0 + static_cast<uint64_t>(threadIdx.x) * kJcKeys;
 #pragma unroll
-  for (int i = 0; i < kRows; ++i) {
-    if (r0 + i < g.nl) offs[g.row0 + r0 + i] = run;
-    run += v[i];
+  for (int k = 0; k < kJcKeys; ++k) {
+    if (first + k < g.nl) offs[g.row0 + first + k] = run;
+    run += cnt[k];
   }
 }
 
@@ -253,28 +242,69 @@ struct JoinOut {
   uint32_t nlc, nrc;
 };
 
+// Output rows [kb, kb + kTileRows) of one join per block.  Output row k comes
+// from the left row i with offs[i] <= k < offs[i + 1] and the right row
+// lo[i] + (k - offs[i]).  Two warps find the tile's left-row range at once;
+// when it holds at most kTileRows + 1 rows, its offsets and lower bounds are
+// staged in shared memory, and each thread walks its rows (k increasing)
+// from the previous one's left row.  Hub keys thus spread over many blocks.
 __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __restrict__ jo,
                                                              const uint64_t* __restrict__ ostart, uint32_t J) {
+  constexpr int kStage = kTileRows + 1;
   __shared__ JoinOut s_o;
+  __shared__ uint64_t s_off[kStage];
+  __shared__ uint32_t s_lo[kStage];
   __shared__ uint64_t s_i[2];
-  __shared__ uint64_t s_kb;
-  if (threadIdx.x == 0) {
-    const uint32_t j = seg_of(ostart, J, blockIdx.x);
-    s_o = jo[j];
-    const uint64_t kb = (blockIdx.x - ostart[j]) * kTileRows;
-    s_kb = kb;
-    const uint64_t klast = (kb + kTileRows < s_o.total ? kb + kTileRows : s_o.total) - 1;
-    const uint64_t f = upper_bound_dev(s_o.offs, 0, s_o.nl, kb) - 1;
-    s_i[0] = f;
-    s_i[1] = upper_bound_dev(s_o.offs, f, s_o.nl, klast);
+  __shared__ uint32_t s_j;
+  if (threadIdx.x == 0) s_j = seg_of(ostart, J, blockIdx.x);
+  __syncthreads();
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&jo[s_j]);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&s_o);
+    for (uint32_t w = threadIdx.x; w < sizeof(JoinOut) / 4; w += kBlock) dst[w] = src[w];
   }
   __syncthreads();
-  const uint64_t ib = s_i[0], ie = s_i[1], kb = s_kb;
+  const uint64_t kb = (blockIdx.x - ostart[s_j]) * static_cast<uint64_t>(kTileRows);
+  const uint64_t kend = (kb + kTileRows < s_o.total) ? kb + kTileRows : s_o.total;
+  if (threadIdx.x < 32) {
+    const uint64_t f = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kb) - 1;
+    if (threadIdx.x == 0) s_i[0] = f;
+  } else if (threadIdx.x < 64) {
+    const uint64_t e = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kend - 1);
+    if (threadIdx.x == 32) s_i[1] = e;
+  }
+  __syncthreads();
+  const uint64_t ib = s_i[0], ie = s_i[1];
+  const uint64_t m = ie - ib;
+  const bool staged = m <= static_cast<uint64_t>(kStage);
+  if (staged)
+    for (uint32_t e = threadIdx.x; e < m; e += kBlock) {
+      s_off[e] = s_o.offs[ib + e];
+      s_lo[e] = s_o.lo[ib + e];
+    }
+  __syncthreads();
+  uint32_t p = 0;   // staged: the current left row, relative to ib
   for (int it = 0; it < kRows; ++it) {
     const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
-    if (k >= s_o.total) break;
-    const uint64_t i = upper_bound_dev(s_o.offs, ib, ie, k) - 1;
-    const uint64_t jj = s_o.lo[i] + (k - s_o.offs[i]);
+    if (k >= kend) break;
+    uint64_t i, jj;
+    if (staged) {
+      // last p with s_off[p] <= k, moving forward from the previous row's p
+      uint32_t step = 1;
+      while (p + step < m && s_off[p + step] <= k) {
+        p += step;
+        step <<= 1;
+      }
+      while (step > 1) {
+        step >>= 1;
+        if (p + step < m && s_off[p + step] <= k) p += step;
+      }
+      i = ib + p;
+      jj = s_lo[p] + (k - s_off[p]);
+    } else {
+      i = upper_bound_dev(s_o.offs, ib, ie, k) - 1;
+      jj = s_o.lo[i] + (k - s_o.offs[i]);
+    }
     uint32_t c = 0;
     for (uint32_t x = 0; x < s_o.nlc; ++x) s_o.oc[c++][k] = s_o.lc[x][i];
     for (uint32_t x = 0; x < s_o.nrc; ++x) s_o.oc[c++][k] = s_o.rc[x][jj];
@@ -374,7 +404,7 @@ void note_unique_writes(Ctx& ctx, const std::vector<SegRows>& segs, const uint64
 std::vector<uint64_t> batched_unique(Ctx& ctx, const std::vector<SegRows>& segs) {
   std::vector<uint64_t> counts(segs.size(), 0);
   if (segs.empty()) return counts;
-  PinnedWords h;
+  PinnedWords h(ctx);
   batched_unique_enqueue(ctx, segs, h.reserve(segs.size()));
   ctx.sync();
   std::copy(h.data(), h.data() + segs.size(), counts.begin());
@@ -451,7 +481,7 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
   jb.r = r;
   if (J == 0) return;
   std::vector<JoinSeg> js(J);
-  std::vector<uint64_t> bstart(J + 1, 0), tstart(J + 1, 0);
+  std::vector<uint64_t> bstart(J + 1, 0);
   uint64_t rows = 0;
   double cbytes = 0;
   jb.row0.resize(J);
@@ -464,39 +494,29 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
     jb.row0[j] = rows;
     rows += l[j]->nrows;
     bstart[j + 1] = bstart[j] + div_up(l[j]->nrows, kJcTile);
-    tstart[j + 1] = tstart[j] + div_up(l[j]->nrows, kTileRows);
     cbytes += 4.0 * (l[j]->nrows + r[j]->nrows);
   }
   JoinSeg* djs = upload(ctx, js);
   uint64_t* dbs = upload(ctx, bstart);
-  uint64_t* dts = upload(ctx, tstart);
   jb.lo = ctx.alloc<uint32_t>(rows);
-  uint32_t* cnt = ctx.alloc<uint32_t>(rows);
   jb.offs = ctx.alloc<uint64_t>(rows);
-  uint64_t* status = ctx.alloc<uint64_t>(tstart[J]);
+  uint64_t* status = ctx.alloc<uint64_t>(bstart[J]);
   uint64_t* totals = ctx.alloc<uint64_t>(J);
   uint32_t* ticket = ctx.alloc<uint32_t>(1);
-  VG_CUDA(cudaMemsetAsync(status, 0, tstart[J] * sizeof(uint64_t), ctx.stream));
+  VG_CUDA(cudaMemsetAsync(status, 0, bstart[J] * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), ctx.stream));
-  ctx.launch("join_count", cbytes, [&] {
-    bjoin_count_kernel<<<static_cast<unsigned>(bstart[J]), kJcBlock, 0, ctx.stream>>>(djs, dbs, J, jb.lo, cnt,
-                                                                                    ctx.d_err);
-  });
-  VG_CUDA(cudaGetLastError());
-  ctx.launch("join_scan", 12.0 * rows, [&] {
-    bjoin_scan_kernel<<<static_cast<unsigned>(tstart[J]), kBlock, 0, ctx.stream>>>(djs, dts, J, cnt, jb.offs, status,
-                                                                                 ticket, totals, ctx.d_err);
+  ctx.launch("join_count_scan", cbytes + 12.0 * rows, [&] {
+    bjoin_count_scan_kernel<<<static_cast<unsigned>(bstart[J]), kJcBlock, 0, ctx.stream>>>(
+        djs, dbs, J, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaMemcpyAsync(totals_host, totals, J * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
-  // the stream orders every later use of these blocks after the kernels above
-  ctx.free(cnt);
+  // the stream orders every later use of these blocks after the kernel above
   ctx.free(status);
   ctx.free(totals);
   ctx.free(ticket);
   ctx.free(djs);
   ctx.free(dbs);
-  ctx.free(dts);
 }
 
 void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::vector<Rel>& out,
@@ -557,7 +577,7 @@ void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<
   out.assign(J, Rel());
   first_last.assign(2 * J, 0);
   if (J == 0) return;
-  PinnedWords tot, fl;
+  PinnedWords tot(ctx), fl(ctx);
   JoinBatch jb;
   batched_join_count(ctx, l, r, jb, tot.reserve(J));
   ctx.sync();
@@ -599,7 +619,7 @@ void batched_col0(Ctx& ctx, const std::vector<const Rel*>& rels, std::vector<std
   out.assign(R, {});
   const uint64_t total = col0_words(rels);
   if (R == 0 || total == 0) return;
-  PinnedWords h;
+  PinnedWords h(ctx);
   uint32_t* p = reinterpret_cast<uint32_t*>(h.reserve((total + 1) / 2));
   batched_col0_enqueue(ctx, rels, p);
   ctx.sync();
@@ -610,19 +630,13 @@ void batched_col0(Ctx& ctx, const std::vector<const Rel*>& rels, std::vector<std
   }
 }
 
-PinnedWords::~PinnedWords() {
-  if (p_) cudaFreeHost(p_);
-}
+PinnedWords::~PinnedWords() { ctx_.give_pinned(p_, cap_); }
 
 uint64_t* PinnedWords::reserve(size_t words) {
-  if (words <= cap_ && p_) return p_;
-  size_t cap = cap_ ? cap_ : 4096;
-  while (cap < words) cap *= 2;
-  if (p_) VG_CUDA(cudaFreeHost(p_));
-  p_ = nullptr;
-  cap_ = 0;
-  VG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&p_), cap * sizeof(uint64_t), cudaHostAllocDefault));
-  cap_ = cap;
+  const size_t bytes = std::max<size_t>(words, 1) * sizeof(uint64_t);
+  if (p_ && bytes <= cap_) return p_;
+  ctx_.give_pinned(p_, cap_);
+  p_ = static_cast<uint64_t*>(ctx_.take_pinned(std::max<size_t>(bytes, size_t{1} << 16), &cap_));
   return p_;
 }
 

@@ -13,21 +13,23 @@
 
 namespace vg {
 
-// Page-locked host words for device->host reads of one pipeline stage.
+// Page-locked host words for device->host reads of one pipeline stage,
+// taken from and returned to the context's pool of page-locked chunks.
 class PinnedWords {
  public:
-  PinnedWords() = default;
+  explicit PinnedWords(Ctx& ctx) : ctx_(ctx) {}
   PinnedWords(const PinnedWords&) = delete;
   PinnedWords& operator=(const PinnedWords&) = delete;
   ~PinnedWords();
-  // At least `words` 64-bit words; may reallocate, so only call it while no
-  // copy into the buffer is pending.
+  // At least `words` 64-bit words; may switch buffers, so only call it while
+  // no copy into the buffer is pending.
   uint64_t* reserve(size_t words);
   uint64_t* data() const { return p_; }
 
  private:
+  Ctx& ctx_;
   uint64_t* p_ = nullptr;
-  size_t cap_ = 0;
+  size_t cap_ = 0;   // bytes
 };
 
 // All pieces in one launch (any number of pieces).

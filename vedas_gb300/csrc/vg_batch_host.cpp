@@ -214,6 +214,7 @@ WaveEngine::WaveEngine(Ctx& ctx, int key_bits) : ctx_(ctx), key_bits_(key_bits) 
 }
 
 WaveEngine::~WaveEngine() {
+  bury();
   if (a_pending_ || b_pending_) cudaStreamSynchronize(ctx_.stream);
   for (auto& r : jouts_) rel_free(ctx_, r);
   if (ev_a_) cudaEventDestroy(ev_a_);
@@ -222,9 +223,15 @@ WaveEngine::~WaveEngine() {
 
 void WaveEngine::add(PlannedQuery* pq) { active_.push_back(pq); }
 
+void WaveEngine::bury() {
+  pfor(graveyard_.size(), [&](size_t k) { graveyard_[k].reset(); });
+  graveyard_.clear();
+}
+
 void WaveEngine::reset() {
   cudaStreamSynchronize(ctx_.stream);
   a_pending_ = b_pending_ = false;
+  bury();
   for (auto& r : jouts_) rel_free(ctx_, r);
   jouts_.clear();
   jb_ = JoinBatch();
@@ -311,9 +318,16 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
 
   auto t0 = Clock::now();
   items_.assign(run_.size(), Item());
-  if (!run_.empty()) {
-    ++waves_;
-    pfor(run_.size(), [&](size_t k) {
+  const size_t nrun = run_.size(), ndead = graveyard_.size();
+  if (nrun > 0) ++waves_;
+  if (nrun + ndead > 0) {
+    // one parallel phase prepares the next jobs and destroys the plans of
+    // the queries handed back in the last stage B
+    pfor(nrun + ndead, [&](size_t k) {
+      if (k >= nrun) {
+        graveyard_[k - nrun].reset();
+        return;
+      }
       PlannedQuery* q = run_[k];
       vedas::QueryJob* job = q->plan->getJob(q->next);
       Item& it = items_[k];
@@ -335,6 +349,7 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
       });
       if (q->out->status != VG_OK) it.kind = Item::kNone;
     });
+    graveyard_.clear();
   }
   prof.prepare_s += since(t0);
 
@@ -474,8 +489,10 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
       }
       out->rel = o;
       if (q->ex) out->log = std::move(q->ex->exe_log);
-      q->plan.reset();  // frees every intermediate relation of the query
     });
+    // the plans (jobs, intermediate relations, host state) of finished
+    // queries are destroyed in the next stage A's parallel phase
+    for (PlannedQuery* q : final_) graveyard_.push_back(std::move(q->plan));
     for (PlannedQuery* q : final_) completed.push_back(q);
     if (host_) {
       std::vector<BatchQuery*> outs;
@@ -617,7 +634,10 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   out.prof.plan_s = plan_s;
   if (out.host) out.host->finish();
   ctx.check_device_errors();
-  // parsed queries and executors (bounds, empty intervals, logs) go on the pool
+  // plans first (their jobs point at the executors), then parsed queries and
+  // executors (bounds, empty intervals, logs) on the pool
+  e0.bury();
+  e1.bury();
   pfor(pq.size(), [&](size_t i) {
     pq[i].plan.reset();
     pq[i].ex.reset();

@@ -106,6 +106,8 @@ class WaveEngine {
   void step(std::vector<PlannedQuery*>& completed);
   // Copies each finished query's result to the host as it finishes.
   void set_host_results(HostResults* h) { host_ = h; }
+  // Destroys the plans of handed-back queries that are still pending.
+  void bury();
   uint32_t waves() const { return waves_; }
   BatchProfile prof;
 
@@ -144,10 +146,11 @@ class WaveEngine {
   std::vector<Rel> jouts_;
   // queries whose last job finished: compacted in stage A, handed back in stage B
   std::vector<PlannedQuery*> final_;
+  std::vector<std::unique_ptr<vedas::QueryPlan>> graveyard_;   // destroyed in the next stage A
   std::vector<SegRows> fin_seg_;
   std::vector<vedas::FullRelationIR*> fin_res_;
   // device -> host results of each stage and the events that mark them
-  PinnedWords h_a_, h_b_;
+  PinnedWords h_a_{ctx_}, h_b_{ctx_};
   size_t off_tot_ = 0, off_fin_ = 0, off_c0_ = 0;   // words into h_a_
   size_t off_fl_ = 0, off_jc0_ = 0;                               // words into h_b_
   cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;

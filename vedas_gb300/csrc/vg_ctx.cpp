@@ -316,10 +316,13 @@ void Ctx::release_upload_ring() {
 }
 
 void* Ctx::take_pinned(size_t bytes, size_t* got) {
+  // best fit among chunks no more than four times the request, so small
+  // buffers do not tie up the large result chunks
   size_t best = SIZE_MAX;
-  for (size_t i = 0; i < pinned_free_.size(); ++i)
-    if (pinned_free_[i].second >= bytes && (best == SIZE_MAX || pinned_free_[i].second < pinned_free_[best].second))
-      best = i;
+  for (size_t i = 0; i < pinned_free_.size(); ++i) {
+    const size_t sz = pinned_free_[i].second;
+    if (sz >= bytes && sz / 4 <= bytes && (best == SIZE_MAX || sz < pinned_free_[best].second)) best = i;
+  }
   if (best != SIZE_MAX) {
     auto pr = pinned_free_[best];
     pinned_free_.erase(pinned_free_.begin() + static_cast<long>(best));

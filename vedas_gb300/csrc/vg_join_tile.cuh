@@ -19,24 +19,50 @@ struct JoinCountSmem {
   uint32_t failed;
 };
 
-__device__ __forceinline__ uint64_t smem_lower(const uint32_t* keys, uint64_t base, uint64_t lo, uint64_t hi,
-                                               uint32_t key) {
-  while (lo < hi) {
-    const uint64_t mid = (lo + hi) >> 1;
-    if (keys[mid - base] < key) lo = mid + 1;
-    else hi = mid;
+// Searches over the staged window, in 32-bit offsets from its first key
+// (s points at it in shared memory, n keys).  kUpper: first offset whose key
+// is above `key`; otherwise first offset whose key is not below it.
+template <bool kUpper>
+__device__ __forceinline__ bool smem_below(const uint32_t* s, uint32_t i, uint32_t key) {
+  const uint32_t a = s[i];
+  return kUpper ? (a <= key) : (a < key);
+}
+
+// Binary search over [lo, n).
+template <bool kUpper>
+__device__ __forceinline__ uint32_t smem_search(const uint32_t* s, uint32_t lo, uint32_t n, uint32_t key) {
+  uint32_t len = n - lo;
+  while (len > 0) {
+    const uint32_t half = len >> 1;
+    if (smem_below<kUpper>(s, lo + half, key)) {
+      lo += half + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
   }
   return lo;
 }
 
-__device__ __forceinline__ uint64_t smem_upper(const uint32_t* keys, uint64_t base, uint64_t lo, uint64_t hi,
-                                               uint32_t key) {
-  while (lo < hi) {
-    const uint64_t mid = (lo + hi) >> 1;
-    if (key < keys[mid - base]) hi = mid;
-    else lo = mid + 1;
+// The same answer at or after `from`, galloping from there (steps 1, 2, 4,
+// ... then a binary search inside the last step): a thread's left keys are
+// consecutive, so the next bound is usually a few keys further on.
+template <bool kUpper>
+__device__ __forceinline__ uint32_t smem_gallop(const uint32_t* s, uint32_t from, uint32_t n, uint32_t key) {
+  if (from >= n || !smem_below<kUpper>(s, from, key)) return from;
+  uint32_t lo = from, step = 1, hi = n;
+  while (true) {
+    const uint32_t nx = lo + step;
+    if (nx >= n) break;
+    if (!smem_below<kUpper>(s, nx, key)) {
+      hi = nx;
+      break;
+    }
+    lo = nx;
+    step <<= 1;
   }
-  return lo;
+  // below(lo) holds and the answer lies in (lo, hi]
+  return smem_search<kUpper>(s, lo + 1, hi, key);
 }
 
 // First index in R[lo, hi) whose key is not below `key` (kUpper: above it),
@@ -44,16 +70,15 @@ __device__ __forceinline__ uint64_t smem_upper(const uint32_t* keys, uint64_t ba
 // ballot of their comparisons narrows the range 32-fold, so a search over
 // 10^8 keys takes six rounds of parallel loads instead of 27 dependent ones.
 // Every lane of the warp must call it with the same arguments.
-template <bool kUpper>
-__device__ __forceinline__ uint64_t warp_bound(const uint32_t* __restrict__ R, uint64_t lo, uint64_t hi,
-                                               uint32_t key) {
+template <bool kUpper, typename T>
+__device__ __forceinline__ uint64_t warp_bound(const T* __restrict__ R, uint64_t lo, uint64_t hi, T key) {
   const uint32_t lane = threadIdx.x & 31;
   while (hi - lo > 32) {
     const uint64_t step = (hi - lo + 31) >> 5;
     const uint64_t p = lo + static_cast<uint64_t>(lane + 1) * step;
     bool below = false;
     if (lane < 31 && p < hi) {
-      const uint32_t a = __ldg(R + p);
+      const T a = __ldg(R + p);
       below = kUpper ? (a <= key) : (a < key);
     }
     const uint32_t c = __popc(__ballot_sync(0xffffffffu, below));
@@ -64,7 +89,7 @@ __device__ __forceinline__ uint64_t warp_bound(const uint32_t* __restrict__ R, u
   }
   bool below = false;
   if (lo + lane < hi) {
-    const uint32_t a = __ldg(R + lo + lane);
+    const T a = __ldg(R + lo + lane);
     below = kUpper ? (a <= key) : (a < key);
   }
   return lo + __popc(__ballot_sync(0xffffffffu, below));
@@ -109,17 +134,22 @@ __device__ __forceinline__ void lockstep_bounds(const uint32_t* __restrict__ R, 
 // an mbarrier, its ragged ends by plain loads.  A window that does not fit (a
 // heavy key, or a right side much larger than the left) is searched in global
 // memory with lockstep bounds instead.
-__device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, uint64_t nl,
-                                                const uint32_t* __restrict__ R, uint64_t nr, uint64_t i0,
-                                                uint32_t* __restrict__ lo_out, uint32_t* __restrict__ cnt_out,
-                                                JoinCountSmem& sm, DeviceErrors* err) {
+// The tile's counts stay in registers: thread t holds the counts of left
+// keys i0 + 8t .. i0 + 8t + 7 in cnt[] (zero past the end); lower bounds go
+// to lo_out.  Every thread of the block must call it.
+__device__ __forceinline__ void join_count_tile_regs(const uint32_t* __restrict__ L, uint64_t nl,
+                                                     const uint32_t* __restrict__ R, uint64_t nr, uint64_t i0,
+                                                     uint32_t* __restrict__ lo_out, uint32_t (&cnt)[kJcKeys],
+                                                     JoinCountSmem& sm, DeviceErrors* err) {
+#pragma unroll
+  for (int j = 0; j < kJcKeys; ++j) cnt[j] = 0;
   const uint32_t tid = threadIdx.x;
   const uint64_t i_end = (i0 + kJcTile < nl) ? i0 + kJcTile : nl;
   if (tid < 32) {
-    const uint64_t w0 = warp_bound<false>(R, 0, nr, L[i0]);
+    const uint64_t w0 = warp_bound<false, uint32_t>(R, 0, nr, L[i0]);
     if (tid == 0) sm.w0 = w0;
   } else if (tid < 64) {
-    const uint64_t w1 = warp_bound<true>(R, 0, nr, L[i_end - 1]);
+    const uint64_t w1 = warp_bound<true, uint32_t>(R, 0, nr, L[i_end - 1]);
     if (tid == 32) sm.w1 = w1;
   }
   __syncthreads();
@@ -166,7 +196,7 @@ __device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, 
   __syncthreads();
   const bool use_smem = staged != 0 && sm.failed == 0;
   const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
-  if (first >= i_end) return;
+  if (first >= i_end) return;   // counts stay zero
 
   if (!use_smem) {
     uint32_t key[kJcKeys];
@@ -182,23 +212,51 @@ __device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, 
       const uint64_t i = first + j;
       if (i < i_end) {
         lo_out[i] = static_cast<uint32_t>(lo[j]);
-        cnt_out[i] = static_cast<uint32_t>(hi[j] - lo[j]);
+        cnt[j] = static_cast<uint32_t>(hi[j] - lo[j]);
       }
     }
     return;
   }
-  uint64_t prev = w0;
+  // staged window: the thread's first key is searched in full, the others
+  // gallop from the previous key's upper bound; equal keys reuse its bounds
+  const uint32_t* win = sm.keys + (w0 - base);
+  const uint32_t n = static_cast<uint32_t>(w1 - w0);
+  uint32_t plo = 0, phi = 0, pkey = 0;
 #pragma unroll
   for (int j = 0; j < kJcKeys; ++j) {
     const uint64_t i = first + j;
-    if (i >= i_end) break;
-    const uint32_t key = L[i];
-    const uint64_t lo = smem_lower(sm.keys, base, prev, w1, key);
-    const uint64_t hi = smem_upper(sm.keys, base, lo, w1, key);
-    prev = lo;
-    lo_out[i] = static_cast<uint32_t>(lo);
-    cnt_out[i] = static_cast<uint32_t>(hi - lo);
+    if (i < i_end) {
+      const uint32_t key = L[i];
+      uint32_t lo, hi;
+      if (j > 0 && key == pkey) {
+        lo = plo;
+        hi = phi;
+      } else {
+        lo = (j == 0) ? smem_search<false>(win, 0, n, key) : smem_gallop<false>(win, phi, n, key);
+        hi = smem_gallop<true>(win, lo, n, key);
+      }
+      lo_out[i] = static_cast<uint32_t>(w0 + lo);
+      cnt[j] = hi - lo;
+      plo = lo;
+      phi = hi;
+      pkey = key;
+    }
   }
+}
+
+// Lower bound and match count of every left key of the tile, to lo_out and
+// cnt_out.
+__device__ __forceinline__ void join_count_tile(const uint32_t* __restrict__ L, uint64_t nl,
+                                                const uint32_t* __restrict__ R, uint64_t nr, uint64_t i0,
+                                                uint32_t* __restrict__ lo_out, uint32_t* __restrict__ cnt_out,
+                                                JoinCountSmem& sm, DeviceErrors* err) {
+  uint32_t cnt[kJcKeys];
+  join_count_tile_regs(L, nl, R, nr, i0, lo_out, cnt, sm, err);
+  const uint64_t first = i0 + static_cast<uint64_t>(threadIdx.x) * kJcKeys;
+  const uint64_t i_end = (i0 + kJcTile < nl) ? i0 + kJcTile : nl;
+#pragma unroll
+  for (int j = 0; j < kJcKeys; ++j)
+    if (first + j < i_end) cnt_out[first + j] = cnt[j];
 }
 
 }  // namespace vg

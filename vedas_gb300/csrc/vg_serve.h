@@ -181,6 +181,7 @@ class Server {
       std::vector<PlannedQuery*> completed;
       try {
         eng_.wave(completed);
+        if (eng_.active() == 0) eng_.bury();   // idle: free finished queries' intermediates now
       } catch (const Error& e) {
         // a device-level failure ends every query in flight with its status
         std::lock_guard<std::mutex> lk(mu_);
