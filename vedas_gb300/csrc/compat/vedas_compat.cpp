@@ -19,6 +19,7 @@ VedasStorage::VedasStorage(vg::Ctx* ctx, const TYPEID* s, const TYPEID* p, const
                            bool inputs_on_device, bool fullIndex) {
   if (inputs_on_device) {
     vg::build_index(*ctx, s, p, o, n, fullIndex, ix_);
+    cacheDevice();
     return;
   }
   vg::Scratch<uint32_t> ds(*ctx, n), dp(*ctx, n), dobj(*ctx, n);
@@ -28,16 +29,30 @@ VedasStorage::VedasStorage(vg::Ctx* ctx, const TYPEID* s, const TYPEID* p, const
     VG_CUDA(cudaMemcpyAsync(dobj.get(), o, n * 4, cudaMemcpyHostToDevice, ctx->stream));
   }
   vg::build_index(*ctx, ds.get(), dp.get(), dobj.get(), n, fullIndex, ix_);
+  cacheDevice();
   ctx->sync();
 }
 
 VedasStorage::VedasStorage(vg::Ctx* ctx, const char* fname, bool fullIndex) {
   vg::open_vds(*ctx, fname, fullIndex, ix_);
+  cacheDevice();
+}
+
+void VedasStorage::cacheDevice() {
+  for (int m = 0; m < kMirrors; ++m) d_[m] = ix_.get(kMirrorName[m]).ptr;
 }
 
 VedasStorage::~VedasStorage() { ix_.release(); }
 
 void VedasStorage::write(const char* fname) { vg::write_vds(ix_, fname); }
+
+const char* const VedasStorage::kMirrorName[VedasStorage::kMirrors] = {
+    "p_idx_values", "p_idx_offsets", "ps_s_idx_values", "ps_idx_offsets", "po_o_idx_values", "po_idx_offsets",
+    "ps_data",      "po_data",       "pso_data",        "pos_data",       "sop_data"};
+
+void VedasStorage::prepareMirrors() {
+  for (int m = 0; m < kMirrors; ++m) h(static_cast<Mirror>(m));
+}
 
 // ---------------------------------------------------------------------------
 // FullRelationIR (src/FullRelationIR.cu)
@@ -600,7 +615,7 @@ void SelectQueryJob::prepare(SelectWork& w) {
     TYPEID_HOST_VEC* l2v = subj ? st->getPredicateObjectIndexValues() : st->getPredicateSubjectIndexValues();
     TYPEID_HOST_VEC* l2o = subj ? st->getPredicateObjectIndexOffsets() : st->getPredicateSubjectIndexOffsets();
     TYPEID_HOST_VEC* data = subj ? st->getPOSdata() : st->getPSOdata();
-    const TYPEID* ddata = st->dev(subj ? "pos_data" : "pso_data");
+    const TYPEID* ddata = subj ? st->devPOSdata() : st->devPSOdata();
     auto r1 = QueryExecutor::findL2OffsetFromL1(l1v, l1o, dataid[0], data->size());
     auto r2 = QueryExecutor::findDataOffsetFromL2(l2v, l2o, static_cast<TYPEID>(r1.first),
                                                   static_cast<TYPEID>(r1.second), dataid[1]);
@@ -623,8 +638,8 @@ void SelectQueryJob::prepare(SelectWork& w) {
   }
   // two variables: level-2 data ps_data (PSO) or po_data (POS)
   TYPEID_HOST_VEC* l2d = pos_index ? st->getPOdata() : st->getPSdata();
-  const TYPEID* dl2d = st->dev(pos_index ? "po_data" : "ps_data");
-  const TYPEID* ddata = st->dev(pos_index ? "pos_data" : "pso_data");
+  const TYPEID* dl2d = pos_index ? st->devPOdata() : st->devPSdata();
+  const TYPEID* ddata = pos_index ? st->devPOSdata() : st->devPSOdata();
   auto r1 = QueryExecutor::findL2OffsetFromL1(l1v, l1o, dataid[0], st->getTripleSize());
   const size_t b0 = r1.first, e0 = r1.second;
   if (e0 == 0 || b0 >= l2d->size() || e0 > l2d->size())
@@ -650,7 +665,7 @@ void SelectQueryJob::prepare(SelectWork& w) {
     // so the distinct keys are exactly the level-2 index keys of the runs
     // that start in [first, second): a contiguous slice of the level-2 values.
     TYPEID_HOST_VEC* l2o = pos_index ? st->getPredicateObjectIndexOffsets() : st->getPredicateSubjectIndexOffsets();
-    const TYPEID* dl2v = st->dev(pos_index ? "po_o_idx_values" : "ps_s_idx_values");
+    const TYPEID* dl2v = pos_index ? st->devPOIdxValues() : st->devPSIdxValues();
     const size_t ra = static_cast<size_t>(std::lower_bound(l2o->begin(), l2o->end(), first) - l2o->begin());
     const size_t rb = static_cast<size_t>(std::lower_bound(l2o->begin(), l2o->end(), second) - l2o->begin());
     if (row > 0 && (ra >= l2o->size() || (*l2o)[ra] != first || rb < ra))

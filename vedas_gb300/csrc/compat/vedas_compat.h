@@ -66,27 +66,42 @@ class VedasStorage {
   size_t getTripleSize() const { return ix_.n; }
   bool isFullIndex() const { return ix_.full; }
   // Host mirrors (the reference's getters return host vectors).
-  TYPEID_HOST_VEC* getPredicateIndexValues() { return h("p_idx_values"); }
-  TYPEID_HOST_VEC* getPredicateIndexOffsets() { return h("p_idx_offsets"); }
-  TYPEID_HOST_VEC* getPredicateSubjectIndexValues() { return h("ps_s_idx_values"); }
-  TYPEID_HOST_VEC* getPredicateSubjectIndexOffsets() { return h("ps_idx_offsets"); }
-  TYPEID_HOST_VEC* getPredicateObjectIndexValues() { return h("po_o_idx_values"); }
-  TYPEID_HOST_VEC* getPredicateObjectIndexOffsets() { return h("po_idx_offsets"); }
-  TYPEID_HOST_VEC* getPSdata() { return h("ps_data"); }
-  TYPEID_HOST_VEC* getPOdata() { return h("po_data"); }
-  TYPEID_HOST_VEC* getPSOdata() { return h("pso_data"); }
-  TYPEID_HOST_VEC* getPOSdata() { return h("pos_data"); }
-  TYPEID_HOST_VEC* getSOPdata() { return h("sop_data"); }
+  TYPEID_HOST_VEC* getPredicateIndexValues() { return h(kPIdxV); }
+  TYPEID_HOST_VEC* getPredicateIndexOffsets() { return h(kPIdxO); }
+  TYPEID_HOST_VEC* getPredicateSubjectIndexValues() { return h(kPSIdxV); }
+  TYPEID_HOST_VEC* getPredicateSubjectIndexOffsets() { return h(kPSIdxO); }
+  TYPEID_HOST_VEC* getPredicateObjectIndexValues() { return h(kPOIdxV); }
+  TYPEID_HOST_VEC* getPredicateObjectIndexOffsets() { return h(kPOIdxO); }
+  TYPEID_HOST_VEC* getPSdata() { return h(kPS); }
+  TYPEID_HOST_VEC* getPOdata() { return h(kPO); }
+  TYPEID_HOST_VEC* getPSOdata() { return h(kPSO); }
+  TYPEID_HOST_VEC* getPOSdata() { return h(kPOS); }
+  TYPEID_HOST_VEC* getSOPdata() { return h(kSOP); }
+  // Makes every host mirror above (downloading on first use); after it the
+  // getters may be called from many threads at once.
+  void prepareMirrors();
   // Device copies (resident).
   const TYPEID* dev(const char* name) const { return ix_.get(name).ptr; }
+  const TYPEID* devPSdata() const { return d_[kPS]; }
+  const TYPEID* devPOdata() const { return d_[kPO]; }
+  const TYPEID* devPSOdata() const { return d_[kPSO]; }
+  const TYPEID* devPOSdata() const { return d_[kPOS]; }
+  const TYPEID* devPSIdxValues() const { return d_[kPSIdxV]; }
+  const TYPEID* devPOIdxValues() const { return d_[kPOIdxV]; }
   uint64_t len(const char* name) const { return ix_.get(name).len; }
   vg::Index& index() { return ix_; }
   void write(const char* fname);
 
  private:
+  enum Mirror { kPIdxV, kPIdxO, kPSIdxV, kPSIdxO, kPOIdxV, kPOIdxO, kPS, kPO, kPSO, kPOS, kSOP, kMirrors };
+  static const char* const kMirrorName[kMirrors];
   vg::Index ix_;
-  TYPEID_HOST_VEC* h(const char* name) {
-    return const_cast<TYPEID_HOST_VEC*>(&ix_.host_array(name));
+  TYPEID_HOST_VEC* mirror_[kMirrors] = {};
+  const TYPEID* d_[kMirrors] = {};
+  void cacheDevice();   // the device arrays' addresses (set at construction)
+  TYPEID_HOST_VEC* h(Mirror m) {
+    if (!mirror_[m]) mirror_[m] = const_cast<TYPEID_HOST_VEC*>(&ix_.host_array(kMirrorName[m]));
+    return mirror_[m];
   }
 };
 

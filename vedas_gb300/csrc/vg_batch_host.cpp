@@ -172,18 +172,7 @@ uint64_t estimate_bytes(vedas::VedasStorage* st, vedas::SparqlQuery& sq) {
 
 }  // namespace
 
-void prepare_mirrors(vedas::VedasStorage* storage) {
-  storage->getPredicateIndexValues();
-  storage->getPredicateIndexOffsets();
-  storage->getPredicateSubjectIndexValues();
-  storage->getPredicateSubjectIndexOffsets();
-  storage->getPredicateObjectIndexValues();
-  storage->getPredicateObjectIndexOffsets();
-  storage->getPSdata();
-  storage->getPOdata();
-  storage->getPSOdata();
-  storage->getPOSdata();
-}
+void prepare_mirrors(vedas::VedasStorage* storage) { storage->prepareMirrors(); }
 
 void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text, PlannedQuery& pq) {
   guarded(pq.out, [&] {
@@ -193,6 +182,7 @@ void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text,
     pq.plan = std::make_unique<vedas::QueryPlan>(sel);
     pq.ex->plan(*pq.sq, *pq.plan);
     pq.plan->beginExecution();
+    pq.ex->exe_log.reserve(2 * pq.plan->jobNum() + 2);
     pq.est_bytes = estimate_bytes(storage, *pq.sq);
   });
 }
