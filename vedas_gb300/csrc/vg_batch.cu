@@ -398,7 +398,7 @@ void batched_unique_enqueue(Ctx& ctx, const std::vector<SegRows>& segs, uint64_t
 void note_unique_writes(Ctx& ctx, const std::vector<SegRows>& segs, const uint64_t* counts) {
   double wb = 0;
   for (size_t s = 0; s < segs.size(); ++s) wb += 4.0 * counts[s] * segs[s].ncols;
-  ctx.kstats["unique_compact"].bytes += wb;
+  ctx.add_bytes("unique_compact", wb);
 }
 
 std::vector<uint64_t> batched_unique(Ctx& ctx, const std::vector<SegRows>& segs) {

@@ -15,6 +15,7 @@
 #include <atomic>
 #include <condition_variable>
 #include <cstdlib>
+#include <exception>
 #include <functional>
 #include <mutex>
 #include <thread>
@@ -199,9 +200,23 @@ BatchResult::~BatchResult() {
 }
 
 WaveEngine::WaveEngine(Ctx& ctx, int key_bits) : ctx_(ctx), key_bits_(key_bits) {
-  VG_CUDA(cudaEventCreateWithFlags(&ev_a_, cudaEventDisableTiming));
-  VG_CUDA(cudaEventCreateWithFlags(&ev_b_, cudaEventDisableTiming));
+  VG_CUDA(cudaEventCreateWithFlags(&ev_a_, cudaEventDisableTiming | cudaEventBlockingSync));
+  VG_CUDA(cudaEventCreateWithFlags(&ev_b_, cudaEventDisableTiming | cudaEventBlockingSync));
 }
+
+namespace {
+// Waits for a stage's event: polls briefly (most stages are nearly done
+// when asked), then sleeps in the driver so that a waiting engine thread
+// leaves its core to the host workers.
+void wait_event(cudaEvent_t ev) {
+  for (int i = 0; i < 100; ++i) {
+    const cudaError_t e = cudaEventQuery(ev);
+    if (e == cudaSuccess) return;
+    if (e != cudaErrorNotReady) VG_CUDA(e);
+  }
+  VG_CUDA(cudaEventSynchronize(ev));
+}
+}  // namespace
 
 WaveEngine::~WaveEngine() {
   bury();
@@ -292,7 +307,7 @@ void WaveEngine::finish_wave() {
 void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
   if (b_pending_) {
     auto t0 = Clock::now();
-    VG_CUDA(cudaEventSynchronize(ev_b_));
+    wait_event(ev_b_);
     b_pending_ = false;
     prof.device_s += since(t0);
   }
@@ -440,7 +455,7 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
 void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   if (!a_pending_) return;
   auto t0 = Clock::now();
-  VG_CUDA(cudaEventSynchronize(ev_a_));
+  wait_event(ev_a_);
   a_pending_ = false;
   prof.device_s += since(t0);
   const uint64_t* ha = h_a_.data();
@@ -545,6 +560,7 @@ void HostResults::retire_stages(bool all) {
 }
 
 void HostResults::add(const std::vector<BatchQuery*>& qs) {
+  std::lock_guard<std::mutex> lk(mu_);
   retire_stages(false);
   uint64_t words = 0;
   for (const BatchQuery* q : qs) words += q->rel.nrows * q->rel.ncols;
@@ -582,6 +598,7 @@ void HostResults::add(const std::vector<BatchQuery*>& qs) {
 }
 
 void HostResults::finish() {
+  std::lock_guard<std::mutex> lk(mu_);
   if (ctx_.dl_stream_) VG_CUDA(cudaStreamSynchronize(ctx_.dl_stream_));
   retire_stages(true);
 }
@@ -610,11 +627,26 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
     e1.set_host_results(out.host.get());
   }
   for (size_t i = 0; i < pq.size(); ++i) (i % 2 ? e1 : e0).add(&pq[i]);
-  std::vector<PlannedQuery*> completed;
-  while (e0.active() > 0 || e1.active() > 0) {
-    if (e0.active() > 0) e0.step(completed);
-    if (e1.active() > 0) e1.step(completed);
+  // each engine on its own host thread: one waits for the device while the
+  // other runs its host stages (parallel phases share the worker pool)
+  std::vector<PlannedQuery*> done0, done1;
+  std::exception_ptr err1;
+  std::thread t1([&] {
+    try {
+      while (e1.active() > 0) e1.step(done1);
+    } catch (...) {
+      err1 = std::current_exception();
+    }
+  });
+  std::exception_ptr err0;
+  try {
+    while (e0.active() > 0) e0.step(done0);
+  } catch (...) {
+    err0 = std::current_exception();
   }
+  t1.join();
+  if (err0) std::rethrow_exception(err0);
+  if (err1) std::rethrow_exception(err1);
   out.waves = std::max(e0.waves(), e1.waves());
   out.prof = e0.prof;
   out.prof.prepare_s += e1.prof.prepare_s;

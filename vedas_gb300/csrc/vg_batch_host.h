@@ -2,6 +2,7 @@
 
 #include <chrono>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -47,6 +48,7 @@ class HostResults {
     cudaEvent_t done;
   };
   Ctx& ctx_;
+  std::mutex mu_;   // add() is called by both engines of a batch
   std::vector<Chunk> chunks_;
   std::vector<Pending> pending_;
   uint64_t bytes_ = 0;
@@ -81,9 +83,9 @@ void prepare_mirrors(vedas::VedasStorage* storage);
 //     finished);
 //  B: wait for that half, hand finished queries back, allocate the join
 //     outputs and enqueue the join writes.
-// Nothing else waits on the device.  Two engines on one stream that take
-// turns (A of one, then A of the other, then B of each) keep the device busy
-// with one engine's work while the host runs the other's stages.
+// Nothing else waits on the device.  Two engines on one stream, each driven
+// by its own host thread, keep the device busy with one engine's work while
+// the host runs the other's stages.
 class WaveEngine {
  public:
   // key_bits bounds every relation value (< 2^key_bits), so the segmented

@@ -262,6 +262,7 @@ size_t Arena::largest_free() const {
 }
 
 void Ctx::upload_bytes(void* dst, const void* src, size_t bytes) {
+  std::lock_guard<std::recursive_mutex> lk(host_mu);
   if (bytes == 0) return;
   constexpr size_t kRingMin = size_t{16} << 20;
   const size_t need = (bytes + 255) / 256 * 256;
@@ -316,6 +317,7 @@ void Ctx::release_upload_ring() {
 }
 
 void* Ctx::take_pinned(size_t bytes, size_t* got) {
+  std::lock_guard<std::recursive_mutex> lk(host_mu);
   // best fit among chunks no more than four times the request, so small
   // buffers do not tie up the large result chunks
   size_t best = SIZE_MAX;
@@ -336,6 +338,7 @@ void* Ctx::take_pinned(size_t bytes, size_t* got) {
 }
 
 void Ctx::give_pinned(void* p, size_t bytes) {
+  std::lock_guard<std::recursive_mutex> lk(host_mu);
   if (p) pinned_free_.emplace_back(p, bytes);
 }
 
@@ -345,6 +348,7 @@ void Ctx::release_pinned() {
 }
 
 cudaStream_t Ctx::dl_stream() {
+  std::lock_guard<std::recursive_mutex> lk(host_mu);
   if (!dl_stream_) VG_CUDA(cudaStreamCreateWithFlags(&dl_stream_, cudaStreamNonBlocking));
   return dl_stream_;
 }
@@ -358,6 +362,7 @@ void Ctx::release_dl_stream() {
 }
 
 cudaEvent_t Ctx::take_event() {
+  std::lock_guard<std::recursive_mutex> lk(host_mu);
   if (!event_pool.empty()) {
     cudaEvent_t e = event_pool.back();
     event_pool.pop_back();
@@ -369,6 +374,7 @@ cudaEvent_t Ctx::take_event() {
 }
 
 void Ctx::collect_timing() {
+  std::lock_guard<std::recursive_mutex> lk(host_mu);
   sync();
   for (auto& kv : kstats) {
     for (auto& pr : kv.second.pending) {
@@ -383,6 +389,7 @@ void Ctx::collect_timing() {
 }
 
 void Ctx::reset_stats() {
+  std::lock_guard<std::recursive_mutex> lk(host_mu);
   collect_timing();
   launches = 0;
   kstats.clear();

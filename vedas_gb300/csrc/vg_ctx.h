@@ -128,9 +128,16 @@ struct Ctx {
   std::map<std::string, KernelStat> kstats;
   std::vector<cudaEvent_t> event_pool;
 
+  // Guards the host-side state below (statistics, event pool, upload ring,
+  // page-locked pool, download stream) when two threads issue work on the
+  // context's stream at once (the two engines of a batch).  Recursive: a
+  // launch may upload.
+  std::recursive_mutex host_mu;
+
   // Wraps one kernel launch on `stream`.
   template <typename F>
   void launch(const char* name, double algo_bytes, F&& f) {
+    std::lock_guard<std::recursive_mutex> lk(host_mu);
     ++launches;
     KernelStat& k = kstats[name];
     k.launches++;
@@ -154,6 +161,11 @@ struct Ctx {
   // take_pinned returns one of at least `bytes`, give_pinned returns it.
   void* take_pinned(size_t bytes, size_t* got);
   void give_pinned(void* p, size_t bytes);
+  // Adds algorithmic bytes to a kernel's statistics.
+  void add_bytes(const char* name, double bytes) {
+    std::lock_guard<std::recursive_mutex> lk(host_mu);
+    kstats[name].bytes += bytes;
+  }
   void release_pinned();
   std::vector<std::pair<void*, size_t>> pinned_free_;
   // A second stream for result downloads (created on first use).

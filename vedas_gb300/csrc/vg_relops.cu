@@ -344,7 +344,7 @@ uint64_t unique_rows(Ctx& ctx, const uint32_t* const* in, uint32_t* const* out, 
   VG_CUDA(cudaMemcpyAsync(ctx.h_small, count.get(), sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.sync();
   const uint64_t kept = ctx.h_small[0];
-  ctx.kstats["unique_compact"].bytes += 4.0 * kept * ncols;
+  ctx.add_bytes("unique_compact", 4.0 * kept * ncols);
   return kept;
 }
 

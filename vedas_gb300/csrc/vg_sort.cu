@@ -168,12 +168,13 @@ template <typename K, bool HAS_V, bool IOTA>
 void launch_pass(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint64_t n,
                  uint32_t shift, const uint64_t* bases, uint64_t* status, uint32_t* ticket) {
   const size_t smem = kTile * sizeof(K) + (HAS_V ? kTile * sizeof(uint32_t) : 0);
-  static bool attr_set = false;
-  if (!attr_set) {
-    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    attr_set = true;
-  }
+  // once per instantiation (thread-safe static initialisation)
+  static const bool attr_set = [smem] {
+    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)));
+    return true;
+  }();
+  (void)attr_set;
   const uint64_t tiles = div_up(n, kTile);
   const double bytes = static_cast<double>(n) * (2 * sizeof(K) + (HAS_V ? (IOTA ? 4 : 8) : 0));
   ctx.launch("radix_onesweep", bytes, [&] {
