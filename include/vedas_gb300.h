@@ -281,6 +281,9 @@ vg_status vg_serve_start(vg_ctx* ctx, vg_index* ix, size_t budget_bytes, vg_serv
 /* Queues one query; `ticket` identifies it.  A query whose estimate alone
  * exceeds the budget finishes at once with VG_ERR_REJECTED. */
 vg_status vg_serve_submit(vg_server* s, const char* sparql, uint64_t* ticket);
+/* Submits n queries at once (planned in parallel, queued in order);
+ * tickets[i] is the ticket of sparql[i]. */
+vg_status vg_serve_submit_many(vg_server* s, const char* const* sparql, uint32_t n, uint64_t* tickets);
 /* Waits up to timeout_s seconds (< 0: forever); *done = 1 when finished. */
 vg_status vg_serve_wait(vg_server* s, uint64_t ticket, double timeout_s, int* done);
 /* The finished query's own status, and its result (as for vg_result_*). */

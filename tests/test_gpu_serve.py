@@ -33,7 +33,15 @@ def test_results_alone_equal_results_in_the_mix(ctx):
             tickets[i] = srv.submit(qs[i])
             time.sleep(0.0005)          # staggered arrivals: queries join waves in flight
 
-    th = [threading.Thread(target=client, args=(list(range(k, len(qs), 4)),)) for k in range(4)]
+    def client_many(part):
+        for c in range(0, len(part), 7):   # groups planned in parallel by submit_many
+            chunk = part[c:c + 7]
+            for i, t in zip(chunk, srv.submit_many([qs[i] for i in chunk])):
+                tickets[i] = t
+            time.sleep(0.001)
+
+    th = [threading.Thread(target=client, args=(list(range(k, len(qs), 4)),)) for k in range(3)]
+    th.append(threading.Thread(target=client_many, args=(list(range(3, len(qs), 4)),)))
     for t in th:
         t.start()
     for t in th:

@@ -113,6 +113,7 @@ def lib():
             "vg_batch_free": (i32, [vp]),
             "vg_serve_start": (i32, [vp, vp, ctypes.c_size_t, ctypes.POINTER(vp)]),
             "vg_serve_submit": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64)]),
+            "vg_serve_submit_many": (i32, [vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(ctypes.c_uint64)]),
             "vg_serve_wait": (i32, [vp, u64, ctypes.c_double, ctypes.POINTER(i32)]),
             "vg_serve_query_status": (i32, [vp, u64]),
             "vg_serve_ncols": (u32, [vp, u64]),
@@ -409,6 +410,16 @@ class Server:
         t = ctypes.c_uint64()
         check(lib().vg_serve_submit(self.h, sparql.encode(), ctypes.byref(t)))
         return t.value
+
+    def submit_many(self, queries) -> list:
+        """Submits many queries at once (planned in parallel); their tickets."""
+        n = len(queries)
+        if n == 0:
+            return []
+        arr = (ctypes.c_char_p * n)(*[q if isinstance(q, bytes) else q.encode() for q in queries])
+        out = (ctypes.c_uint64 * n)()
+        check(lib().vg_serve_submit_many(self.h, arr, n, out))
+        return list(out)
 
     def wait(self, ticket: int, timeout_s: float = -1.0) -> bool:
         done = ctypes.c_int()

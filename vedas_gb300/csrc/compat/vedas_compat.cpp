@@ -627,7 +627,8 @@ void SelectQueryJob::prepare(SelectWork& w) {
     ir->setHeader(0, variables[0], false);
     intermediateResult = ir;
     w.ir = ir;
-    ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), rows, 1));
+    ex->exe_log.push_back(
+        ExecuteLogRecord(gpuId, UPLOAD_OP, ex->log_text ? ir->getHeaders("") : std::string(), rows, 1));
     if (ex->variables_bound.count(variables[0]) > 0) {
       if (rows == 0) QueryExecutor::updateBoundDict(&ex->variables_bound, variables[0], 0, 0);
       else
@@ -676,7 +677,8 @@ void SelectQueryJob::prepare(SelectWork& w) {
     ir->setHeader(0, variables[0], false);
     intermediateResult = ir;
     w.ir = ir;
-    ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), row, 1));
+    ex->exe_log.push_back(
+        ExecuteLogRecord(gpuId, UPLOAD_OP, ex->log_text ? ir->getHeaders("") : std::string(), row, 1));
     return;
   }
   size_t total = 0;
@@ -692,7 +694,8 @@ void SelectQueryJob::prepare(SelectWork& w) {
     ir->setHeader(1, variables[1], false);
     intermediateResult = ir;
     w.ir = ir;
-    ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), total, 2));
+    ex->exe_log.push_back(
+        ExecuteLogRecord(gpuId, UPLOAD_OP, ex->log_text ? ir->getHeaders("") : std::string(), total, 2));
     return;
   }
   auto* ir = new FullRelationIR(ctx, 2, total);
@@ -700,7 +703,8 @@ void SelectQueryJob::prepare(SelectWork& w) {
   ir->setHeader(1, variables[1], false);
   intermediateResult = ir;
   w.ir = ir;
-  ex->exe_log.push_back(ExecuteLogRecord(gpuId, UPLOAD_OP, ir->getHeaders(""), total, 2));
+  ex->exe_log.push_back(
+      ExecuteLogRecord(gpuId, UPLOAD_OP, ex->log_text ? ir->getHeaders("") : std::string(), total, 2));
   for (size_t i = 0; i < up.size(); ++i) {
     if (up[i].second < up[i].first) throw ReferenceUB("negative upload interval");
     const size_t len = up[i].second - up[i].first;
@@ -768,7 +772,9 @@ void JoinQueryJob::finish(JoinWork& w, vg::Rel& joined, TYPEID first, TYPEID las
   setHeaders(w, out);
   intermediateResult = out;
   const size_t result_size = out->size();
-  ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP, w.lir->getHeaders("") + " x " + w.rir->getHeaders(""),
+  ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP,
+                                         ex->log_text ? w.lir->getHeaders("") + " x " + w.rir->getHeaders("")
+                                                      : std::string(),
                                          w.lir->size(), w.rir->size(), result_size));
   if (QueryExecutor::ENABLE_UPDATE_BOUND_AFTER_JOIN) {
     if (result_size > 0) {
@@ -846,7 +852,9 @@ void JoinQueryJob::prepare(JoinWork& w) {
     auto* out = new FullRelationIR(ex->ctx, new_col_num, 0);
     setHeaders(w, out);
     intermediateResult = out;
-    ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP, lir->getHeaders("") + " x " + rir->getHeaders(""),
+    ex->exe_log.push_back(ExecuteLogRecord(gpuId, JOIN_OP,
+                                           ex->log_text ? lir->getHeaders("") + " x " + rir->getHeaders("")
+                                                        : std::string(),
                                            lir->size(), rir->size(), 0));
   }
 }
@@ -882,7 +890,9 @@ FullRelationIR* IndexSwapJob::prepare() {
 void IndexSwapJob::finish(const std::vector<TYPEID>* col0) {
   auto* ir = dynamic_cast<FullRelationIR*>(intermediateResult);
   ex->exe_log.push_back(ExecuteLogRecord(gpuId, SWAP_OP,
-                                         ir->getHeader(0) + " <-> " + ir->getHeader(swapped_col), ir->size(),
+                                         ex->log_text ? ir->getHeader(0) + " <-> " + ir->getHeader(swapped_col)
+                                                      : std::string(),
+                                         ir->size(),
                                          ir->getColumnNum()));
   if (ir->size() > 2 && ir->size() < 100) {
     if (!col0 || col0->size() != ir->size()) throw vg::Error(VG_ERR_INVALID, "swap: column 0 not staged");
@@ -1003,8 +1013,8 @@ void QueryGraph::mergeEdge(const std::string end1, const std::string end2) {
 std::tuple<size_t, size_t, std::string> QueryGraph::sameMaxDegAndTotalCard(
     std::vector<std::pair<std::string, GraphEdge*>>& links) {
   std::unordered_map<std::string, size_t> varCount, varEstCard;
-  for (auto node : links) {
-    for (auto var : node.second->vars) {
+  for (const auto& node : links) {
+    for (const auto& var : node.second->vars) {
       if (varCount.count(var)) {
         varCount[var] += 1;
         varEstCard[var] += node.second->estimateCardinality;
@@ -1016,7 +1026,7 @@ std::tuple<size_t, size_t, std::string> QueryGraph::sameMaxDegAndTotalCard(
   }
   size_t maxDeg = 0, maxDegMinCard = 0;
   std::string bestVar;
-  for (auto v : varCount) {
+  for (const auto& v : varCount) {
     const size_t est = varEstCard[v.first];
     if (v.second > maxDeg || (v.second == maxDeg && est < maxDegMinCard)) {
       maxDeg = v.second;
@@ -1030,7 +1040,7 @@ std::tuple<size_t, size_t, std::string> QueryGraph::sameMaxDegAndTotalCard(
 std::pair<std::string, std::string> QueryGraph::findBestStarNode() {
   std::string bestNode, bestVar;
   size_t maxDegree = 0, maxDegCardSum = 0;
-  for (auto node : adjacencyList) {
+  for (auto& node : adjacencyList) {
     auto t = sameMaxDegAndTotalCard(node.second);
     const size_t degree = std::get<0>(t), est = std::get<1>(t);
     if (degree > maxDegree || (degree == maxDegree && est < maxDegCardSum)) {
@@ -1090,7 +1100,7 @@ PlanTreeNode* QueryGraph::generateJoinPlanForNode(const std::string& vertex, con
       if (e1->estimateCardinality < 1000 && e2->estimateCardinality < 1000) sigma = 0.001;
       else if (e1->estimateCardinality < 1000 || e2->estimateCardinality < 1000) sigma = 0.0001;
       e1->estimateCardinality *= std::ceil(e2->estimateCardinality * sigma);
-      for (auto v : e2->vars) e1->vars.insert(v);
+      for (const auto& v : e2->vars) e1->vars.insert(v);
     }
   }
   for (int i = static_cast<int>(adj.size()) - 1; i > static_cast<int>(first); --i) {

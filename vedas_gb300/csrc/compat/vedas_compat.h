@@ -416,6 +416,9 @@ class QueryExecutor {
 
   // Execution log of the current query (QueryExecutor::exe_log).
   std::vector<ExecuteLogRecord> exe_log;
+  // Whether log records carry the reference's text (relation headers); the
+  // batched engine turns it off, its logs are read as numbers only.
+  bool log_text = true;
   static bool ENABLE_UPDATE_BOUND_AFTER_JOIN;
 
   VedasStorage* storage;

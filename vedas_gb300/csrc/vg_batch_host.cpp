@@ -47,11 +47,11 @@ class WorkerPool {
   }
 
   void run(size_t n, const std::function<void(size_t)>& f) {
-    std::lock_guard<std::mutex> serial(run_mu_);  // one parallel loop at a time
-    if (n < 64 || workers_.empty()) {
+    if (n < 64 || workers_.empty()) {   // small loops run on the caller alone
       for (size_t i = 0; i < n; ++i) f(i);
       return;
     }
+    std::lock_guard<std::mutex> serial(run_mu_);  // one parallel loop at a time
     fn_ = &f;
     n_ = n;
     next_.store(0, std::memory_order_relaxed);
@@ -184,6 +184,7 @@ void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text,
     pq.ex->plan(*pq.sq, *pq.plan);
     pq.plan->beginExecution();
     pq.ex->exe_log.reserve(2 * pq.plan->jobNum() + 2);
+    pq.ex->log_text = false;   // batch logs are read as numbers (vg_batch_log)
     pq.est_bytes = estimate_bytes(storage, *pq.sq);
   });
 }
@@ -667,6 +668,8 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   });
   out.prof.total_s = since(t_all);
 }
+
+void parallel_for(size_t n, const std::function<void(size_t)>& f) { WorkerPool::get().run(n, f); }
 
 int key_bits_for(vedas::VedasStorage* storage) {
   const uint32_t m = storage->index().max_id;

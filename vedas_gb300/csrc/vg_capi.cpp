@@ -596,6 +596,11 @@ vg_status vg_serve_submit(vg_server* s, const char* sparql, uint64_t* ticket) {
   return guard([&] { *ticket = s->srv->submit(sparql); });
 }
 
+vg_status vg_serve_submit_many(vg_server* s, const char* const* sparql, uint32_t n, uint64_t* tickets) {
+  if (!s || (n && (!sparql || !tickets))) return VG_ERR_INVALID;
+  return guard([&] { s->srv->submit_many(sparql, n, tickets); });
+}
+
 vg_status vg_serve_wait(vg_server* s, uint64_t ticket, double timeout_s, int* done) {
   if (!s || !done) return VG_ERR_INVALID;
   return guard([&] { *done = s->srv->wait(ticket, timeout_s) ? 1 : 0; });

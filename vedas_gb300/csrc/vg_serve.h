@@ -55,27 +55,41 @@ class Server {
   }
 
   uint64_t submit(const char* text) {
-    auto it = std::make_unique<ServeItem>();
-    it->t_submit = Clock::now();
-    it->pq.out = &it->q;
-    plan_query(ctx_, st_, text, it->pq);  // host only, on the caller's thread
+    uint64_t t = 0;
+    submit_many(&text, 1, &t);
+    return t;
+  }
+
+  // Plans n queries (host only; on the worker pool when there are many,
+  // otherwise on the caller's thread) and queues them in order.
+  void submit_many(const char* const* texts, size_t n, uint64_t* tickets) {
+    std::vector<std::unique_ptr<ServeItem>> its(n);
+    const auto now = Clock::now();
+    for (size_t i = 0; i < n; ++i) {
+      its[i] = std::make_unique<ServeItem>();
+      its[i]->t_submit = now;
+      its[i]->pq.out = &its[i]->q;
+    }
+    parallel_for(n, [&](size_t i) { plan_query(ctx_, st_, texts[i] ? texts[i] : "", its[i]->pq); });
     std::lock_guard<std::mutex> lk(mu_);
-    it->ticket = ++next_ticket_;
-    ++submitted_;
-    ServeItem* raw = it.get();
-    items_[raw->ticket] = std::move(it);
-    if (raw->q.status == VG_OK && raw->pq.est_bytes > budget_) {
-      raw->q.status = VG_ERR_REJECTED;
-      raw->q.error = "estimated relation bytes exceed the serving budget";
+    for (size_t i = 0; i < n; ++i) {
+      ServeItem* raw = its[i].get();
+      raw->ticket = ++next_ticket_;
+      tickets[i] = raw->ticket;
+      ++submitted_;
+      items_[raw->ticket] = std::move(its[i]);
+      if (raw->q.status == VG_OK && raw->pq.est_bytes > budget_) {
+        raw->q.status = VG_ERR_REJECTED;
+        raw->q.error = "estimated relation bytes exceed the serving budget";
+      }
+      if (raw->q.status != VG_OK) {
+        finish_locked(raw);
+        ++rejected_;
+      } else {
+        queue_.push_back(raw);
+      }
     }
-    if (raw->q.status != VG_OK) {
-      finish_locked(raw);
-      ++rejected_;
-    } else {
-      queue_.push_back(raw);
-      cv_work_.notify_all();
-    }
-    return raw->ticket;
+    cv_work_.notify_all();
   }
 
   bool wait(uint64_t ticket, double timeout_s) {
