@@ -7,6 +7,7 @@
 #include <cstring>
 
 #include "vg_join_tile.cuh"
+#include "vg_pool.h"
 #include "vg_prims.cuh"
 #include "vg_sort.h"
 
@@ -446,25 +447,26 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in, int key_b
   ctx.free(keys_alt);
   std::vector<SegRows> segs(S);
   double bytes = 4.0 * N;
-  for (uint32_t s = 0; s < S; ++s) {
+  for (uint32_t s = 0; s < S; ++s) bytes += 8.0 * rels[s]->nrows * rels[s]->ncols;
+  parallel_for(S, [&](size_t s) {
     segs[s].ncols = rels[s]->ncols;
     segs[s].n = rels[s]->nrows;
     for (uint32_t c = 0; c < rels[s]->ncols; ++c) {
       segs[s].in[c] = rels[s]->cols[c];
       segs[s].out[c] = ctx.alloc<uint32_t>(rels[s]->nrows);
     }
-    bytes += 8.0 * rels[s]->nrows * rels[s]->ncols;
-  }
+  });
   SegRows* dsg = upload(ctx, segs);
   ctx.launch("gather", bytes, [&] {
     seg_gather_kernel<<<grid_cap(ctx, N, 4), kBlock, 0, ctx.stream>>>(dsg, drs, S, perm);
   });
   VG_CUDA(cudaGetLastError());
-  for (uint32_t s = 0; s < S; ++s)
+  parallel_for(S, [&](size_t s) {
     for (uint32_t c = 0; c < rels[s]->ncols; ++c) {
       rel_drop_col(ctx, *rels[s], c);
       rels[s]->cols[c] = segs[s].out[c];
     }
+  });
   ctx.free(vals);
   ctx.free(vals_alt);
   ctx.free(dsg);
@@ -529,6 +531,11 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
   double wbytes = 0;
   for (uint32_t j = 0; j < J; ++j) {
     if (totals[j] > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
+    ostart[j + 1] = ostart[j] + div_up(totals[j], kTileRows);
+    wbytes += 4.0 * totals[j] * (2.0 * (jb.l[j]->ncols + jb.r[j]->ncols - 1) - 1);
+  }
+  // the outputs of a wave's joins are allocated and described on the host pool
+  parallel_for(J, [&](size_t j) {
     const Rel* l = jb.l[j];
     const Rel* r = jb.r[j];
     const uint32_t ncols = l->ncols + r->ncols - 1;
@@ -544,9 +551,7 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
     for (uint32_t c = 0; c < ncols; ++c) o.oc[c] = out[j].cols[c];
     o.nlc = l->ncols;
     o.nrc = r->ncols - 1;
-    ostart[j + 1] = ostart[j] + div_up(totals[j], kTileRows);
-    wbytes += 4.0 * totals[j] * (2.0 * ncols - 1);
-  }
+  });
   JoinOut* djo = upload(ctx, jo);
   uint32_t* dfl = ctx.alloc<uint32_t>(2 * J);
   VG_CUDA(cudaMemsetAsync(dfl, 0, 2 * J * sizeof(uint32_t), ctx.stream));

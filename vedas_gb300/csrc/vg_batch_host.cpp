@@ -69,6 +69,13 @@ class WorkerPool {
       done_cv_.wait(lk, [&] { return busy_.load(std::memory_order_acquire) == 0; });
     }
     fn_ = nullptr;
+    std::exception_ptr e;
+    {
+      std::lock_guard<std::mutex> lk(err_mu_);
+      e = err_;
+      err_ = nullptr;
+    }
+    if (e) std::rethrow_exception(e);
   }
 
   ~WorkerPool() {
@@ -96,8 +103,24 @@ class WorkerPool {
     for (unsigned t = 0; t < nt; ++t) workers_.emplace_back([this] { loop(); });
   }
 
+  // Items are taken a few at a time: one shared counter hit per item would
+  // make the counter's cache line the bottleneck of short items.  The first
+  // exception an item throws is kept and rethrown by run() on the caller.
   void drain(const std::function<void(size_t)>& f, size_t n) {
-    for (size_t i = next_.fetch_add(1); i < n; i = next_.fetch_add(1)) f(i);
+    const size_t parts = workers_.size() + 1;
+    size_t chunk = n / (parts * 8);
+    chunk = chunk < 1 ? 1 : (chunk > 16 ? 16 : chunk);
+    for (size_t b = next_.fetch_add(chunk); b < n; b = next_.fetch_add(chunk)) {
+      const size_t e = b + chunk < n ? b + chunk : n;
+      for (size_t i = b; i < e; ++i) {
+        try {
+          f(i);
+        } catch (...) {
+          std::lock_guard<std::mutex> lk(err_mu_);
+          if (!err_) err_ = std::current_exception();
+        }
+      }
+    }
   }
 
   void loop() {
@@ -129,6 +152,8 @@ class WorkerPool {
   std::atomic<size_t> busy_{0};
   std::atomic<uint64_t> gen_{0};
   std::atomic<bool> stop_{false};
+  std::mutex err_mu_;
+  std::exception_ptr err_;
 };
 
 template <typename F>

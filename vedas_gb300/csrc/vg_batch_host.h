@@ -9,6 +9,7 @@
 
 #include "compat/vedas_compat.h"
 #include "vg_batch.h"
+#include "vg_pool.h"
 #include "vg_relops.h"
 
 namespace vg {
@@ -168,10 +169,6 @@ struct BatchResult {
   std::unique_ptr<HostResults> host;   // with run_batch(..., to_host)
   ~BatchResult();
 };
-
-// Runs f(0) .. f(n - 1) on the host worker pool (and the calling thread);
-// one parallel loop at a time, so callers from other threads take turns.
-void parallel_for(size_t n, const std::function<void(size_t)>& f);
 
 // Bits that hold every id of the storage's index (for WaveEngine's key_bits).
 int key_bits_for(vedas::VedasStorage* storage);
