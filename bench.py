@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=256, help="queries per CPU-baseline step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ingest-triples", type=int, default=20_000_000,
+                    help="triples of the N-Triples ingest measurement (0: skip)")
     ap.add_argument("--arena-gb", type=float, default=0.0,
                     help="HBM arena size (0: 90%% of free memory; profilers need room to replay)")
     return ap.parse_args()
@@ -258,6 +260,40 @@ def bench_reference(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def bench_ingest(args, ctx, g):
+    """N-Triples ingest on the device (parse + dictionary encoding) of the
+    first ingest_triples triples of the graph written as N-Triples text;
+    wall time of the call (text upload, kernels, dictionary terms to the
+    host) and kernel time, beside the CPU restatement on a sample."""
+    import vedas_gb300 as vg
+    from vedas_gb300 import workloads
+    m = min(args.ingest_triples, g.n)
+    sub = workloads.Graph(g.s[:m], g.p[:m], g.o[:m])
+    text = workloads.to_ntriples(sub)
+    vg.ingest_ntriples(ctx, text).free()          # warm-up
+    ctx.stats_reset(timing=True)
+    ctx.sync()
+    t0 = time.perf_counter()
+    ing = vg.ingest_ntriples(ctx, text)
+    wall = time.perf_counter() - t0
+    st = ctx.stats()
+    ing.free()
+    ctx.stats_reset(timing=False)
+    kms = sum(v[2] for v in st.values())
+    out = {"triples": m, "text_bytes": len(text), "wall_ms": 1000 * wall, "triples_per_s": m / wall,
+           "text_GBps": len(text) / wall / 1e9, "device_ms": kms,
+           "dictionary": {"so": ing.dict.size("so"), "p": ing.dict.size("p")},
+           "kernels": {k: round(v[2], 3) for k, v in st.items() if k.startswith("ingest") or k.startswith("radix")}}
+    if not args.no_cpu_baseline:
+        from oracle import oracle_py
+        k = min(m, 2_000_000)
+        t1 = time.perf_counter()
+        oracle_py.ingest_ntriples(text[:101 * k])
+        out["cpu_oracle_triples_per_s"] = k / (time.perf_counter() - t1)
+        out["cpu_oracle_sample"] = f"{k} triples, one thread (the loader's sequential hash-map rule)"
+    return out
+
+
 def bench_ours(args, rank, world, local, pg):
     import torch
     import vedas_gb300 as vg
@@ -283,6 +319,7 @@ def bench_ours(args, rank, world, local, pg):
         build = {"triples": g.n, "device_ms": kms, "rows_per_s": g.n / (kms / 1000.0),
                  "algorithmic_GBps": 2 * 24.0 * g.n / (kms / 1000.0) / 1e9,
                  "kernels": {k: round(v[2], 3) for k, v in kst.items()}}
+    ingest = bench_ingest(args, ctx, g) if args.ingest_triples > 0 else None
     chain = None
     try:
         from vedas_gb300 import workloads as wl
@@ -392,6 +429,7 @@ def bench_ours(args, rank, world, local, pg):
             "host_device_split_s_per_step": {k: round(v / args.steps, 4) for k, v in prof.items()},
             "index_build": build,
             "chain_query": chain,
+            "ingest": ingest,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h // max(args.steps, 1)},

@@ -267,6 +267,37 @@ void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint6
                   uint64_t* p3);
 vg_status vg_batch_free(vg_batch* b);
 
+/* ---- ingest (N-Triples) -------------------------------------------------- */
+typedef struct vg_dict vg_dict;
+
+/* Parses len bytes of N-Triples text (host memory) on the device and assigns
+ * ids in order of first appearance, as the reference's loader does with
+ * Raptor (load_rdf, src/loader.cu:19-93): subjects and non-literal objects
+ * share one dictionary (ids from 1), predicates have their own (ids from 1),
+ * literal objects a third (ids from 50,000,000) when literal_dict is set and
+ * share the first otherwise.  On success *s, *p, *o are device columns of *n
+ * ids (pass them to vg_index_build with inputs_on_device = 1; free them with
+ * vg_ingest_free) and *dict the dictionaries.  A malformed statement gives
+ * VG_ERR_PARSE with its line number in vg_last_error(). */
+vg_status vg_ingest_ntriples(vg_ctx* ctx, const char* text, uint64_t len, int literal_dict, uint32_t** s,
+                             uint32_t** p, uint32_t** o, uint64_t* n, vg_dict** dict);
+vg_status vg_ingest_free(vg_ctx* ctx, uint32_t* s, uint32_t* p, uint32_t* o);
+/* Dictionary kinds: 0 subject/object, 1 predicate, 2 literal. */
+uint64_t vg_dict_size(const vg_dict* d, int kind);
+/* The term of an id (its N-Triples text), NULL when unknown; valid until
+ * vg_dict_free. */
+const char* vg_dict_term(const vg_dict* d, int kind, uint32_t id);
+/* The id of a term, 0 when absent (the query front end's IRI lookup). */
+uint32_t vg_dict_lookup(vg_dict* d, int kind, const char* term);
+/* The reference's .vdd text (VedasBuild save_dict, src/VedasBuild.cu:145-160),
+ * written in id order; vg_dict_open reads entries in any order. */
+vg_status vg_dict_write(const vg_dict* d, const char* path);
+vg_status vg_dict_open(const char* path, vg_dict** out);
+vg_status vg_dict_free(vg_dict* d);
+/* Test hook, no reference counterpart: hash bits used to group terms (63
+ * by default); fewer force hash collisions, which ingest resolves exactly. */
+void vg_ingest_set_hash_bits(int bits);
+
 /* ---- serving (continuous batching) -------------------------------------- */
 typedef struct vg_server vg_server;
 

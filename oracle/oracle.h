@@ -58,6 +58,14 @@ void vo_sort_by_first(uint32_t** cols, uint32_t ncols, uint64_t nrows);
 uint64_t vo_inner_join(const uint32_t* a, uint64_t na, const uint32_t* b, uint64_t nb,
                        uint64_t* out_l, uint64_t* out_r);
 
+/* N-Triples ingest (src/loader.cu:19-53): 0 on success with malloc'd id
+ * columns and '\n'-joined dictionary terms in id order (subject/object,
+ * predicate, literal); otherwise the 1-based number of the first malformed
+ * line.  Free every output with vo_free.  Parity unpinned (Raptor absent). */
+uint64_t vo_ingest_ntriples(const char* text, uint64_t len, int literal_dict, uint64_t* n_out, uint32_t** s,
+                            uint32_t** p, uint32_t** o, char** so_terms, char** p_terms, char** l_terms);
+void vo_free(void* ptr);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,11 @@ def lib():
         L.vo_inner_join.restype = u64
         L.vo_inner_join.argtypes = [pu32, u64, pu32, u64, ctypes.POINTER(u64),
                                     ctypes.POINTER(u64)]
+        L.vo_ingest_ntriples.restype = u64
+        L.vo_ingest_ntriples.argtypes = [ctypes.c_char_p, u64, ctypes.c_int, ctypes.POINTER(u64),
+                                         ctypes.POINTER(pu32), ctypes.POINTER(pu32), ctypes.POINTER(pu32),
+                                         ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+        L.vo_free.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -153,3 +158,29 @@ def inner_join(a, b):
                         li.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
                         ri.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
     return li, ri
+
+
+def ingest_ntriples(text: bytes, literal_dict: bool = False):
+    """(s, p, o, {"so": [...], "p": [...], "l": [...]}) as the reference's
+    loader assigns them (src/loader.cu:19-53); raises ValueError with the
+    line number of a malformed statement."""
+    L = lib()
+    pu32 = ctypes.POINTER(ctypes.c_uint32)
+    n = ctypes.c_uint64()
+    s, p, o = pu32(), pu32(), pu32()
+    ts = [ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()]
+    bad = L.vo_ingest_ntriples(text, len(text), int(literal_dict), ctypes.byref(n), ctypes.byref(s),
+                               ctypes.byref(p), ctypes.byref(o), ctypes.byref(ts[0]), ctypes.byref(ts[1]),
+                               ctypes.byref(ts[2]))
+    if bad:
+        raise ValueError(f"malformed N-Triples statement on line {bad}")
+    cols = []
+    for c in (s, p, o):
+        cols.append(np.ctypeslib.as_array(c, shape=(max(n.value, 1),))[:n.value].copy())
+        L.vo_free(ctypes.cast(c, ctypes.c_void_p))
+    dicts = {}
+    for name, t in zip(("so", "p", "l"), ts):
+        raw = ctypes.string_at(t.value).decode("utf-8", "surrogateescape")
+        dicts[name] = raw.split("\n")[:-1] if raw else []
+        L.vo_free(t)
+    return cols[0], cols[1], cols[2], dicts

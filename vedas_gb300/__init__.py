@@ -113,6 +113,17 @@ def lib():
             "vg_batch_free": (i32, [vp]),
             "vg_serve_start": (i32, [vp, vp, ctypes.c_size_t, ctypes.POINTER(vp)]),
             "vg_serve_submit": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(u64)]),
+            "vg_ingest_ntriples": (i32, [vp, ctypes.c_char_p, u64, ctypes.c_int, ctypes.POINTER(vp),
+                                         ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(u64),
+                                         ctypes.POINTER(vp)]),
+            "vg_ingest_free": (i32, [vp, vp, vp, vp]),
+            "vg_dict_size": (u64, [vp, ctypes.c_int]),
+            "vg_dict_term": (ctypes.c_char_p, [vp, ctypes.c_int, u32]),
+            "vg_dict_lookup": (u32, [vp, ctypes.c_int, ctypes.c_char_p]),
+            "vg_dict_write": (i32, [vp, ctypes.c_char_p]),
+            "vg_dict_open": (i32, [ctypes.c_char_p, ctypes.POINTER(vp)]),
+            "vg_dict_free": (i32, [vp]),
+            "vg_ingest_set_hash_bits": (None, [ctypes.c_int]),
             "vg_serve_submit_many": (i32, [vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(ctypes.c_uint64)]),
             "vg_serve_wait": (i32, [vp, u64, ctypes.c_double, ctypes.POINTER(i32)]),
             "vg_serve_query_status": (i32, [vp, u64]),
@@ -549,3 +560,94 @@ def eif_scan(ctx: Context, rel: Relation):
     out = (ctypes.c_uint64 * 4)()
     check(lib().vg_eif_scan(ctx.h, ctypes.byref(rel.ir), out))
     return tuple(out)
+
+
+class Dict:
+    """The loader's dictionaries (vg_dict): kind 0 subject/object, 1
+    predicate, 2 literal; terms are their N-Triples text."""
+
+    KINDS = {"so": 0, "p": 1, "l": 2}
+
+    def __init__(self, handle):
+        self.h = handle
+
+    @staticmethod
+    def open(path: str) -> "Dict":
+        h = ctypes.c_void_p()
+        check(lib().vg_dict_open(path.encode(), ctypes.byref(h)))
+        return Dict(h)
+
+    def write(self, path: str) -> None:
+        check(lib().vg_dict_write(self.h, path.encode()))
+
+    def size(self, kind) -> int:
+        return int(lib().vg_dict_size(self.h, self.KINDS.get(kind, kind)))
+
+    def term(self, kind, ident: int):
+        t = lib().vg_dict_term(self.h, self.KINDS.get(kind, kind), ident)
+        return None if t is None else t.decode("utf-8", "surrogateescape")
+
+    def terms(self, kind) -> list:
+        k = self.KINDS.get(kind, kind)
+        base = 50000000 if k == 2 else 1
+        return [self.term(k, base + i) for i in range(self.size(k))]
+
+    def lookup(self, kind, term: str) -> int:
+        return int(lib().vg_dict_lookup(self.h, self.KINDS.get(kind, kind), term.encode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vg_dict_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ingested:
+    """Device id columns from vg_ingest_ntriples and their dictionary."""
+
+    def __init__(self, ctx, s, p, o, n, d):
+        self.ctx, self.s, self.p, self.o, self.n, self.dict = ctx, s, p, o, n, d
+
+    def device_ptrs(self):
+        return [self.s, self.p, self.o]
+
+    def index(self, full: bool = False) -> "Index":
+        """Builds the permutation indexes straight from the device columns."""
+        return Index(self.ctx, device_ptrs=self.device_ptrs(), n=self.n, full=full)
+
+    def columns(self):
+        """The three id columns copied to host arrays."""
+        ir = vg_ir()
+        ir.ncols, ir.nrows = 3, self.n
+        for c, ptr in enumerate(self.device_ptrs()):
+            ir.cols[c] = ptr
+        out = []
+        for c in range(3):
+            a = np.zeros(self.n, dtype=np.uint32)
+            if self.n:
+                check(lib().vg_ir_download(self.ctx.h, ctypes.byref(ir), c, _p32(a)))
+            out.append(a)
+        return out
+
+    def free(self):
+        if self.s is not None:
+            check(lib().vg_ingest_free(self.ctx.h, self.s, self.p, self.o))
+            self.s = self.p = self.o = None
+
+
+def ingest_ntriples(ctx: Context, text: bytes, literal_dict: bool = False) -> Ingested:
+    """Parses N-Triples text on the device (vg_ingest_ntriples)."""
+    s, p, o, d = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    n = ctypes.c_uint64()
+    check(lib().vg_ingest_ntriples(ctx.h, text, len(text), int(literal_dict), ctypes.byref(s), ctypes.byref(p),
+                                   ctypes.byref(o), ctypes.byref(n), ctypes.byref(d)))
+    return Ingested(ctx, s.value, p.value, o.value, n.value, Dict(d))
+
+
+def set_ingest_hash_bits(bits: int) -> None:
+    lib().vg_ingest_set_hash_bits(bits)

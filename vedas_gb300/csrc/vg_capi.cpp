@@ -7,6 +7,7 @@
 #include "compat/vedas_compat.h"
 #include "vg_batch.h"
 #include "vg_batch_host.h"
+#include "vg_ingest.h"
 #include "vg_ctx.h"
 #include "vg_serve.h"
 #include "vg_index.h"
@@ -23,6 +24,10 @@ struct vg_index {
 
 struct vg_batch {
   vg::BatchResult r;
+};
+
+struct vg_dict {
+  vg::Dict d;
 };
 
 struct vg_server {
@@ -581,6 +586,78 @@ vg_status vg_batch_free(vg_batch* b) {
   delete b;
   return VG_OK;
 }
+
+vg_status vg_ingest_ntriples(vg_ctx* ctx, const char* text, uint64_t len, int literal_dict, uint32_t** s,
+                             uint32_t** p, uint32_t** o, uint64_t* n, vg_dict** dict) {
+  if (!ctx || (len && !text) || !s || !p || !o || !n || !dict) return VG_ERR_INVALID;
+  *s = *p = *o = nullptr;
+  *n = 0;
+  *dict = nullptr;
+  auto d = std::make_unique<vg_dict>();
+  vg::Ingested in;
+  vg_status st = guard([&] {
+    vg::ingest_ntriples(ctx->c, text, len, literal_dict != 0, in);
+    d->d = std::move(in.dict);
+  });
+  if (st != VG_OK) {
+    if (in.s) ctx->c.free(in.s);
+    if (in.p) ctx->c.free(in.p);
+    if (in.o) ctx->c.free(in.o);
+    return st;
+  }
+  *s = in.s;
+  *p = in.p;
+  *o = in.o;
+  *n = in.n;
+  *dict = d.release();
+  return VG_OK;
+}
+
+vg_status vg_ingest_free(vg_ctx* ctx, uint32_t* s, uint32_t* p, uint32_t* o) {
+  if (!ctx) return VG_ERR_INVALID;
+  return guard([&] {
+    ctx->c.free(s);
+    ctx->c.free(p);
+    ctx->c.free(o);
+  });
+}
+
+uint64_t vg_dict_size(const vg_dict* d, int kind) {
+  if (!d) return 0;
+  return kind == 0 ? d->d.so.size() : kind == 1 ? d->d.p.size() : kind == 2 ? d->d.l.size() : 0;
+}
+
+const char* vg_dict_term(const vg_dict* d, int kind, uint32_t id) {
+  if (!d) return nullptr;
+  const std::string* t = d->d.term(kind, id);
+  return t ? t->c_str() : nullptr;
+}
+
+uint32_t vg_dict_lookup(vg_dict* d, int kind, const char* term) {
+  if (!d || !term) return 0;
+  return d->d.lookup(kind, term);
+}
+
+vg_status vg_dict_write(const vg_dict* d, const char* path) {
+  if (!d || !path) return VG_ERR_INVALID;
+  return guard([&] { vg::write_vdd(d->d, path); });
+}
+
+vg_status vg_dict_open(const char* path, vg_dict** out) {
+  if (!path || !out) return VG_ERR_INVALID;
+  *out = nullptr;
+  auto d = std::make_unique<vg_dict>();
+  vg_status st = guard([&] { vg::read_vdd(path, d->d); });
+  if (st == VG_OK) *out = d.release();
+  return st;
+}
+
+vg_status vg_dict_free(vg_dict* d) {
+  delete d;
+  return VG_OK;
+}
+
+void vg_ingest_set_hash_bits(int bits) { vg::set_ingest_hash_bits(bits); }
 
 vg_status vg_serve_start(vg_ctx* ctx, vg_index* ix, size_t budget_bytes, vg_server** out) {
   if (!ctx || !ix || !out) return VG_ERR_INVALID;

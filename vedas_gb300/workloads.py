@@ -297,3 +297,65 @@ def chain_query(g: Graph, preds=(1, 2, 5, 9), seed: int = 0) -> str:
     a, b, cc, d = preds
     return (f"SELECT * WHERE {{ ?a <{a}> ?b . ?b <{b}> ?c . ?c <{cc}> ?d . "
             f"?d <{d}> <{c}> . }}")
+
+
+def to_ntriples(g: Graph, blank_every: int = 97, lang_every: int = 5) -> bytes:
+    """The graph as N-Triples text, one statement per line in triple order.
+
+    Entities are IRIs <http://example.org/eNNNNNNNNNN>, except ids with
+    id % blank_every == 7, which are blank nodes _:bNNNNNNNNNN; predicates
+    are <http://example.org/pNNNNNNNNNN>; objects with ids from
+    LITERAL_START_ID are literals "vNNNNNNNNNN", every lang_every-th of them
+    tagged @en.  Every line is 101 bytes (terms padded with spaces), so the
+    text is built with array arithmetic."""
+    n = g.n
+    W = 101
+    buf = np.full((n, W), ord(" "), dtype=np.uint8)
+    s = g.s.astype(np.uint64)
+    p = g.p.astype(np.uint64)
+    o = g.o.astype(np.uint64)
+
+    def put(rows, col, text: bytes):
+        buf[rows, col:col + len(text)] = np.frombuffer(text, dtype=np.uint8)
+
+    def digits(rows, col, vals):
+        v = vals.copy()
+        for k in range(9, -1, -1):
+            buf[rows, col + k] = (48 + v % 10).astype(np.uint8)
+            v //= 10
+
+    def entity(col, ids):
+        blank = (ids % blank_every) == 7
+        iri = ~blank
+        put(iri, col, b"<http://example.org/e")
+        digits(iri, col + 21, ids[iri])
+        buf[iri, col + 31] = ord(">")
+        put(blank, col, b"_:b")
+        digits(blank, col + 3, ids[blank])
+
+    entity(0, s)
+    put(slice(None), 33, b"<http://example.org/p")
+    digits(slice(None), 54, p)
+    buf[:, 64] = ord(">")
+    lit = o >= LITERAL_START_ID
+    ent_rows = np.nonzero(~lit)[0]
+    if ent_rows.size:
+        # entity objects at column 66
+        ids = o[ent_rows]
+        blank = (ids % blank_every) == 7
+        iri_r, blank_r = ent_rows[~blank], ent_rows[blank]
+        put(iri_r, 66, b"<http://example.org/e")
+        digits(iri_r, 87, ids[~blank])
+        buf[iri_r, 97] = ord(">")
+        put(blank_r, 66, b"_:b")
+        digits(blank_r, 69, ids[blank])
+    lit_rows = np.nonzero(lit)[0]
+    if lit_rows.size:
+        put(lit_rows, 66, b'"v')
+        digits(lit_rows, 68, o[lit_rows])
+        buf[lit_rows, 78] = ord('"')
+        tagged = lit_rows[(o[lit_rows] % lang_every) == 0]
+        put(tagged, 79, b"@en")
+    buf[:, 99] = ord(".")
+    buf[:, 100] = ord("\n")
+    return buf.tobytes()
