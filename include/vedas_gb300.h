@@ -294,6 +294,24 @@ uint32_t vg_dict_lookup(vg_dict* d, int kind, const char* term);
 vg_status vg_dict_write(const vg_dict* d, const char* path);
 vg_status vg_dict_open(const char* path, vg_dict** out);
 vg_status vg_dict_free(vg_dict* d);
+/* Makes the queries on ix (vg_query, vg_batch_*, vg_serve_*) take constant
+ * terms as text, mapped through d as the reference's TriplePattern does
+ * (src/TriplePattern.cu:11-49): <iri> among subjects/objects or predicates by
+ * position, a quoted object among literals (language tag and datatype
+ * dropped, as Rasqal's value is), an absent term as id 0.  The ids are copied
+ * into ix, so d may be freed afterwards; NULL restores numeric <ID>
+ * constants. */
+vg_status vg_index_set_dict(vg_index* ix, const vg_dict* d);
+/* A result's rows as text (SparqlResult::printResult, src/SparqlResult.cu:
+ * 42-123, without the table frame): one line per row, tab-separated terms,
+ * each id decoded through the literal dictionary when it is in use and the
+ * id is a literal id, through the subject/object dictionary otherwise;
+ * unknown ids print as "?<id>".  *needed receives the size with the final
+ * NUL; VG_ERR_OVERFLOW when cap is smaller (call again with a larger buf). */
+vg_status vg_result_decode(const vg_result* r, const vg_dict* d, char* buf, size_t cap, size_t* needed);
+/* The same for query q of a batch (from its host copies when the batch was
+ * run with vg_batch_run_host). */
+vg_status vg_batch_decode(const vg_batch* b, uint32_t q, const vg_dict* d, char* buf, size_t cap, size_t* needed);
 /* Test hook, no reference counterpart: hash bits used to group terms (63
  * by default); fewer force hash collisions, which ingest resolves exactly. */
 void vg_ingest_set_hash_bits(int bits);

@@ -85,3 +85,48 @@ def test_ingested_columns_build_the_index_and_answer_queries(ctx, tmp_path):
     r.close()
     ix.close()
     ing.free()
+
+
+def test_iri_queries_and_decoded_results(ctx):
+    """Queries written with IRIs and literals go through the dictionary as the
+    reference's TriplePattern maps them; results decode back to terms."""
+    import vedas_gb300 as vg
+    g = workloads.graph_chain(n=200_000, n_entities=20_000, seed=25)
+    text = workloads.to_ntriples(g)
+    ing = vg.ingest_ntriples(ctx, text, literal_dict=True)
+    s, p, o, d = oracle_py.ingest_ntriples(text, True)
+    ix = ing.index()
+    ix.set_dict(ing.dict)
+    ref = oracle_py.OracleIndex(s, p, o)
+    so_id = {t: i + 1 for i, t in enumerate(d["so"])}
+    p_id = {t: i + 1 for i, t in enumerate(d["p"])}
+    l_id = {t: i + 50_000_000 for i, t in enumerate(d["l"])}
+    P1, P2 = "<http://example.org/p0000000001>", "<http://example.org/p0000000002>"
+    # an entity object and an untagged literal that occur with P1
+    rows = np.nonzero(p == p_id[P1])[0]
+    ent = next(d["so"][o[r] - 1] for r in rows if o[r] < 50_000_000)
+    lit = next(d["l"][o[r] - 50_000_000] for r in rows if o[r] >= 50_000_000 and "@" not in d["l"][o[r] - 50_000_000])
+    cases = [
+        (f"SELECT * WHERE {{ ?x {P1} ?a . ?x {P2} ?b . }}",
+         f"SELECT * WHERE {{ ?x <{p_id[P1]}> ?a . ?x <{p_id[P2]}> ?b . }}"),
+        (f"SELECT ?x WHERE {{ ?x {P1} {ent} . }}", f"SELECT ?x WHERE {{ ?x <{p_id[P1]}> <{so_id[ent]}> . }}"),
+        (f"SELECT ?x WHERE {{ ?x {P1} {lit} . }}", f"SELECT ?x WHERE {{ ?x <{p_id[P1]}> <{l_id[lit]}> . }}"),
+        # Rasqal keeps only the literal's text: the tag is dropped before the lookup
+        (f"SELECT ?x WHERE {{ ?x {P1} {lit}@en . }}", f"SELECT ?x WHERE {{ ?x <{p_id[P1]}> <{l_id[lit]}> . }}"),
+        # an absent IRI is id 0, which matches nothing
+        (f"SELECT ?x WHERE {{ ?x {P1} <http://example.org/nowhere> . }}", f"SELECT ?x WHERE {{ ?x <{p_id[P1]}> <0> . }}"),
+    ]
+    batch = vg.Batch(ix, [c[0] for c in cases], to_host=True)
+    for qi, (iri_q, num_q) in enumerate(cases):
+        r, rr = ix.query(iri_q), ref.query(num_q)
+        assert rr.status == 0
+        for a, b in zip(r.columns(), rr.columns):
+            np.testing.assert_array_equal(a, b)
+        want = [[(d["l"][v - 50_000_000] if v >= 50_000_000 else d["so"][v - 1]) for v in row]
+                for row in zip(*rr.columns)] if rr.columns and len(rr.columns[0]) else []
+        assert vg.decode_result(r, ing.dict) == want
+        assert vg.decode_batch(batch, qi, ing.dict) == want
+        r.close()
+    batch.close()
+    ix.close()
+    ing.free()

@@ -123,6 +123,10 @@ def lib():
             "vg_dict_write": (i32, [vp, ctypes.c_char_p]),
             "vg_dict_open": (i32, [ctypes.c_char_p, ctypes.POINTER(vp)]),
             "vg_dict_free": (i32, [vp]),
+            "vg_index_set_dict": (i32, [vp, vp]),
+            "vg_result_decode": (i32, [vp, vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+            "vg_batch_decode": (i32, [vp, u32, vp, ctypes.c_char_p, ctypes.c_size_t,
+                                      ctypes.POINTER(ctypes.c_size_t)]),
             "vg_ingest_set_hash_bits": (None, [ctypes.c_int]),
             "vg_serve_submit_many": (i32, [vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(ctypes.c_uint64)]),
             "vg_serve_wait": (i32, [vp, u64, ctypes.c_double, ctypes.POINTER(i32)]),
@@ -231,6 +235,11 @@ class Index:
 
     def write(self, path: str) -> None:
         check(lib().vg_index_write(self.h, path.encode()))
+
+    def set_dict(self, d) -> None:
+        """Query constants as IRIs / literals through the dictionary d
+        (None: numeric <ID> constants again)."""
+        check(lib().vg_index_set_dict(self.h, d.h if d is not None else None))
 
     def close(self):
         if getattr(self, "h", None):
@@ -651,3 +660,24 @@ def ingest_ntriples(ctx: Context, text: bytes, literal_dict: bool = False) -> In
 
 def set_ingest_hash_bits(bits: int) -> None:
     lib().vg_ingest_set_hash_bits(bits)
+
+
+def _decode(call) -> list:
+    need = ctypes.c_size_t()
+    st = call(None, 0, ctypes.byref(need))
+    if st not in (0, 7):   # 7: VG_ERR_OVERFLOW, the size is in need
+        check(st)
+    buf = ctypes.create_string_buffer(need.value)
+    check(call(buf, need.value, ctypes.byref(need)))
+    text = buf.value.decode("utf-8", "surrogateescape")
+    return [line.split("\t") for line in text.split("\n")[:-1]]
+
+
+def decode_result(res: "Result", d: Dict) -> list:
+    """Rows of a query result as terms (vg_result_decode)."""
+    return _decode(lambda b, c, n: lib().vg_result_decode(res.h, d.h, b, c, n))
+
+
+def decode_batch(batch: "Batch", q: int, d: Dict) -> list:
+    """Rows of query q of a batch as terms (vg_batch_decode)."""
+    return _decode(lambda b, c, n: lib().vg_batch_decode(batch.h, q, d.h, b, c, n))

@@ -266,12 +266,14 @@ static bool parse_id(const std::string& t, TYPEID& id) {
   return true;
 }
 
-TriplePattern::TriplePattern(size_t id_, const std::string& s, const std::string& p, const std::string& o)
+TriplePattern::TriplePattern(size_t id_, const std::string& s, const std::string& p, const std::string& o,
+                             const TermResolver* resolver)
     : id(id_) {
   const std::string* t[3] = {&s, &p, &o};
   for (int k = 0; k < 3; ++k) {
     isVar[k] = !t[k]->empty() && (*t[k])[0] == '?';
     if (isVar[k]) names[k] = *t[k];
+    else if (resolver) ids[k] = resolver->resolve(k, *t[k]);
     else if (!parse_id(*t[k], ids[k])) throw vg::Error(VG_ERR_PARSE, "bad constant term " + *t[k]);
   }
 }
@@ -282,7 +284,7 @@ bool TriplePattern::hasVariable(const std::string& v) const {
   return false;
 }
 
-SparqlQuery::SparqlQuery(const char* q) {
+SparqlQuery::SparqlQuery(const char* q, const TermResolver* resolver) {
   std::string text(q);
   std::vector<std::string> toks;
   for (size_t i = 0; i < text.size();) {
@@ -296,6 +298,14 @@ SparqlQuery::SparqlQuery(const char* q) {
       const size_t e = text.find(c == '<' ? '>' : '"', i + 1);
       if (e == std::string::npos) throw vg::Error(VG_ERR_PARSE, "unterminated term");
       i = e + 1;
+      if (c == '"' && i < text.size() && text[i] == '@') {   // language tag
+        ++i;
+        while (i < text.size() && (std::isalnum(static_cast<unsigned char>(text[i])) || text[i] == '-')) ++i;
+      } else if (c == '"' && i + 1 < text.size() && text[i] == '^' && text[i + 1] == '^') {   // datatype
+        const size_t d = text.find('>', i + 2);
+        if (d == std::string::npos) throw vg::Error(VG_ERR_PARSE, "unterminated datatype");
+        i = d + 1;
+      }
     } else if (c == '{' || c == '}' || c == '.' || c == '*') {
       ++i;
     } else {
@@ -329,7 +339,7 @@ SparqlQuery::SparqlQuery(const char* q) {
     if (toks[k] == ".") continue;
     t3.push_back(toks[k]);
     if (t3.size() == 3) {
-      TriplePattern tp(patterns.size(), t3[0], t3[1], t3[2]);
+      TriplePattern tp(patterns.size(), t3[0], t3[1], t3[2], resolver);
       for (int j = 0; j < 3; ++j)
         if (t3[j][0] == '?') note(t3[j]);
       if (tp.subjectIsVariable()) vars_count[tp.getSubject()] += 1;  // src/SparqlQuery.cu:65-67

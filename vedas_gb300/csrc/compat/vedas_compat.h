@@ -54,6 +54,16 @@ class IR {
   virtual ~IR() = default;
 };
 
+// Maps the text of a constant query term to its dictionary id (the
+// reference's TriplePattern constructor, src/TriplePattern.cu:11-49): pos 0
+// subject, 1 predicate, 2 object.  Absent terms give 0, as the reference's
+// map lookups do.  Must be callable from many threads at once.
+class TermResolver {
+ public:
+  virtual ~TermResolver() = default;
+  virtual TYPEID resolve(int pos, const std::string& term) const = 0;
+};
+
 class VedasStorage {
  public:
   // Builds the index on the device from host or device columns.
@@ -90,12 +100,17 @@ class VedasStorage {
   const TYPEID* devPOIdxValues() const { return d_[kPOIdxV]; }
   uint64_t len(const char* name) const { return ix_.get(name).len; }
   vg::Index& index() { return ix_; }
+  // Dictionary for constant terms written as text (IRIs, literals) in the
+  // queries run on this storage; null: constants are numeric ids.
+  const TermResolver* resolver() const { return resolver_; }
+  void setResolver(const TermResolver* r) { resolver_ = r; }
   void write(const char* fname);
 
  private:
   enum Mirror { kPIdxV, kPIdxO, kPSIdxV, kPSIdxO, kPOIdxV, kPOIdxO, kPS, kPO, kPSO, kPOS, kSOP, kMirrors };
   static const char* const kMirrorName[kMirrors];
   vg::Index ix_;
+  const TermResolver* resolver_ = nullptr;
   TYPEID_HOST_VEC* mirror_[kMirrors] = {};
   const TYPEID* d_[kMirrors] = {};
   void cacheDevice();   // the device arrays' addresses (set at construction)
@@ -162,7 +177,10 @@ class EmptyIntervalDict {
 
 class TriplePattern {
  public:
-  TriplePattern(size_t id, const std::string& s, const std::string& p, const std::string& o);
+  // Constants are <ID> / "ID" numbers, or any term text when a resolver maps
+  // them through the dictionaries.
+  TriplePattern(size_t id, const std::string& s, const std::string& p, const std::string& o,
+                const TermResolver* resolver = nullptr);
   size_t getId() const { return id; }
   TYPEID getSubjectId() const { return ids[0]; }
   TYPEID getPredicateId() const { return ids[1]; }
@@ -190,7 +208,7 @@ class TriplePattern {
 // constants written as <ID> or "ID".
 class SparqlQuery {
  public:
-  explicit SparqlQuery(const char* q);
+  explicit SparqlQuery(const char* q, const TermResolver* resolver = nullptr);
   size_t getPatternNum() const { return patterns.size(); }
   TriplePattern* getPatternPtr(size_t i) { return &patterns[i]; }
   std::map<std::string, int>& getVarCountMap() { return vars_count; }

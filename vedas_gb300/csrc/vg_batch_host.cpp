@@ -203,7 +203,7 @@ void prepare_mirrors(vedas::VedasStorage* storage) { storage->prepareMirrors(); 
 void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text, PlannedQuery& pq) {
   guarded(pq.out, [&] {
     pq.ex = std::make_unique<vedas::QueryExecutor>(storage, &ctx);
-    pq.sq = std::make_unique<vedas::SparqlQuery>(text.c_str());
+    pq.sq = std::make_unique<vedas::SparqlQuery>(text.c_str(), storage->resolver());
     std::set<std::string> sel = pq.sq->getSelectedVariables();
     pq.plan = std::make_unique<vedas::QueryPlan>(sel);
     pq.ex->plan(*pq.sq, *pq.plan);

@@ -20,6 +20,7 @@ struct vg_ctx {
 struct vg_index {
   vg_ctx* ctx = nullptr;
   std::unique_ptr<vedas::VedasStorage> st;
+  std::unique_ptr<vg::DictResolver> resolver;   // set by vg_index_set_dict
 };
 
 struct vg_batch {
@@ -375,7 +376,7 @@ vg_status vg_query(vg_ctx* ctx, vg_index* ix, const char* sparql, vg_result** ou
   auto res = std::make_unique<vg_result>();
   vg_status st = guard([&] {
     vedas::QueryExecutor ex(ix->st.get(), &ctx->c);
-    vedas::SparqlQuery sq(sparql);
+    vedas::SparqlQuery sq(sparql, ix->st->resolver());
     std::set<std::string> sel = sq.getSelectedVariables();
     vedas::QueryPlan plan(sel);
     ex.plan(sq, plan);
@@ -650,6 +651,72 @@ vg_status vg_dict_open(const char* path, vg_dict** out) {
   vg_status st = guard([&] { vg::read_vdd(path, d->d); });
   if (st == VG_OK) *out = d.release();
   return st;
+}
+
+namespace {
+vg_status decode_into(const vg::Dict& d, const std::vector<const uint32_t*>& cols, uint64_t nrows, char* buf,
+                      size_t cap, size_t* needed) {
+  const std::string text = vg::decode_rows(d, cols, nrows);
+  if (needed) *needed = text.size() + 1;
+  if (!buf || cap < text.size() + 1) return VG_ERR_OVERFLOW;
+  std::memcpy(buf, text.c_str(), text.size() + 1);
+  return VG_OK;
+}
+
+// The result columns of a relation in host memory.
+std::vector<std::vector<uint32_t>> host_columns(vg::Ctx& ctx, const vg::Rel& r) {
+  std::vector<std::vector<uint32_t>> h(r.ncols);
+  for (uint32_t c = 0; c < r.ncols; ++c) {
+    h[c].resize(r.nrows);
+    if (r.nrows)
+      VG_CUDA(cudaMemcpyAsync(h[c].data(), r.cols[c], r.nrows * 4, cudaMemcpyDeviceToHost, ctx.stream));
+  }
+  ctx.sync();
+  return h;
+}
+}  // namespace
+
+vg_status vg_result_decode(const vg_result* r, const vg_dict* d, char* buf, size_t cap, size_t* needed) {
+  if (!r || !d) return VG_ERR_INVALID;
+  vg_status st = VG_OK;
+  vg_status g = guard([&] {
+    auto h = host_columns(r->ctx->c, r->rel);
+    std::vector<const uint32_t*> cols;
+    for (auto& v : h) cols.push_back(v.data());
+    st = decode_into(d->d, cols, r->rel.nrows, buf, cap, needed);
+  });
+  return g != VG_OK ? g : st;
+}
+
+vg_status vg_batch_decode(const vg_batch* b, uint32_t q, const vg_dict* d, char* buf, size_t cap, size_t* needed) {
+  if (!b || !d || q >= b->r.queries.size()) return VG_ERR_INVALID;
+  const vg::BatchQuery& bq = b->r.queries[q];
+  if (bq.status != VG_OK) return bq.status;
+  vg_status st = VG_OK;
+  vg_status g = guard([&] {
+    std::vector<std::vector<uint32_t>> h;
+    std::vector<const uint32_t*> cols;
+    if (b->r.host && (bq.rel.nrows == 0 || bq.host[0])) {
+      for (uint32_t c = 0; c < bq.rel.ncols; ++c) cols.push_back(bq.host[c]);   // copies made during the batch
+    } else {
+      h = host_columns(*b->r.ctx, bq.rel);
+      for (auto& v : h) cols.push_back(v.data());
+    }
+    st = decode_into(d->d, cols, bq.rel.nrows, buf, cap, needed);
+  });
+  return g != VG_OK ? g : st;
+}
+
+vg_status vg_index_set_dict(vg_index* ix, const vg_dict* d) {
+  if (!ix) return VG_ERR_INVALID;
+  return guard([&] {
+    ix->st->setResolver(nullptr);
+    ix->resolver.reset();
+    if (d) {
+      ix->resolver = std::make_unique<vg::DictResolver>(&d->d);
+      ix->st->setResolver(ix->resolver.get());
+    }
+  });
 }
 
 vg_status vg_dict_free(vg_dict* d) {

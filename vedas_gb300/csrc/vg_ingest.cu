@@ -683,6 +683,53 @@ void ingest_ntriples(Ctx& ctx, const char* text, uint64_t len, bool literal_dict
   ctx.check_device_errors();
 }
 
+DictResolver::DictResolver(const Dict* d) {
+  const std::vector<std::string>* v[3] = {&d->so, &d->p, &d->l};
+  for (int k = 0; k < 3; ++k) {
+    const uint32_t base = k == 2 ? kLiteralStartId : 1u;
+    rev_[k].reserve(v[k]->size());
+    for (size_t i = 0; i < v[k]->size(); ++i) rev_[k].emplace((*v[k])[i], base + static_cast<uint32_t>(i));
+  }
+}
+
+vedas::TYPEID DictResolver::resolve(int pos, const std::string& term) const {
+  int kind = pos == 1 ? 1 : 0;
+  std::string key = term;
+  if (pos == 2 && !term.empty() && term[0] == '"') {
+    kind = 2;
+    key = term.substr(0, term.find('"', 1) + 1);   // "text" without @lang / ^^<type>
+  }
+  auto it = rev_[kind].find(key);
+  return it == rev_[kind].end() ? 0 : it->second;
+}
+
+std::string decode_rows(const Dict& d, const std::vector<const uint32_t*>& cols, uint64_t nrows) {
+  // rows are decoded in parallel blocks, then joined
+  constexpr uint64_t kRowsPerPart = 4096;
+  const uint64_t parts = (nrows + kRowsPerPart - 1) / kRowsPerPart;
+  std::vector<std::string> out(parts);
+  parallel_for(parts, [&](size_t b) {
+    std::string& o = out[b];
+    const uint64_t r1 = std::min<uint64_t>(nrows, (b + 1) * kRowsPerPart);
+    for (uint64_t r = b * kRowsPerPart; r < r1; ++r) {
+      for (size_t c = 0; c < cols.size(); ++c) {
+        if (c) o += '\t';
+        const uint32_t id = cols[c][r];
+        const std::string* t = (d.literal_dict && id >= kLiteralStartId) ? d.term(2, id) : d.term(0, id);
+        if (t) o += *t;
+        else o += "?" + std::to_string(id);
+      }
+      o += '\n';
+    }
+  });
+  size_t total = 0;
+  for (const auto& x : out) total += x.size();
+  std::string all;
+  all.reserve(total);
+  for (const auto& x : out) all += x;
+  return all;
+}
+
 void write_vdd(const Dict& d, const char* path) {
   std::ofstream out(path);
   if (!out) fail(VG_ERR_INVALID, std::string("cannot write ") + path);

@@ -7,6 +7,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "compat/vedas_compat.h"
 #include "vg_ctx.h"
 
 namespace vg {
@@ -27,6 +28,21 @@ struct Dict {
   std::unordered_map<std::string, uint32_t> rev_[3];     // built on first lookup
 };
 
+// Query constants through the dictionaries, with the reference's rules
+// (src/TriplePattern.cu:24-43 and toVedasString, src/SparqlQuery.cu:12-27):
+// a subject is looked up among subjects/objects, a predicate among
+// predicates, an object among literals when it is quoted (only its quoted
+// part: Rasqal drops the language tag and datatype) and among
+// subjects/objects otherwise.  Absent terms give 0.
+class DictResolver : public vedas::TermResolver {
+ public:
+  explicit DictResolver(const Dict* d);   // builds the reverse maps once
+  vedas::TYPEID resolve(int pos, const std::string& term) const override;
+
+ private:
+  std::unordered_map<std::string, uint32_t> rev_[3];
+};
+
 struct Ingested {
   uint64_t n = 0;                                      // triples
   uint32_t *s = nullptr, *p = nullptr, *o = nullptr;   // device columns (context arena)
@@ -38,6 +54,13 @@ struct Ingested {
 // appearance, exactly as the reference's statement handler does.  Malformed
 // lines raise VG_ERR_PARSE with the line number.
 void ingest_ntriples(Ctx& ctx, const char* text, uint64_t len, bool literal_dict, Ingested& out);
+
+// Result rows as text, one line per row, terms separated by tabs: an id
+// decodes through the literal dictionary when that dictionary is in use and
+// the id is a literal id, through the subject/object dictionary otherwise
+// (SparqlResult::printResult, src/SparqlResult.cu:95-104; result columns
+// never hold predicates here).  Unknown ids print as "?<id>".
+std::string decode_rows(const Dict& d, const std::vector<const uint32_t*>& cols, uint64_t nrows);
 
 // Reads and writes the reference's .vdd dictionary text: three sections
 // (subject/object, predicate, literal), each its size and then "id term"
