@@ -316,6 +316,13 @@ vg_status vg_batch_decode(const vg_batch* b, uint32_t q, const vg_dict* d, char*
  * by default); fewer force hash collisions, which ingest resolves exactly. */
 void vg_ingest_set_hash_bits(int bits);
 
+/* ---- self-check ----------------------------------------------------------- */
+/* No reference counterpart: runs one device wait that can never be satisfied
+ * (which 0: a look-back status word nobody publishes; 1: an mbarrier that
+ * expects bytes no copy delivers).  The wait gives up after about a second
+ * and the call returns VG_ERR_TIMEOUT; the context stays usable. */
+vg_status vg_selfcheck_bounded_wait(vg_ctx* ctx, int which);
+
 /* ---- serving (continuous batching) -------------------------------------- */
 typedef struct vg_server vg_server;
 

@@ -182,3 +182,18 @@ def test_select_results_own_their_columns(ctx):
         rel.free()
     ix.close()
     assert ctx.memory()[0] == used0               # every column freed exactly once
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_bounded_waits_time_out_and_context_stays_usable(ctx, which):
+    """A device wait that can never be satisfied gives up with a timeout
+    status instead of hanging; the next work on the context runs normally."""
+    import vedas_gb300 as vg
+    st = vg.lib().vg_selfcheck_bounded_wait(ctx.h, which)
+    assert st == 4                                   # VG_ERR_TIMEOUT
+    g = workloads.graph_small_star(n=20_000, n_subjects=1_000, seed=30)
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    ref = oracle_py.OracleIndex(g.s, g.p, g.o)
+    q = workloads.star_query(1, 2)
+    _same_result(ix.query(q), ref.query(q))
+    ix.close()

@@ -16,7 +16,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["vg_sort.cu", "vg_index.cu", "vg_relops.cu", "vg_batch.cu", "vg_noalloc.cu", "vg_ingest.cu"]
+CU_SOURCES = ["vg_sort.cu", "vg_index.cu", "vg_relops.cu", "vg_batch.cu", "vg_noalloc.cu", "vg_ingest.cu", "vg_selfcheck.cu"]
 CPP_SOURCES = ["vg_ctx.cpp", "vg_storage.cpp", "vg_capi.cpp", "compat/vedas_compat.cpp",
                "vg_batch_host.cpp", "vg_serve.cpp"]
 

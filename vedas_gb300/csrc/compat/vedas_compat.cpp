@@ -60,7 +60,7 @@ void VedasStorage::prepareMirrors() {
 FullRelationIR::FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSize) : ctx_(ctx) {
   r_ = vg::rel_alloc(*ctx, static_cast<uint32_t>(columnNum), relationSize);
   headers.resize(columnNum);
-  is_predicates.resize(columnNum);
+  var_column_map.v.reserve(columnNum + 1);
 }
 
 FullRelationIR::FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSize, const TYPEID* const* views)
@@ -71,7 +71,7 @@ FullRelationIR::FullRelationIR(vg::Ctx* ctx, size_t columnNum, size_t relationSi
   for (size_t c = 0; c < columnNum; ++c) r_.cols[c] = const_cast<TYPEID*>(views[c]);
   r_.borrowed = (1u << columnNum) - 1u;
   headers.resize(columnNum);
-  is_predicates.resize(columnNum);
+  var_column_map.v.reserve(columnNum + 1);
 }
 
 FullRelationIR::~FullRelationIR() { vg::rel_free(*ctx_, r_); }
@@ -89,9 +89,9 @@ vg::Rel FullRelationIR::release() {
 }
 
 size_t FullRelationIR::getColumnId(const std::string& var) const {
-  auto it = var_column_map.find(var);
-  if (it == var_column_map.end()) throw ReferenceUB("getColumnId: no column for " + var);
-  return it->second;
+  const size_t* c = var_column_map.find(var);
+  if (!c) throw ReferenceUB("getColumnId: no column for " + var);
+  return *c;
 }
 
 void FullRelationIR::setHeader(size_t i, const std::string& h, bool is_predicate) {
@@ -132,7 +132,8 @@ void FullRelationIR::removeColumn(size_t i) {  // src/FullRelationIR.cu:729-736
   for (size_t k = i; k + 1 < r_.ncols; ++k) r_.cols[k] = r_.cols[k + 1];
   r_.cols[r_.ncols - 1] = nullptr;
   r_.ncols -= 1;
-  is_predicates.erase(is_predicates.begin() + static_cast<long>(i));
+  for (size_t k = i; k + 1 < VG_MAX_COLS; ++k) is_predicates[k] = is_predicates[k + 1];
+  is_predicates[VG_MAX_COLS - 1] = false;
   headers.erase(headers.begin() + static_cast<long>(i));
   for (size_t k = i; k < headers.size(); ++k) var_column_map[headers[k]] = k;
 }

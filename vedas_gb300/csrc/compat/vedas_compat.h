@@ -18,6 +18,7 @@
 #pragma once
 
 #include <cstdint>
+#include <array>
 #include <map>
 #include <memory>
 #include <set>
@@ -154,9 +155,27 @@ class FullRelationIR : public IR {
  private:
   vg::Ctx* ctx_;
   vg::Rel r_;
-  std::vector<bool> is_predicates;
+  // per column (at most VG_MAX_COLS): kept in place, no allocation
+  std::array<bool, VG_MAX_COLS> is_predicates{};
   std::vector<std::string> headers;
-  std::unordered_map<std::string, size_t> var_column_map;
+  // Variable -> column.  A relation has at most nine columns, so a short
+  // list searched in order replaces the reference's hash map.  Entries are
+  // assigned and found as in a map and never removed: the reference's map
+  // also keeps a removed column's stale index.
+  struct VarColumns {
+    std::vector<std::pair<std::string, size_t>> v;
+    const size_t* find(const std::string& k) const {
+      for (const auto& e : v)
+        if (e.first == k) return &e.second;
+      return nullptr;
+    }
+    size_t& operator[](const std::string& k) {
+      for (auto& e : v)
+        if (e.first == k) return e.second;
+      v.emplace_back(k, 0);
+      return v.back().second;
+    }
+  } var_column_map;
 };
 
 class EmptyIntervalDict {

@@ -8,6 +8,7 @@
 #include "vg_batch.h"
 #include "vg_batch_host.h"
 #include "vg_ingest.h"
+#include "vg_selfcheck.h"
 #include "vg_ctx.h"
 #include "vg_serve.h"
 #include "vg_index.h"
@@ -725,6 +726,11 @@ vg_status vg_dict_free(vg_dict* d) {
 }
 
 void vg_ingest_set_hash_bits(int bits) { vg::set_ingest_hash_bits(bits); }
+
+vg_status vg_selfcheck_bounded_wait(vg_ctx* ctx, int which) {
+  if (!ctx || which < 0 || which > 1) return VG_ERR_INVALID;
+  return guard([&] { vg::selfcheck_bounded_wait(ctx->c, which); });
+}
 
 vg_status vg_serve_start(vg_ctx* ctx, vg_index* ix, size_t budget_bytes, vg_server** out) {
   if (!ctx || !ix || !out) return VG_ERR_INVALID;

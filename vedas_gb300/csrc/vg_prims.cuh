@@ -198,9 +198,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait for phase `parity` of an mbarrier; false (and a recorded
 // timeout) when it did not complete.
+// Non-blocking test of phase `parity`.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Polls with non-blocking tests and short sleeps, so the bound is in time
+// (about kSpinLimit x 64 ns) and not in hardware suspend periods.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, DeviceErrors* err) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    if (mbar_test_wait(bar, parity)) return true;
+    __nanosleep(64);
+  }
   atomicExch(&err->timeout, 1u);
   return false;
 }
