@@ -51,7 +51,19 @@ const char* const VedasStorage::kMirrorName[VedasStorage::kMirrors] = {
     "ps_data",      "po_data",       "pso_data",        "pos_data",       "sop_data"};
 
 void VedasStorage::prepareMirrors() {
-  for (int m = 0; m < kMirrors; ++m) h(static_cast<Mirror>(m));
+  std::call_once(mirrors_once_, [this] {
+    for (int m = 0; m < kMirrors; ++m) h(static_cast<Mirror>(m));
+    const TYPEID_HOST_VEC& l1o = *mirror_[kPIdxO];
+    for (int po = 0; po < 2; ++po) {
+      const TYPEID_HOST_VEC& l2o = *mirror_[po ? kPOIdxO : kPSIdxO];
+      std::vector<size_t>& r = l2r_[po];
+      r.resize(l1o.size() + 1);
+      for (size_t s = 0; s <= l1o.size(); ++s) {
+        const TYPEID v = s < l1o.size() ? l1o[s] : static_cast<TYPEID>(ix_.n);
+        r[s] = static_cast<size_t>(std::lower_bound(l2o.begin(), l2o.end(), v) - l2o.begin());
+      }
+    }
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -385,6 +397,21 @@ std::pair<size_t, size_t> QueryExecutor::findL2OffsetFromL1(const TYPEID_HOST_VE
   return {(*l1o)[s], (e == l1o->size()) ? n : (*l1o)[e]};
 }
 
+// std::upper_bound(a + from, a + hi, key), searched from the front: steps of
+// 1, 2, 4, ... and a binary search inside the last one.  An upper bound just
+// after the lower bound of the same key (a run of equal keys) takes a few
+// reads in cache instead of a second search over the whole range.
+static size_t upper_from(const TYPEID* a, size_t from, size_t hi, TYPEID key) {
+  size_t lo = from, step = 1;
+  while (lo < hi && !(key < a[lo])) {
+    const size_t nx = lo + step;
+    if (nx >= hi || key < a[nx]) return static_cast<size_t>(std::upper_bound(a + lo + 1, a + std::min(nx, hi), key) - a);
+    lo = nx;
+    step <<= 1;
+  }
+  return lo;
+}
+
 std::pair<size_t, size_t> QueryExecutor::findDataOffsetFromL2(const TYPEID_HOST_VEC* l2v,
                                                               const TYPEID_HOST_VEC* l2o, TYPEID lo,
                                                               TYPEID hi, TYPEID id2) {
@@ -392,7 +419,7 @@ std::pair<size_t, size_t> QueryExecutor::findDataOffsetFromL2(const TYPEID_HOST_
   const size_t b = std::lower_bound(l2o->begin(), l2o->end(), lo) - l2o->begin();
   const size_t e = std::lower_bound(l2o->begin(), l2o->end(), hi) - l2o->begin();
   const size_t s2 = std::lower_bound(l2v->begin() + b, l2v->begin() + e, id2) - l2v->begin();
-  const size_t e2 = std::upper_bound(l2v->begin() + b, l2v->begin() + e, id2) - l2v->begin();
+  const size_t e2 = upper_from(l2v->data(), s2, e, id2);
   if (s2 >= l2o->size() || e2 >= l2o->size())
     throw ReferenceUB("findDataOffsetFromL2 reads past the level-2 offsets");
   return {(*l2o)[s2], (*l2o)[e2]};
@@ -401,8 +428,29 @@ std::pair<size_t, size_t> QueryExecutor::findDataOffsetFromL2(const TYPEID_HOST_
 std::pair<size_t, size_t> QueryExecutor::findDataOffsetFromL2(const TYPEID_HOST_VEC* d, size_t lo, size_t hi,
                                                               TYPEID id2) {
   const size_t s = std::lower_bound(d->begin() + lo, d->begin() + hi, id2) - d->begin();
-  const size_t e = std::upper_bound(d->begin() + lo, d->begin() + hi, id2) - d->begin();
-  return {s, e};
+  return {s, upper_from(d->data(), s, hi, id2)};
+}
+
+std::pair<size_t, size_t> QueryExecutor::findDataOffsetForKey(VedasStorage* st, bool po, TYPEID id1, TYPEID id2,
+                                                              size_t n) {
+  TYPEID_HOST_VEC* l1v = st->getPredicateIndexValues();
+  TYPEID_HOST_VEC* l1o = st->getPredicateIndexOffsets();
+  TYPEID_HOST_VEC* l2v = po ? st->getPredicateObjectIndexValues() : st->getPredicateSubjectIndexValues();
+  TYPEID_HOST_VEC* l2o = po ? st->getPredicateObjectIndexOffsets() : st->getPredicateSubjectIndexOffsets();
+  const std::vector<size_t>& r = st->l2RangeOfL1(po);
+  if (l1v->empty() || l2o->empty() || r.size() != l1o->size() + 1 || n != st->getTripleSize()) {
+    auto r1 = findL2OffsetFromL1(l1v, l1o, id1, n);
+    return findDataOffsetFromL2(l2v, l2o, static_cast<TYPEID>(r1.first), static_cast<TYPEID>(r1.second), id2);
+  }
+  const size_t s = std::lower_bound(l1v->begin(), l1v->end(), id1) - l1v->begin();
+  if (s >= l1o->size()) throw ReferenceUB("findL2OffsetFromL1 reads past the level-1 index");
+  // lower_bound(l2o, l1o[s]) and lower_bound(l2o, l1o[s + 1] or n)
+  const size_t b = r[s], e = r[s + 1];
+  const size_t s2 = std::lower_bound(l2v->begin() + b, l2v->begin() + e, id2) - l2v->begin();
+  const size_t e2 = upper_from(l2v->data(), s2, e, id2);
+  if (s2 >= l2o->size() || e2 >= l2o->size())
+    throw ReferenceUB("findDataOffsetFromL2 reads past the level-2 offsets");
+  return {(*l2o)[s2], (*l2o)[e2]};
 }
 
 QueryExecutor::QueryExecutor(VedasStorage* s, vg::Ctx* c) : storage(s), ctx(c) {}
@@ -623,13 +671,9 @@ void SelectQueryJob::prepare(SelectWork& w) {
   TYPEID_HOST_VEC* l1o = st->getPredicateIndexOffsets();
   if (variable_num == 1) {
     const bool subj = pos_index;
-    TYPEID_HOST_VEC* l2v = subj ? st->getPredicateObjectIndexValues() : st->getPredicateSubjectIndexValues();
-    TYPEID_HOST_VEC* l2o = subj ? st->getPredicateObjectIndexOffsets() : st->getPredicateSubjectIndexOffsets();
     TYPEID_HOST_VEC* data = subj ? st->getPOSdata() : st->getPSOdata();
     const TYPEID* ddata = subj ? st->devPOSdata() : st->devPSOdata();
-    auto r1 = QueryExecutor::findL2OffsetFromL1(l1v, l1o, dataid[0], data->size());
-    auto r2 = QueryExecutor::findDataOffsetFromL2(l2v, l2o, static_cast<TYPEID>(r1.first),
-                                                  static_cast<TYPEID>(r1.second), dataid[1]);
+    auto r2 = QueryExecutor::findDataOffsetForKey(st, subj, dataid[0], dataid[1], data->size());
     if (r2.first > r2.second) r2.second = r2.first;
     const size_t rows = r2.second - r2.first;
     // the uploaded slice is read, never written: the relation views it
@@ -678,8 +722,17 @@ void SelectQueryJob::prepare(SelectWork& w) {
     // that start in [first, second): a contiguous slice of the level-2 values.
     TYPEID_HOST_VEC* l2o = pos_index ? st->getPredicateObjectIndexOffsets() : st->getPredicateSubjectIndexOffsets();
     const TYPEID* dl2v = pos_index ? st->devPOIdxValues() : st->devPSIdxValues();
-    const size_t ra = static_cast<size_t>(std::lower_bound(l2o->begin(), l2o->end(), first) - l2o->begin());
-    const size_t rb = static_cast<size_t>(std::lower_bound(l2o->begin(), l2o->end(), second) - l2o->begin());
+    // first and second lie in the predicate's data range, so their positions
+    // among the level-2 offsets lie in the predicate's level-2 range
+    auto l2lo = l2o->begin(), l2hi = l2o->end();
+    const std::vector<size_t>& l2r = st->l2RangeOfL1(pos_index);
+    if (l2r.size() == l1o->size() + 1) {
+      const size_t s1 = std::lower_bound(l1v->begin(), l1v->end(), dataid[0]) - l1v->begin();
+      l2lo = l2o->begin() + l2r[s1];
+      l2hi = l2o->begin() + l2r[s1 + 1];
+    }
+    const size_t ra = static_cast<size_t>(std::lower_bound(l2lo, l2hi, first) - l2o->begin());
+    const size_t rb = static_cast<size_t>(std::lower_bound(l2lo, l2hi, second) - l2o->begin());
     if (row > 0 && (ra >= l2o->size() || (*l2o)[ra] != first || rb < ra))
       throw vg::Error(VG_ERR_INVALID, "select range does not start a level-2 run");
     const size_t kept = row > 0 ? rb - ra : 0;

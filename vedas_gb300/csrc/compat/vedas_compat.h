@@ -21,6 +21,7 @@
 #include <array>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <set>
 #include <string>
 #include <tuple>
@@ -88,9 +89,16 @@ class VedasStorage {
   TYPEID_HOST_VEC* getPSOdata() { return h(kPSO); }
   TYPEID_HOST_VEC* getPOSdata() { return h(kPOS); }
   TYPEID_HOST_VEC* getSOPdata() { return h(kSOP); }
-  // Makes every host mirror above (downloading on first use); after it the
-  // getters may be called from many threads at once.
+  // Makes every host mirror above (downloading on first use) and the level-2
+  // range tables below; after it the getters may be called from many threads
+  // at once.
   void prepareMirrors();
+  // Level-2 range of every predicate, for the predicate-subject (po = false)
+  // or predicate-object (po = true) index: entry s is the first level-2 entry
+  // whose offset is not below the predicate index offset s (the last entry
+  // uses the triple count), i.e. findDataOffsetFromL2's two searches of the
+  // level-2 offsets done once per predicate.  Empty before prepareMirrors().
+  const std::vector<size_t>& l2RangeOfL1(bool po) const { return l2r_[po ? 1 : 0]; }
   // Device copies (resident).
   const TYPEID* dev(const char* name) const { return ix_.get(name).ptr; }
   const TYPEID* devPSdata() const { return d_[kPS]; }
@@ -114,6 +122,8 @@ class VedasStorage {
   const TermResolver* resolver_ = nullptr;
   TYPEID_HOST_VEC* mirror_[kMirrors] = {};
   const TYPEID* d_[kMirrors] = {};
+  std::vector<size_t> l2r_[2];
+  std::once_flag mirrors_once_;
   void cacheDevice();   // the device arrays' addresses (set at construction)
   TYPEID_HOST_VEC* h(Mirror m) {
     if (!mirror_[m]) mirror_[m] = const_cast<TYPEID_HOST_VEC*>(&ix_.host_array(kMirrorName[m]));
@@ -450,6 +460,12 @@ class QueryExecutor {
                                                         TYPEID id2);
   static std::pair<size_t, size_t> findDataOffsetFromL2(const TYPEID_HOST_VEC* l2_data, size_t lo,
                                                         size_t hi, TYPEID id2);
+  // findL2OffsetFromL1(l1v, l1o, id1, n) followed by the five-argument
+  // findDataOffsetFromL2 on the predicate-subject (po = false) or
+  // predicate-object index, with the level-2 offset searches read from the
+  // storage's per-predicate table; the same result (and the same errors).
+  static std::pair<size_t, size_t> findDataOffsetForKey(VedasStorage* st, bool po, TYPEID id1, TYPEID id2,
+                                                        size_t n);
 
   // Execution log of the current query (QueryExecutor::exe_log).
   std::vector<ExecuteLogRecord> exe_log;

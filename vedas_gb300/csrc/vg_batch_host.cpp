@@ -15,12 +15,14 @@
 #include <atomic>
 #include <condition_variable>
 #include <cstdlib>
+#include <deque>
 #include <exception>
 #include <functional>
 #include <mutex>
 #include <thread>
 
 #include "vg_batch.h"
+#include "vg_pool.h"
 
 namespace vg {
 
@@ -78,6 +80,38 @@ class WorkerPool {
     if (e) std::rethrow_exception(e);
   }
 
+  // Work that no caller waits for.  Idle workers run it between parallel
+  // loops; a pool without workers runs it at once on the caller.
+  void post(void (*fn)(void*), void* arg) {
+    if (workers_.empty()) {
+      run_task({fn, arg});
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(bg_mu_);
+      bg_.push_back({fn, arg});
+      bg_n_.fetch_add(1, std::memory_order_release);
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);   // a worker about to sleep sees bg_n_ or this notify
+    }
+    cv_.notify_one();
+  }
+
+  // Runs the queued work on the caller and waits for the work that workers
+  // are running; the first error a task raised is rethrown here.
+  void drain() {
+    while (run_one()) {
+    }
+    while (bg_running_.load(std::memory_order_acquire) != 0) std::this_thread::yield();
+    std::string msg;
+    {
+      std::lock_guard<std::mutex> lk(bg_mu_);
+      msg.swap(bg_err_);
+    }
+    if (!msg.empty()) throw Error(VG_ERR_INVALID, "background release: " + msg);
+  }
+
   ~WorkerPool() {
     stop_.store(true);
     {
@@ -123,15 +157,55 @@ class WorkerPool {
     }
   }
 
+  struct Task {
+    void (*fn)(void*);
+    void* arg;
+  };
+
+  void run_task(Task t) {
+    try {
+      t.fn(t.arg);
+    } catch (const std::exception& e) {
+      std::lock_guard<std::mutex> lk(bg_mu_);
+      if (bg_err_.empty()) bg_err_ = e.what();
+    } catch (...) {
+      std::lock_guard<std::mutex> lk(bg_mu_);
+      if (bg_err_.empty()) bg_err_ = "unknown exception";
+    }
+  }
+
+  // Takes and runs one queued task; false when none is queued.
+  bool run_one() {
+    if (bg_n_.load(std::memory_order_acquire) == 0) return false;
+    Task t;
+    {
+      std::lock_guard<std::mutex> lk(bg_mu_);
+      if (bg_.empty()) return false;
+      t = bg_.front();
+      bg_.pop_front();
+      bg_running_.fetch_add(1, std::memory_order_acq_rel);
+      bg_n_.fetch_sub(1, std::memory_order_release);
+    }
+    run_task(t);
+    bg_running_.fetch_sub(1, std::memory_order_acq_rel);
+    return true;
+  }
+
   void loop() {
     uint64_t seen = 0;
     while (true) {
       uint64_t g = gen_.load(std::memory_order_acquire);
-      for (int i = 0; g == seen && i < kSpin; ++i) g = gen_.load(std::memory_order_acquire);
+      for (int i = 0; g == seen && i < kSpin; ++i) {
+        if (bg_n_.load(std::memory_order_relaxed) != 0 && run_one()) i = 0;
+        g = gen_.load(std::memory_order_acquire);
+      }
       if (g == seen) {
         std::unique_lock<std::mutex> lk(mu_);
-        cv_.wait(lk, [&] { return gen_.load(std::memory_order_acquire) != seen; });
+        cv_.wait(lk, [&] {
+          return gen_.load(std::memory_order_acquire) != seen || bg_n_.load(std::memory_order_acquire) != 0;
+        });
         g = gen_.load(std::memory_order_acquire);
+        if (g == seen) continue;   // woken for queued work: run it from the polling loop
       }
       seen = g;
       if (stop_.load()) return;
@@ -154,6 +228,11 @@ class WorkerPool {
   std::atomic<bool> stop_{false};
   std::mutex err_mu_;
   std::exception_ptr err_;
+  // queued work (post / drain)
+  std::mutex bg_mu_;
+  std::deque<Task> bg_;
+  std::string bg_err_;
+  std::atomic<size_t> bg_n_{0}, bg_running_{0};
 };
 
 template <typename F>
@@ -255,7 +334,7 @@ WaveEngine::~WaveEngine() {
 void WaveEngine::add(PlannedQuery* pq) { active_.push_back(pq); }
 
 void WaveEngine::bury() {
-  pfor(graveyard_.size(), [&](size_t k) { graveyard_[k].reset(); });
+  release_later(graveyard_);
   graveyard_.clear();
 }
 
@@ -349,16 +428,10 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
 
   auto t0 = Clock::now();
   items_.assign(run_.size(), Item());
-  const size_t nrun = run_.size(), ndead = graveyard_.size();
-  if (nrun > 0) ++waves_;
-  if (nrun + ndead > 0) {
-    // one parallel phase prepares the next jobs and destroys the plans of
-    // the queries handed back in the last stage B
-    pfor(nrun + ndead, [&](size_t k) {
-      if (k >= nrun) {
-        graveyard_[k - nrun].reset();
-        return;
-      }
+  const size_t nrun = run_.size();
+  if (nrun > 0) {
+    ++waves_;
+    pfor(nrun, [&](size_t k) {
       PlannedQuery* q = run_[k];
       vedas::QueryJob* job = q->plan->getJob(q->next);
       Item& it = items_[k];
@@ -380,7 +453,6 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
       });
       if (q->out->status != VG_OK) it.kind = Item::kNone;
     });
-    graveyard_.clear();
   }
   prof.prepare_s += since(t0);
 
@@ -522,8 +594,9 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
       if (q->ex) out->log = std::move(q->ex->exe_log);
     });
     // the plans (jobs, intermediate relations, host state) of finished
-    // queries are destroyed in the next stage A's parallel phase
+    // queries are destroyed by idle host workers
     for (PlannedQuery* q : final_) graveyard_.push_back(std::move(q->plan));
+    bury();
     for (PlannedQuery* q : final_) completed.push_back(q);
     if (host_) {
       std::vector<BatchQuery*> outs;
@@ -682,19 +755,66 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   out.prof.plan_s = plan_s;
   if (out.host) out.host->finish();
   ctx.check_device_errors();
-  // plans first (their jobs point at the executors), then parsed queries and
-  // executors (bounds, empty intervals, logs) on the pool
+  // plans, parsed queries and executors (bounds, empty intervals, logs) are
+  // destroyed by idle host workers
   e0.bury();
   e1.bury();
-  pfor(pq.size(), [&](size_t i) {
-    pq[i].plan.reset();
-    pq[i].ex.reset();
-    pq[i].sq.reset();
-  });
+  release_later(pq);
   out.prof.total_s = since(t_all);
 }
 
 void parallel_for(size_t n, const std::function<void(size_t)>& f) { WorkerPool::get().run(n, f); }
+
+void post_background(void (*fn)(void*), void* arg) { WorkerPool::get().post(fn, arg); }
+
+void drain_background() { WorkerPool::get().drain(); }
+
+namespace {
+const bool kReclaimHook = (set_arena_reclaim(&drain_background), true);
+
+// Groups of this many queries' host state per queued task.
+constexpr size_t kReleaseGroup = 16;
+
+template <typename T>
+void release_groups(std::vector<T>& v) {
+  for (size_t b = 0; b < v.size(); b += kReleaseGroup) {
+    const size_t e = std::min(v.size(), b + kReleaseGroup);
+    auto* grp = new std::vector<T>();
+    grp->reserve(e - b);
+    for (size_t i = b; i < e; ++i) grp->push_back(std::move(v[i]));
+    post_background([](void* p) { delete static_cast<std::vector<T>*>(p); }, grp);
+  }
+  v.clear();
+}
+}  // namespace
+
+void release_later(std::vector<std::unique_ptr<vedas::QueryPlan>>& plans) { release_groups(plans); }
+
+// A planned query's plan goes first (its jobs point at the executor), then
+// the parsed query and the executor.
+void release_later(std::vector<PlannedQuery>& pq) {
+  struct Remains {
+    std::unique_ptr<vedas::QueryPlan> plan;
+    std::unique_ptr<vedas::SparqlQuery> sq;
+    std::unique_ptr<vedas::QueryExecutor> ex;
+    ~Remains() {
+      plan.reset();
+      ex.reset();
+      sq.reset();
+    }
+  };
+  std::vector<std::unique_ptr<Remains>> r;
+  r.reserve(pq.size());
+  for (PlannedQuery& q : pq) {
+    if (!q.plan && !q.sq && !q.ex) continue;
+    auto x = std::make_unique<Remains>();
+    x->plan = std::move(q.plan);
+    x->sq = std::move(q.sq);
+    x->ex = std::move(q.ex);
+    r.push_back(std::move(x));
+  }
+  release_groups(r);
+}
 
 int key_bits_for(vedas::VedasStorage* storage) {
   const uint32_t m = storage->index().max_id;

@@ -75,6 +75,12 @@ struct PlannedQuery {
 // Plans one query on the host (thread-safe across queries once the storage's
 // host mirrors exist: see prepare_mirrors).  Errors go to pq.out.
 void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text, PlannedQuery& pq);
+// Destroys the host state of finished queries (plans with their jobs and
+// intermediate relations, parsed queries, executors) on idle host workers
+// (post_background); the vectors are left empty.  Device memory goes back to
+// the arena when a worker gets to it: drain_background() waits for that.
+void release_later(std::vector<std::unique_ptr<vedas::QueryPlan>>& plans);
+void release_later(std::vector<PlannedQuery>& pq);
 void prepare_mirrors(vedas::VedasStorage* storage);
 
 // Advances every added query by one job per wave; the device work of a wave
@@ -150,7 +156,7 @@ class WaveEngine {
   std::vector<Rel> jouts_;
   // queries whose last job finished: compacted in stage A, handed back in stage B
   std::vector<PlannedQuery*> final_;
-  std::vector<std::unique_ptr<vedas::QueryPlan>> graveyard_;   // destroyed in the next stage A
+  std::vector<std::unique_ptr<vedas::QueryPlan>> graveyard_;   // handed to release_later by bury()
   std::vector<SegRows> fin_seg_;
   std::vector<vedas::FullRelationIR*> fin_res_;
   // device -> host results of each stage and the events that mark them

@@ -138,6 +138,8 @@ vg_status vg_ctx_create(int device, size_t arena_bytes, vg_ctx** out) {
 vg_status vg_ctx_destroy(vg_ctx* ctx) {
   if (!ctx) return VG_OK;
   vg::Ctx& c = ctx->c;
+  // queued releases of finished queries free into this context's arena
+  guard([] { vg::drain_background(); });
   if (c.stream) cudaStreamSynchronize(c.stream);
   c.release_dl_stream();
   c.release_pinned();
@@ -152,6 +154,8 @@ vg_status vg_ctx_destroy(vg_ctx* ctx) {
 
 vg_status vg_ctx_memory(vg_ctx* ctx, size_t* used, size_t* peak, size_t* capacity) {
   if (!ctx) return VG_ERR_INVALID;
+  const vg_status st = guard([] { vg::drain_background(); });
+  if (st != VG_OK) return st;
   if (used) *used = ctx->c.arena.used();
   if (peak) *peak = ctx->c.arena.peak();
   if (capacity) *capacity = ctx->c.arena.capacity();
@@ -208,6 +212,7 @@ vg_status vg_index_build(vg_ctx* ctx, const uint32_t* s, const uint32_t* p, cons
 vg_status vg_index_free(vg_index* ix) {
   if (!ix) return VG_OK;
   vg_status st = guard([&] {
+    vg::drain_background();
     ix->ctx->c.sync();
     ix->st.reset();
   });

@@ -27,7 +27,7 @@ void Arena::setup(char* base, size_t bytes, bool owned) {
   for (size_t k = 0; k < nchunks_; ++k) chunk_class_[k].store(-1, std::memory_order_relaxed);
   shards_.reset(new Shard[kShards]);
   if (bytes) add_free(0, bytes);
-  used_.store(0);
+  big_used_ = 0;
   peak_.store(0);
 }
 
@@ -55,11 +55,25 @@ int Arena::small_class(size_t off) const {
   return chunk_class_[off / kChunk].load(std::memory_order_relaxed);
 }
 
-void Arena::note_used(size_t add) {
-  const size_t u = used_.fetch_add(add, std::memory_order_relaxed) + add;
+size_t Arena::used() const {
+  if (!shards_) return 0;
+  int64_t u = 0;
+  for (int k = 0; k < kShards; ++k) u += shards_[k].used.load(std::memory_order_relaxed);
+  std::lock_guard<std::mutex> lk(mu_);
+  return static_cast<size_t>(u) + big_used_;
+}
+
+size_t Arena::sample_peak() const {
+  const size_t u = used();
   size_t pk = peak_.load(std::memory_order_relaxed);
   while (u > pk && !peak_.compare_exchange_weak(pk, u, std::memory_order_relaxed)) {
   }
+  return u;
+}
+
+size_t Arena::peak() const {
+  sample_peak();
+  return peak_.load(std::memory_order_relaxed);
 }
 
 void Arena::erase_by_size(size_t sz, size_t off) { by_size_.erase({sz, off}); }
@@ -143,13 +157,14 @@ void* Arena::try_alloc(size_t bytes) {
       if (!sh.free[c].empty()) {
         const size_t off = sh.free[c].back();
         sh.free[c].pop_back();
-        note_used(csz);
+        sh.used.fetch_add(static_cast<int64_t>(csz), std::memory_order_relaxed);
         return base_ + off;
       }
     }
     // refill from the global list (a quarter of a chunk's worth of blocks,
     // at least two), or carve a new chunk
     std::vector<size_t> got;
+    size_t big_off = SIZE_MAX;
     {
       std::lock_guard<std::mutex> lk(mu_);
       std::vector<size_t>& g = small_free_[c];
@@ -167,33 +182,53 @@ void* Arena::try_alloc(size_t bytes) {
           for (size_t k = cb / csz; k-- > 0;) got.push_back(a + k * csz);
         } else {
           // no aligned chunk left: serve it as a large block
-          const size_t off = big_alloc(bytes);
-          if (off == SIZE_MAX) return nullptr;
-          live_[off] = bytes;
-          note_used(bytes);
-          return base_ + off;
+          big_off = big_alloc(bytes);
+          if (big_off == SIZE_MAX) return nullptr;
+          live_[big_off] = bytes;
+          big_used_ += bytes;
         }
       }
     }
+    if (big_off != SIZE_MAX) {
+      sample_peak();
+      return base_ + big_off;
+    }
     const size_t off = got.back();
     got.pop_back();
-    if (!got.empty()) {
+    {
       std::lock_guard<std::mutex> lk(sh.mu);
       sh.free[c].insert(sh.free[c].end(), got.begin(), got.end());
+      sh.used.fetch_add(static_cast<int64_t>(csz), std::memory_order_relaxed);
     }
-    note_used(csz);
+    sample_peak();
     return base_ + off;
   }
-  std::lock_guard<std::mutex> lk(mu_);
-  const size_t off = big_alloc(bytes);
-  if (off == SIZE_MAX) return nullptr;
-  live_[off] = bytes;
-  note_used(bytes);
+  size_t off;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    off = big_alloc(bytes);
+    if (off == SIZE_MAX) return nullptr;
+    live_[off] = bytes;
+    big_used_ += bytes;
+  }
+  sample_peak();
   return base_ + off;
 }
 
+namespace {
+std::atomic<void (*)()> g_reclaim{nullptr};
+}
+
+void set_arena_reclaim(void (*fn)()) { g_reclaim.store(fn); }
+
 void* Arena::alloc(size_t bytes) {
   void* p = try_alloc(bytes);
+  if (!p) {
+    if (void (*fn)() = g_reclaim.load()) {
+      fn();
+      p = try_alloc(bytes);
+    }
+  }
   if (!p)
     fail(VG_ERR_OOM, "arena exhausted: requested " + std::to_string(bytes) + " bytes, used " +
                          std::to_string(used()) + " of " + std::to_string(cap_));
@@ -207,11 +242,11 @@ void Arena::free(void* p) {
   const int c = small_class(off);
   if (c >= 0) {
     const size_t csz = kAlign << c;
-    used_.fetch_sub(csz, std::memory_order_relaxed);
     Shard& sh = shards_[my_shard()];
     std::vector<size_t> spill;
     {
       std::lock_guard<std::mutex> lk(sh.mu);
+      sh.used.fetch_sub(static_cast<int64_t>(csz), std::memory_order_relaxed);
       std::vector<size_t>& v = sh.free[c];
       v.push_back(off);
       // a shard keeps up to a chunk's worth of a class (at least 8 blocks);
@@ -233,7 +268,7 @@ void Arena::free(void* p) {
   if (it == live_.end()) fail(VG_ERR_INVALID, "arena free of an unknown block");
   const size_t sz = it->second;
   live_.erase(it);
-  used_.fetch_sub(sz, std::memory_order_relaxed);
+  big_used_ -= sz;
   big_free(off, sz);
 }
 
@@ -250,7 +285,7 @@ void Arena::shrink(void* p, size_t new_bytes) {
   if (new_bytes >= it->second) return;
   const size_t tail = it->second - new_bytes;
   it->second = new_bytes;
-  used_.fetch_sub(tail, std::memory_order_relaxed);
+  big_used_ -= tail;
   big_free(off + new_bytes, tail);
 }
 

@@ -31,6 +31,10 @@ namespace vg {
 // wait on each other.  Shards hand surplus blocks back to a global list and
 // refill from it in batches.  Larger blocks are best-fit with coalescing
 // under one lock.
+// Called by Arena::alloc when a request does not fit, before it fails: frees
+// whose release was deferred (drain_background) get their chance first.
+void set_arena_reclaim(void (*fn)());
+
 class Arena {
  public:
   Arena() = default;
@@ -49,8 +53,13 @@ class Arena {
   // (small blocks keep their class).
   void shrink(void* p, size_t new_bytes);
   size_t capacity() const { return cap_; }
-  size_t used() const { return used_.load(std::memory_order_relaxed); }
-  size_t peak() const { return peak_.load(std::memory_order_relaxed); }
+  // Bytes in live blocks (small blocks count their class size).  Exact once
+  // no other thread allocates or frees.
+  size_t used() const;
+  // The highest used() seen at a large allocation, a small-block refill from
+  // the shared lists, or a call of used()/peak(): small blocks are counted in
+  // their thread's shard, so no shared counter is touched per block.
+  size_t peak() const;
   size_t largest_free() const;
 
   static constexpr size_t kAlign = 256;
@@ -67,11 +76,15 @@ class Arena {
   struct alignas(64) Shard {
     std::mutex mu;
     std::vector<size_t> free[kClasses];
+    // bytes allocated minus bytes freed by the threads of this shard (a block
+    // may be freed by another shard's thread, so one shard may go negative)
+    std::atomic<int64_t> used{0};
   };
   char* base_ = nullptr;
   bool owned_ = false;
   size_t cap_ = 0;
-  std::atomic<size_t> used_{0}, peak_{0};
+  size_t big_used_ = 0;                                // live large blocks, under mu_
+  mutable std::atomic<size_t> peak_{0};
   // under mu_
   std::map<size_t, size_t> free_;                      // offset -> size (large free blocks)
   std::set<std::pair<size_t, size_t>> by_size_;        // (size, offset) of the same blocks
@@ -90,7 +103,7 @@ class Arena {
   void erase_by_size(size_t sz, size_t off);
   void take_free(size_t off, size_t sz);               // removes a free block from both indexes
   void add_free(size_t off, size_t sz);
-  void note_used(size_t add);
+  size_t sample_peak() const;                          // used(), folded into peak_
   int small_class(size_t off) const;
   static int my_shard();
 };
