@@ -716,54 +716,62 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
     plan_query(ctx, storage, texts[i], pq[i]);
   });
   const double plan_s = since(t0);
-  // two engines take turns on the stream: while the device runs one
-  // engine's half-wave, the host runs the other's stages
+  // engines take turns on the stream: while the device runs one engine's
+  // half-wave, the host runs another's stages.  Each engine runs on its own
+  // host thread (parallel phases share the worker pool).
   const int kb = key_bits_for(storage);
-  WaveEngine e0(ctx, kb), e1(ctx, kb);
+  const size_t ne = batch_engines();
+  std::vector<std::unique_ptr<WaveEngine>> eng;
+  for (size_t e = 0; e < ne; ++e) eng.push_back(std::make_unique<WaveEngine>(ctx, kb));
   if (to_host) {
     out.host = std::make_unique<HostResults>(ctx);
-    e0.set_host_results(out.host.get());
-    e1.set_host_results(out.host.get());
+    for (auto& e : eng) e->set_host_results(out.host.get());
   }
-  for (size_t i = 0; i < pq.size(); ++i) (i % 2 ? e1 : e0).add(&pq[i]);
-  // each engine on its own host thread: one waits for the device while the
-  // other runs its host stages (parallel phases share the worker pool)
-  std::vector<PlannedQuery*> done0, done1;
-  std::exception_ptr err1;
-  std::thread t1([&] {
+  for (size_t i = 0; i < pq.size(); ++i) eng[i % ne]->add(&pq[i]);
+  std::vector<std::exception_ptr> err(ne);
+  auto drive = [&](size_t e) {
+    std::vector<PlannedQuery*> done;
     try {
-      while (e1.active() > 0) e1.step(done1);
+      while (eng[e]->active() > 0) eng[e]->step(done);
     } catch (...) {
-      err1 = std::current_exception();
+      err[e] = std::current_exception();
     }
-  });
-  std::exception_ptr err0;
-  try {
-    while (e0.active() > 0) e0.step(done0);
-  } catch (...) {
-    err0 = std::current_exception();
+  };
+  std::vector<std::thread> th;
+  for (size_t e = 1; e < ne; ++e) th.emplace_back(drive, e);
+  drive(0);
+  for (auto& t : th) t.join();
+  for (auto& e : err)
+    if (e) std::rethrow_exception(e);
+  out.waves = 0;
+  out.prof = BatchProfile();
+  for (auto& e : eng) {
+    out.waves = std::max(out.waves, e->waves());
+    out.prof.prepare_s += e->prof.prepare_s;
+    out.prof.device_s += e->prof.device_s;
+    out.prof.finish_s += e->prof.finish_s;
+    out.prof.final_s += e->prof.final_s;
   }
-  t1.join();
-  if (err0) std::rethrow_exception(err0);
-  if (err1) std::rethrow_exception(err1);
-  out.waves = std::max(e0.waves(), e1.waves());
-  out.prof = e0.prof;
-  out.prof.prepare_s += e1.prof.prepare_s;
-  out.prof.device_s += e1.prof.device_s;
-  out.prof.finish_s += e1.prof.finish_s;
-  out.prof.final_s += e1.prof.final_s;
   out.prof.plan_s = plan_s;
   if (out.host) out.host->finish();
   ctx.check_device_errors();
   // plans, parsed queries and executors (bounds, empty intervals, logs) are
   // destroyed by idle host workers
-  e0.bury();
-  e1.bury();
+  for (auto& e : eng) e->bury();
   release_later(pq);
   out.prof.total_s = since(t_all);
 }
 
 void parallel_for(size_t n, const std::function<void(size_t)>& f) { WorkerPool::get().run(n, f); }
+
+size_t batch_engines() {
+  static const size_t n = [] {
+    long v = 2;
+    if (const char* e = std::getenv("VG_BATCH_ENGINES")) v = std::strtol(e, nullptr, 10);
+    return static_cast<size_t>(std::min(8L, std::max(1L, v)));
+  }();
+  return n;
+}
 
 void post_background(void (*fn)(void*), void* arg) { WorkerPool::get().post(fn, arg); }
 
@@ -790,30 +798,39 @@ void release_groups(std::vector<T>& v) {
 
 void release_later(std::vector<std::unique_ptr<vedas::QueryPlan>>& plans) { release_groups(plans); }
 
-// A planned query's plan goes first (its jobs point at the executor), then
-// the parsed query and the executor.
+// The whole vector is handed over at once; queued tasks release ranges of
+// it (a query's plan first, since its jobs point at the executor, then the
+// parsed query and the executor) and the last one deletes it.
 void release_later(std::vector<PlannedQuery>& pq) {
-  struct Remains {
-    std::unique_ptr<vedas::QueryPlan> plan;
-    std::unique_ptr<vedas::SparqlQuery> sq;
-    std::unique_ptr<vedas::QueryExecutor> ex;
-    ~Remains() {
-      plan.reset();
-      ex.reset();
-      sq.reset();
-    }
+  if (pq.empty()) return;
+  struct Held {
+    std::vector<PlannedQuery> v;
+    std::atomic<size_t> left{0};
   };
-  std::vector<std::unique_ptr<Remains>> r;
-  r.reserve(pq.size());
-  for (PlannedQuery& q : pq) {
-    if (!q.plan && !q.sq && !q.ex) continue;
-    auto x = std::make_unique<Remains>();
-    x->plan = std::move(q.plan);
-    x->sq = std::move(q.sq);
-    x->ex = std::move(q.ex);
-    r.push_back(std::move(x));
+  struct Range {
+    Held* h;
+    size_t b, e;
+  };
+  constexpr size_t kRange = 64;
+  auto* h = new Held;
+  h->v = std::move(pq);
+  pq.clear();
+  const size_t n = h->v.size(), groups = (n + kRange - 1) / kRange;
+  h->left.store(groups);
+  for (size_t b = 0; b < n; b += kRange) {
+    post_background(
+        [](void* p) {
+          std::unique_ptr<Range> r(static_cast<Range*>(p));
+          for (size_t i = r->b; i < r->e; ++i) {
+            PlannedQuery& q = r->h->v[i];
+            q.plan.reset();
+            q.ex.reset();
+            q.sq.reset();
+          }
+          if (r->h->left.fetch_sub(1, std::memory_order_acq_rel) == 1) delete r->h;
+        },
+        new Range{h, b, std::min(n, b + kRange)});
   }
-  release_groups(r);
 }
 
 int key_bits_for(vedas::VedasStorage* storage) {

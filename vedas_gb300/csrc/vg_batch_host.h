@@ -81,6 +81,9 @@ void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text,
 // the arena when a worker gets to it: drain_background() waits for that.
 void release_later(std::vector<std::unique_ptr<vedas::QueryPlan>>& plans);
 void release_later(std::vector<PlannedQuery>& pq);
+// Wave engines of one run_batch, each on its own host thread
+// (VG_BATCH_ENGINES, 1..8; default 2).
+size_t batch_engines();
 void prepare_mirrors(vedas::VedasStorage* storage);
 
 // Advances every added query by one job per wave; the device work of a wave
