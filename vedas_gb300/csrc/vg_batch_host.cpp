@@ -41,12 +41,42 @@ double since(Clock::time_point t0) {
 // sleep on the condition variable, and the caller polls for the workers'
 // completion the same way: a sleeping thread takes tens of microseconds to
 // wake, which would add up over the hundreds of phases of a batch.
+//
+// There is one process-wide pool over all host threads, and one smaller pool
+// per wave engine of a batch: the engines' parallel phases run at the same
+// time on disjoint threads (see EnginePools), while planning uses them all.
 class WorkerPool {
  public:
+  // The calling thread's pool: its engine's pool on an engine thread, else
+  // the process-wide one.
   static WorkerPool& get() {
-    static WorkerPool pool;
+    WorkerPool* p = current();
+    return p ? *p : global();
+  }
+  static WorkerPool& global() {
+    static WorkerPool pool(host_threads());
     return pool;
   }
+  static WorkerPool*& current() {
+    static thread_local WorkerPool* p = nullptr;
+    return p;
+  }
+  // VG_HOST_THREADS sets the number of host threads of the process-wide pool,
+  // the calling thread included (default: the hardware threads, at most 32).
+  static unsigned host_threads() {
+    unsigned total = std::thread::hardware_concurrency();
+    if (const char* e = std::getenv("VG_HOST_THREADS")) {
+      const long v = std::strtol(e, nullptr, 10);
+      if (v >= 1) total = static_cast<unsigned>(v);
+    }
+    return std::max(1u, std::min(total, 32u));
+  }
+  // threads: the calling thread and threads - 1 workers.
+  explicit WorkerPool(unsigned threads) {
+    for (unsigned t = 1; t < threads; ++t) workers_.emplace_back([this] { loop(); });
+  }
+  WorkerPool(const WorkerPool&) = delete;
+  WorkerPool& operator=(const WorkerPool&) = delete;
 
   void run(size_t n, const std::function<void(size_t)>& f) {
     if (n < 64 || workers_.empty()) {   // small loops run on the caller alone
@@ -124,18 +154,6 @@ class WorkerPool {
 
  private:
   static constexpr int kSpin = 1 << 16;
-
-  // VG_HOST_THREADS sets the number of host threads of a parallel phase,
-  // the calling thread included (default: the hardware threads, at most 32).
-  WorkerPool() {
-    unsigned total = std::thread::hardware_concurrency();
-    if (const char* e = std::getenv("VG_HOST_THREADS")) {
-      const long v = std::strtol(e, nullptr, 10);
-      if (v >= 1) total = static_cast<unsigned>(v);
-    }
-    const unsigned nt = total > 1 ? std::min<unsigned>(total - 1, 31) : 0;
-    for (unsigned t = 0; t < nt; ++t) workers_.emplace_back([this] { loop(); });
-  }
 
   // Items are taken a few at a time: one shared counter hit per item would
   // make the counter's cache line the bottleneck of short items.  The first
@@ -233,6 +251,37 @@ class WorkerPool {
   std::deque<Task> bg_;
   std::string bg_err_;
   std::atomic<size_t> bg_n_{0}, bg_running_{0};
+};
+
+// The pools of the wave engines of a batch (batch_engines() of them), each
+// over an equal share of the host threads, the engine's own thread included;
+// made on first use.  With one engine, the engine uses the process-wide pool.
+std::atomic<bool> g_engine_pools_made{false};
+
+std::vector<std::unique_ptr<WorkerPool>>& engine_pools() {
+  static std::vector<std::unique_ptr<WorkerPool>> v = [] {
+    std::vector<std::unique_ptr<WorkerPool>> p;
+    const size_t ne = batch_engines();
+    const unsigned share = std::max<unsigned>(1, WorkerPool::host_threads() / static_cast<unsigned>(ne));
+    if (ne > 1)
+      for (size_t e = 0; e < ne; ++e) p.emplace_back(new WorkerPool(share));
+    g_engine_pools_made.store(true);
+    return p;
+  }();
+  return v;
+}
+
+// Makes engine e's pool the calling thread's pool for its lifetime.
+class UseEnginePool {
+ public:
+  explicit UseEnginePool(size_t e) : prev_(WorkerPool::current()) {
+    auto& p = engine_pools();
+    if (e < p.size()) WorkerPool::current() = p[e].get();
+  }
+  ~UseEnginePool() { WorkerPool::current() = prev_; }
+
+ private:
+  WorkerPool* prev_;
 };
 
 template <typename F>
@@ -717,8 +766,9 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   });
   const double plan_s = since(t0);
   // engines take turns on the stream: while the device runs one engine's
-  // half-wave, the host runs another's stages.  Each engine runs on its own
-  // host thread (parallel phases share the worker pool).
+  // half-wave, the host runs the others' stages.  Each engine runs on its own
+  // host thread with its own share of the worker threads, so the engines'
+  // parallel phases run at the same time.
   const int kb = key_bits_for(storage);
   const size_t ne = batch_engines();
   std::vector<std::unique_ptr<WaveEngine>> eng;
@@ -730,6 +780,7 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::st
   for (size_t i = 0; i < pq.size(); ++i) eng[i % ne]->add(&pq[i]);
   std::vector<std::exception_ptr> err(ne);
   auto drive = [&](size_t e) {
+    UseEnginePool use(e);
     std::vector<PlannedQuery*> done;
     try {
       while (eng[e]->active() > 0) eng[e]->step(done);
@@ -766,7 +817,7 @@ void parallel_for(size_t n, const std::function<void(size_t)>& f) { WorkerPool::
 
 size_t batch_engines() {
   static const size_t n = [] {
-    long v = 2;
+    long v = 4;
     if (const char* e = std::getenv("VG_BATCH_ENGINES")) v = std::strtol(e, nullptr, 10);
     return static_cast<size_t>(std::min(8L, std::max(1L, v)));
   }();
@@ -775,7 +826,11 @@ size_t batch_engines() {
 
 void post_background(void (*fn)(void*), void* arg) { WorkerPool::get().post(fn, arg); }
 
-void drain_background() { WorkerPool::get().drain(); }
+void drain_background() {
+  WorkerPool::global().drain();
+  if (g_engine_pools_made.load())
+    for (auto& p : engine_pools()) p->drain();
+}
 
 namespace {
 const bool kReclaimHook = (set_arena_reclaim(&drain_background), true);

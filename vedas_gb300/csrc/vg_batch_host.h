@@ -81,8 +81,8 @@ void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text,
 // the arena when a worker gets to it: drain_background() waits for that.
 void release_later(std::vector<std::unique_ptr<vedas::QueryPlan>>& plans);
 void release_later(std::vector<PlannedQuery>& pq);
-// Wave engines of one run_batch, each on its own host thread
-// (VG_BATCH_ENGINES, 1..8; default 2).
+// Wave engines of one run_batch, each on its own host thread with its own
+// share of the host worker threads (VG_BATCH_ENGINES, 1..8; default 4).
 size_t batch_engines();
 void prepare_mirrors(vedas::VedasStorage* storage);
 

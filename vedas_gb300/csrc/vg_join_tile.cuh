@@ -127,56 +127,54 @@ __device__ __forceinline__ void lockstep_bounds(const uint32_t* __restrict__ R, 
   }
 }
 
-// Lower bound (in R) and match count of L[i0, min(i0 + kJcTile, nl)).  R is
-// sorted; the window of R that can match the tile, [lower(L[i0]),
-// upper(L[last])), is found by two warps at once and staged in shared memory
-// when it fits: its 16-byte aligned middle by one cp.async.bulk completed on
-// an mbarrier, its ragged ends by plain loads.  A window that does not fit (a
-// heavy key, or a right side much larger than the left) is searched in global
-// memory with lockstep bounds instead.
-// The tile's counts stay in registers: thread t holds the counts of left
-// keys i0 + 8t .. i0 + 8t + 7 in cnt[] (zero past the end); lower bounds go
-// to lo_out.  Every thread of the block must call it.
-__device__ __forceinline__ void join_count_tile_regs(const uint32_t* __restrict__ L, uint64_t nl,
-                                                     const uint32_t* __restrict__ R, uint64_t nr, uint64_t i0,
-                                                     uint32_t* __restrict__ lo_out, uint32_t (&cnt)[kJcKeys],
-                                                     JoinCountSmem& sm, DeviceErrors* err) {
-#pragma unroll
-  for (int j = 0; j < kJcKeys; ++j) cnt[j] = 0;
-  const uint32_t tid = threadIdx.x;
-  const uint64_t i_end = (i0 + kJcTile < nl) ? i0 + kJcTile : nl;
-  if (tid < 32) {
-    const uint64_t w0 = warp_bound<false, uint32_t>(R, 0, nr, L[i0]);
-    if (tid == 0) sm.w0 = w0;
-  } else if (tid < 64) {
-    const uint64_t w1 = warp_bound<true, uint32_t>(R, 0, nr, L[i_end - 1]);
-    if (tid == 32) sm.w1 = w1;
-  }
-  __syncthreads();
+// Thread 0 of the block: records the tile's right-key window [w0, w1) and
+// decides how it is staged in shared memory (sm.staged: 0 not staged, 1 by
+// the block's threads, 2 its 16-byte aligned middle by one cp.async.bulk
+// completed on sm.bar, its ragged ends by the threads).  The block must pass
+// a barrier before jc_count_staged.
+__device__ __forceinline__ void jc_issue_window(const uint32_t* __restrict__ R, uint64_t w0, uint64_t w1,
+                                                JoinCountSmem& sm) {
+  sm.w0 = w0;
+  sm.w1 = w1;
+  sm.staged = 0;
+  sm.failed = 0;
   // R may start at any 4-byte boundary (a view of an index slice): element e
   // sits on a 16-byte boundary when (e + mis) % 4 == 0, and the window is laid
   // out in shared memory from `base`, the aligned element at or below w0
   // (index arithmetic is modulo 2^64, so base may lie below element 0).
   const uint64_t mis = (reinterpret_cast<uintptr_t>(R) >> 2) & 3u;
-  if (tid == 0) {
-    const uint64_t w0 = sm.w0, w1 = sm.w1;
-    sm.staged = 0;
-    sm.failed = 0;
-    if (w1 > w0 && w1 - w0 <= kJcWindow) {
-      const uint64_t base = ((w0 + mis) & ~3ull) - mis;
-      const uint64_t a0 = ((w0 + mis + 3) & ~3ull) - mis, a1 = ((w1 + mis) & ~3ull) - mis;
-      if (a1 > a0 && a1 <= w1) {
-        mbar_init(&sm.bar, 1);
-        const uint32_t bytes = static_cast<uint32_t>((a1 - a0) * 4);
-        mbar_arrive_expect_tx(&sm.bar, bytes);
-        bulk_copy_g2s(&sm.keys[a0 - base], R + a0, bytes, &sm.bar);
-        sm.staged = 2;
-      } else {
-        sm.staged = 1;
-      }
+  if (w1 > w0 && w1 - w0 <= kJcWindow) {
+    const uint64_t base = ((w0 + mis) & ~3ull) - mis;
+    const uint64_t a0 = ((w0 + mis + 3) & ~3ull) - mis, a1 = ((w1 + mis) & ~3ull) - mis;
+    if (a1 > a0 && a1 <= w1) {
+      mbar_init(&sm.bar, 1);
+      const uint32_t bytes = static_cast<uint32_t>((a1 - a0) * 4);
+      mbar_arrive_expect_tx(&sm.bar, bytes);
+      bulk_copy_g2s(&sm.keys[a0 - base], R + a0, bytes, &sm.bar);
+      sm.staged = 2;
+    } else {
+      sm.staged = 1;
     }
   }
-  __syncthreads();
+}
+
+// Lower bound (in R) and match count of L[i0, min(i0 + kJcTile, nl)), given
+// the window that jc_issue_window recorded: every left key of the tile lies
+// in it.  A staged window is searched in shared memory; one that does not
+// fit (a heavy key, or a right side much longer than the left) is searched in
+// global memory with lockstep bounds instead.
+// The tile's counts stay in registers: thread t holds the counts of left
+// keys i0 + 8t .. i0 + 8t + 7 in cnt[] (zero past the end); lower bounds go
+// to lo_out.  Every thread of the block must call it.
+__device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, uint64_t nl,
+                                                const uint32_t* __restrict__ R, uint64_t i0,
+                                                uint32_t* __restrict__ lo_out, uint32_t (&cnt)[kJcKeys],
+                                                JoinCountSmem& sm, DeviceErrors* err) {
+#pragma unroll
+  for (int j = 0; j < kJcKeys; ++j) cnt[j] = 0;
+  const uint32_t tid = threadIdx.x;
+  const uint64_t i_end = (i0 + kJcTile < nl) ? i0 + kJcTile : nl;
+  const uint64_t mis = (reinterpret_cast<uintptr_t>(R) >> 2) & 3u;
   const uint64_t w0 = sm.w0, w1 = sm.w1 > sm.w0 ? sm.w1 : sm.w0;
   const uint32_t staged = sm.staged;
   const uint64_t base = ((w0 + mis) & ~3ull) - mis;
@@ -242,6 +240,33 @@ __device__ __forceinline__ void join_count_tile_regs(const uint32_t* __restrict_
       pkey = key;
     }
   }
+}
+
+// The tile's window: lower bound of its first key and upper bound of its
+// last key in R, found by one warp each (every lane of the warp calls it).
+__device__ __forceinline__ uint64_t jc_window_bound(const uint32_t* __restrict__ L, uint64_t nl,
+                                                    const uint32_t* __restrict__ R, uint64_t nr, uint64_t i0,
+                                                    bool upper) {
+  const uint64_t i_end = (i0 + kJcTile < nl) ? i0 + kJcTile : nl;
+  return upper ? warp_bound<true, uint32_t>(R, 0, nr, L[i_end - 1]) : warp_bound<false, uint32_t>(R, 0, nr, L[i0]);
+}
+
+// jc_count_staged with the window found by the block itself: two warps
+// search R at once, then thread 0 stages the window.
+__device__ __forceinline__ void join_count_tile_regs(const uint32_t* __restrict__ L, uint64_t nl,
+                                                     const uint32_t* __restrict__ R, uint64_t nr, uint64_t i0,
+                                                     uint32_t* __restrict__ lo_out, uint32_t (&cnt)[kJcKeys],
+                                                     JoinCountSmem& sm, DeviceErrors* err) {
+  const uint32_t tid = threadIdx.x;
+  if (tid < 64) {
+    const uint64_t w = jc_window_bound(L, nl, R, nr, i0, tid >= 32);
+    if (tid == 0) sm.w0 = w;
+    if (tid == 32) sm.w1 = w;
+  }
+  __syncthreads();
+  if (tid == 0) jc_issue_window(R, sm.w0, sm.w1, sm);
+  __syncthreads();
+  jc_count_staged(L, nl, R, i0, lo_out, cnt, sm, err);
 }
 
 // Lower bound and match count of every left key of the tile, to lo_out and
