@@ -323,6 +323,13 @@ void vg_ingest_set_hash_bits(int bits);
  * and the call returns VG_ERR_TIMEOUT; the context stays usable. */
 vg_status vg_selfcheck_bounded_wait(vg_ctx* ctx, int which);
 
+/* No reference counterpart, no device use: `pools` threads, each with its own
+ * host worker pool of `threads` threads (as the batch's wave engines have),
+ * run `loops` parallel loops of random sizes and queue background work
+ * between them.  *errors = items that did not run exactly once plus queued
+ * tasks that never ran. */
+vg_status vg_selfcheck_pools(uint32_t pools, uint32_t threads, uint32_t loops, uint64_t* errors);
+
 /* ---- serving (continuous batching) -------------------------------------- */
 typedef struct vg_server vg_server;
 

@@ -205,3 +205,16 @@ def test_oracle_against_live_reference(tmp_path, oracle_built):
         assert m.status == 0 and m.headers == r.headers
         for a, b in zip(m.columns, r.columns):
             np.testing.assert_array_equal(a, b)
+
+
+def test_worker_pools_run_every_item_once(built):
+    """Host worker pools as the batch's wave engines use them (four caller
+    threads, each with its own pool, plus queued background work): every item
+    of every parallel loop runs exactly once and every queued task runs.  No
+    device is used."""
+    import vedas_gb300 as vg
+    L = vg.lib()
+    errors = ctypes.c_uint64(123)
+    assert L.vg_selfcheck_pools(4, 4, 3000, ctypes.byref(errors)) == 0
+    assert errors.value == 0
+    assert L.vg_selfcheck_pools(0, 4, 10, ctypes.byref(errors)) != 0   # invalid arguments

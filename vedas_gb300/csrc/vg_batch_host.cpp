@@ -38,9 +38,11 @@ double since(Clock::time_point t0) {
 // out indices through one atomic counter; the calling thread works too.  A
 // wave has several parallel phases a few hundred microseconds apart, so
 // idle workers poll for the next phase for a while (kSpin polls) before they
-// sleep on the condition variable, and the caller polls for the workers'
+// sleep on the condition variable, and the caller polls for the loop's
 // completion the same way: a sleeping thread takes tens of microseconds to
-// wake, which would add up over the hundreds of phases of a batch.
+// wake, which would add up over the hundreds of phases of a batch.  A loop is
+// complete when all of its items have run; workers busy with queued work
+// (post) join it late or not at all, and it does not wait for them.
 //
 // There is one process-wide pool over all host threads, and one smaller pool
 // per wave engine of a batch: the engines' parallel phases run at the same
@@ -84,22 +86,32 @@ class WorkerPool {
       return;
     }
     std::lock_guard<std::mutex> serial(run_mu_);  // one parallel loop at a time
+    // No worker is inside a loop here (the last one closed with active_ at 0),
+    // so the loop's state can be written before it is opened.
     fn_ = &f;
     n_ = n;
-    next_.store(0, std::memory_order_relaxed);
-    busy_.store(workers_.size(), std::memory_order_relaxed);
+    next_.store(0);
+    done_.store(0);
+    open_.store(true);
     {
       std::lock_guard<std::mutex> lk(mu_);
-      gen_.fetch_add(1, std::memory_order_release);
+      gen_.fetch_add(1);
     }
     cv_.notify_all();
     drain(f, n);
-    for (int i = 0; i < kSpin && busy_.load(std::memory_order_acquire) != 0; ++i) {
+    // The loop ends when every item has run.  Workers that are still busy
+    // with queued work never joined it, and nothing waits for them.
+    for (int i = 0; i < kSpin && done_.load() != n; ++i) {
     }
-    if (busy_.load(std::memory_order_acquire) != 0) {
+    if (done_.load() != n) {
       std::unique_lock<std::mutex> lk(mu_);
-      done_cv_.wait(lk, [&] { return busy_.load(std::memory_order_acquire) == 0; });
+      done_cv_.wait(lk, [&] { return done_.load() == n; });
     }
+    // Close it, then wait for the workers inside to leave (they find no more
+    // items).  A worker that joins after the close sees it closed and leaves
+    // without touching the loop's state.
+    open_.store(false);
+    while (active_.load() != 0) std::this_thread::yield();
     fn_ = nullptr;
     std::exception_ptr e;
     {
@@ -172,6 +184,10 @@ class WorkerPool {
           if (!err_) err_ = std::current_exception();
         }
       }
+      if (done_.fetch_add(e - b) + (e - b) == n) {
+        std::lock_guard<std::mutex> lk(mu_);
+        done_cv_.notify_all();
+      }
     }
   }
 
@@ -227,11 +243,10 @@ class WorkerPool {
       }
       seen = g;
       if (stop_.load()) return;
-      drain(*fn_, n_);
-      if (busy_.fetch_sub(1, std::memory_order_acq_rel) == 1) {
-        std::lock_guard<std::mutex> lk(mu_);
-        done_cv_.notify_all();
-      }
+      // join the loop only while it is open (see run)
+      active_.fetch_add(1);
+      if (open_.load() && gen_.load() == g) drain(*fn_, n_);
+      active_.fetch_sub(1);
     }
   }
 
@@ -241,7 +256,9 @@ class WorkerPool {
   const std::function<void(size_t)>* fn_ = nullptr;   // published by gen_ (release/acquire)
   size_t n_ = 0;
   std::atomic<size_t> next_{0};
-  std::atomic<size_t> busy_{0};
+  std::atomic<size_t> done_{0};     // items of the open loop that have run
+  std::atomic<size_t> active_{0};   // workers inside the open loop
+  std::atomic<bool> open_{false};
   std::atomic<uint64_t> gen_{0};
   std::atomic<bool> stop_{false};
   std::mutex err_mu_;
@@ -886,6 +903,34 @@ void release_later(std::vector<PlannedQuery>& pq) {
         },
         new Range{h, b, std::min(n, b + kRange)});
   }
+}
+
+uint64_t selfcheck_pools(unsigned pools, unsigned threads, unsigned loops) {
+  // one caller thread per pool, as the wave engines use theirs
+  std::atomic<uint64_t> bad{0}, posted{0}, ran{0};
+  std::vector<std::thread> callers;
+  for (unsigned k = 0; k < pools; ++k)
+    callers.emplace_back([&, k] {
+      WorkerPool pool(threads);
+      uint64_t x = 0x9E3779B97F4A7C15ull * (k + 1);
+      for (unsigned it = 0; it < loops; ++it) {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        const size_t n = 1 + x % 4000;
+        std::vector<std::atomic<uint32_t>> hit(n);
+        for (auto& h : hit) h.store(0);
+        pool.run(n, [&](size_t i) { hit[i].fetch_add(1); });
+        for (auto& h : hit) bad += h.load() != 1;
+        if (it % 3 == 0) {   // queued work that the loops must not wait for
+          ++posted;
+          pool.post([](void* a) { static_cast<std::atomic<uint64_t>*>(a)->fetch_add(1); }, &ran);
+        }
+      }
+      pool.drain();
+    });
+  for (auto& t : callers) t.join();
+  return bad.load() + (posted.load() - ran.load());
 }
 
 int key_bits_for(vedas::VedasStorage* storage) {

@@ -182,6 +182,13 @@ struct BatchResult {
 // Bits that hold every id of the storage's index (for WaveEngine's key_bits).
 int key_bits_for(vedas::VedasStorage* storage);
 
+// Host-only self-check of the worker pools: `pools` caller threads, each
+// with its own pool of `threads` threads, run `loops` parallel loops of
+// random sizes and queue work between them.  Returns the number of items
+// that did not run exactly once plus queued tasks that never ran (0 when
+// correct).
+uint64_t selfcheck_pools(unsigned pools, unsigned threads, unsigned loops);
+
 // Runs every query to completion together; per-query failures are recorded
 // in their BatchQuery and do not stop the others.
 // With to_host, every result is also copied to page-locked host memory

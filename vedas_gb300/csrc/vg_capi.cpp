@@ -737,6 +737,11 @@ vg_status vg_selfcheck_bounded_wait(vg_ctx* ctx, int which) {
   return guard([&] { vg::selfcheck_bounded_wait(ctx->c, which); });
 }
 
+vg_status vg_selfcheck_pools(uint32_t pools, uint32_t threads, uint32_t loops, uint64_t* errors) {
+  if (!errors || pools == 0 || pools > 16 || threads == 0 || threads > 32) return VG_ERR_INVALID;
+  return guard([&] { *errors = vg::selfcheck_pools(pools, threads, loops); });
+}
+
 vg_status vg_serve_start(vg_ctx* ctx, vg_index* ix, size_t budget_bytes, vg_server** out) {
   if (!ctx || !ix || !out) return VG_ERR_INVALID;
   *out = nullptr;
