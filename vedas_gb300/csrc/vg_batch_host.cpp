@@ -46,7 +46,8 @@ double since(Clock::time_point t0) {
 //
 // There is one process-wide pool over all host threads, and one smaller pool
 // per wave engine of a batch: the engines' parallel phases run at the same
-// time on disjoint threads (see EnginePools), while planning uses them all.
+// time on disjoint threads (engine_pools, UseEnginePool), while planning uses
+// them all.
 class WorkerPool {
  public:
   // The calling thread's pool: its engine's pool on an engine thread, else
@@ -253,7 +254,7 @@ class WorkerPool {
   std::vector<std::thread> workers_;
   std::mutex mu_, run_mu_;
   std::condition_variable cv_, done_cv_;
-  const std::function<void(size_t)>* fn_ = nullptr;   // published by gen_ (release/acquire)
+  const std::function<void(size_t)>* fn_ = nullptr;   // with n_: read by workers only while open_
   size_t n_ = 0;
   std::atomic<size_t> next_{0};
   std::atomic<size_t> done_{0};     // items of the open loop that have run
