@@ -265,6 +265,9 @@ vg_status vg_batch_download_all(const vg_batch* b, uint32_t* host);
 uint32_t vg_batch_nlog(const vg_batch* b, uint32_t q);
 void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint64_t* p1, uint64_t* p2,
                   uint64_t* p3);
+/* Releases the batch and its results.  The release runs on an idle host
+ * worker after the call returns; vg_ctx_memory, vg_ctx_destroy, vg_index_free
+ * and an allocation that would not fit otherwise wait for it. */
 vg_status vg_batch_free(vg_batch* b);
 
 /* ---- ingest (N-Triples) -------------------------------------------------- */

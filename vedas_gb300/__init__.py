@@ -312,6 +312,20 @@ class Result:
         return recs
 
 
+def _pack_texts(queries):
+    """The queries as a C array of NUL-terminated strings (const char**),
+    built from one joined buffer; the second value keeps the buffer alive."""
+    qb = [q if isinstance(q, bytes) else q.encode() for q in queries]
+    n = len(qb)
+    blob = np.frombuffer(b"\0".join(qb) + b"\0", dtype=np.uint8)
+    lens = np.fromiter(map(len, qb), dtype=np.uint64, count=n)
+    offs = np.zeros(n, dtype=np.uint64)
+    if n > 1:
+        np.cumsum(lens[:-1] + 1, out=offs[1:])
+    ptrs = offs + np.uint64(blob.ctypes.data)
+    return ptrs.ctypes.data_as(ctypes.POINTER(ctypes.c_char_p)), (blob, ptrs)
+
+
 class Batch:
     """Many queries executed together (vg_batch_run)."""
 
@@ -323,7 +337,7 @@ class Batch:
         self.ix = ix
         self.n = len(queries)
         self.to_host = to_host
-        arr = (ctypes.c_char_p * self.n)(*[q if isinstance(q, bytes) else q.encode() for q in queries])
+        arr, self._keep = _pack_texts(queries)
         h = ctypes.c_void_p()
         run = lib().vg_batch_run_host if to_host else lib().vg_batch_run
         check(run(ix.ctx.h, ix.h, arr, self.n, ctypes.byref(h)))
@@ -438,7 +452,7 @@ class Server:
         n = len(queries)
         if n == 0:
             return []
-        arr = (ctypes.c_char_p * n)(*[q if isinstance(q, bytes) else q.encode() for q in queries])
+        arr, keep = _pack_texts(queries)
         out = (ctypes.c_uint64 * n)()
         check(lib().vg_serve_submit_many(self.h, arr, n, out))
         return list(out)

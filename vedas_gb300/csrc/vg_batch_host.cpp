@@ -361,14 +361,19 @@ void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text,
 }
 
 BatchResult::~BatchResult() {
-  // results, headers and logs of thousands of queries are released on the pool
-  pfor(queries.size(), [&](size_t i) {
+  // results, headers and logs of thousands of queries
+  auto release = [&](size_t i) {
     BatchQuery& q = queries[i];
     if (ctx) rel_free(*ctx, q.rel);
     std::vector<std::string>().swap(q.headers);
     std::vector<vedas::ExecuteLogRecord>().swap(q.log);
     std::string().swap(q.error);
-  });
+  };
+  if (serial) {
+    for (size_t i = 0; i < queries.size(); ++i) release(i);
+  } else {
+    pfor(queries.size(), release);
+  }
 }
 
 WaveEngine::WaveEngine(Ctx& ctx, int key_bits) : ctx_(ctx), key_bits_(key_bits) {

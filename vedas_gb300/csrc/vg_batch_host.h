@@ -176,6 +176,9 @@ struct BatchResult {
   uint32_t waves = 0;
   BatchProfile prof;
   std::unique_ptr<HostResults> host;   // with run_batch(..., to_host)
+  // Releases results, headers and logs on the worker pool (one thread when
+  // serial: a queued release runs on one idle worker).
+  bool serial = false;
   ~BatchResult();
 };
 

@@ -590,8 +590,12 @@ void vg_batch_log(const vg_batch* b, uint32_t q, uint32_t i, uint32_t* op, uint6
   if (p3) *p3 = l.param3;
 }
 vg_status vg_batch_free(vg_batch* b) {
-  delete b;
-  return VG_OK;
+  if (!b) return VG_OK;
+  // released by an idle host worker; the context drains such releases before
+  // it is destroyed, before its memory statistics are read, and before its
+  // arena reports that it is out of memory
+  b->r.serial = true;
+  return guard([&] { vg::post_background([](void* p) { delete static_cast<vg_batch*>(p); }, b); });
 }
 
 vg_status vg_ingest_ntriples(vg_ctx* ctx, const char* text, uint64_t len, int literal_dict, uint32_t** s,
