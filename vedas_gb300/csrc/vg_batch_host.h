@@ -94,9 +94,9 @@ void prepare_mirrors(vedas::VedasStorage* storage);
 //     finished);
 //  B: wait for that half, hand finished queries back, allocate the join
 //     outputs and enqueue the join writes.
-// Nothing else waits on the device.  Two engines on one stream, each driven
-// by its own host thread, keep the device busy with one engine's work while
-// the host runs the other's stages.
+// Nothing else waits on the device.  Several engines on one stream, each
+// driven by its own host thread with its own worker pool, keep the device
+// busy with one engine's work while the host runs the others' stages.
 class WaveEngine {
  public:
   // key_bits bounds every relation value (< 2^key_bits), so the segmented

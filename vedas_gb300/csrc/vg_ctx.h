@@ -142,8 +142,8 @@ struct Ctx {
   std::vector<cudaEvent_t> event_pool;
 
   // Guards the host-side state below (statistics, event pool, upload ring,
-  // page-locked pool, download stream) when two threads issue work on the
-  // context's stream at once (the two engines of a batch).  Recursive: a
+  // page-locked pool, download stream) when several threads issue work on
+  // the context's stream at once (the wave engines of a batch).  Recursive: a
   // launch may upload.
   std::recursive_mutex host_mu;
 
