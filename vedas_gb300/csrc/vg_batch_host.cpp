@@ -346,10 +346,10 @@ uint64_t estimate_bytes(vedas::VedasStorage* st, vedas::SparqlQuery& sq) {
 
 void prepare_mirrors(vedas::VedasStorage* storage) { storage->prepareMirrors(); }
 
-void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text, PlannedQuery& pq) {
+void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const char* text, PlannedQuery& pq) {
   guarded(pq.out, [&] {
     pq.ex = std::make_unique<vedas::QueryExecutor>(storage, &ctx);
-    pq.sq = std::make_unique<vedas::SparqlQuery>(text.c_str(), storage->resolver());
+    pq.sq = std::make_unique<vedas::SparqlQuery>(text, storage->resolver());
     std::set<std::string> sel = pq.sq->getSelectedVariables();
     pq.plan = std::make_unique<vedas::QueryPlan>(sel);
     pq.ex->plan(*pq.sq, *pq.plan);
@@ -774,18 +774,18 @@ void HostResults::finish() {
   retire_stages(true);
 }
 
-void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts, BatchResult& out,
+void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts, size_t n, BatchResult& out,
                bool to_host) {
   auto t_all = Clock::now();
   out.ctx = &ctx;
   out.queries.clear();
-  out.queries.resize(texts.size());
+  out.queries.resize(n);
   prepare_mirrors(storage);
-  std::vector<PlannedQuery> pq(texts.size());
+  std::vector<PlannedQuery> pq(n);
   auto t0 = Clock::now();
-  pfor(texts.size(), [&](size_t i) {
+  pfor(n, [&](size_t i) {
     pq[i].out = &out.queries[i];
-    plan_query(ctx, storage, texts[i], pq[i]);
+    plan_query(ctx, storage, texts[i] ? texts[i] : "", pq[i]);
   });
   const double plan_s = since(t0);
   // engines take turns on the stream: while the device runs one engine's

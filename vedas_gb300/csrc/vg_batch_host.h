@@ -74,7 +74,7 @@ struct PlannedQuery {
 
 // Plans one query on the host (thread-safe across queries once the storage's
 // host mirrors exist: see prepare_mirrors).  Errors go to pq.out.
-void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const std::string& text, PlannedQuery& pq);
+void plan_query(Ctx& ctx, vedas::VedasStorage* storage, const char* text, PlannedQuery& pq);
 // Destroys the host state of finished queries (plans with their jobs and
 // intermediate relations, parsed queries, executors) on idle host workers
 // (post_background); the vectors are left empty.  Device memory goes back to
@@ -195,8 +195,9 @@ uint64_t selfcheck_pools(unsigned pools, unsigned threads, unsigned loops);
 // Runs every query to completion together; per-query failures are recorded
 // in their BatchQuery and do not stop the others.
 // With to_host, every result is also copied to page-locked host memory
-// while the batch runs (BatchQuery::host).
-void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const std::vector<std::string>& texts,
-               BatchResult& out, bool to_host = false);
+// while the batch runs (BatchQuery::host).  texts[i] is query i's text (a
+// null pointer reads as an empty query); the texts are read during the call.
+void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts, size_t n, BatchResult& out,
+               bool to_host = false);
 
 }  // namespace vg

@@ -480,12 +480,7 @@ vg_status batch_run(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint3
   if (!ctx || !ix || !out || (nq && !queries)) return VG_ERR_INVALID;
   *out = nullptr;
   auto b = std::make_unique<vg_batch>();
-  vg_status st = guard([&] {
-    std::vector<std::string> texts;
-    texts.reserve(nq);
-    for (uint32_t i = 0; i < nq; ++i) texts.emplace_back(queries[i] ? queries[i] : "");
-    vg::run_batch(ctx->c, ix->st.get(), texts, b->r, to_host);
-  });
+  vg_status st = guard([&] { vg::run_batch(ctx->c, ix->st.get(), queries, nq, b->r, to_host); });
   if (st == VG_OK) *out = b.release();
   return st;
 }
