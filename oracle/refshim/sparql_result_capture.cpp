@@ -3,7 +3,7 @@
 // src/SparqlResult.h:13) is called by QueryPlan::execute with the final IR,
 // which QueryPlan's destructor may free before QueryExecutor::query returns
 // (a select job owns its IR, src/SelectQueryJob.cu:68-72).  This version
-// copies headers and columns out at setResult time so the driver can read the
+// copies headers and columns out at setResult time so refdriver.cpp can read the
 // result after the query; printing is not needed and is a no-op.
 #include "SparqlResult.h"
 

@@ -383,7 +383,7 @@ WaveEngine::WaveEngine(Ctx& ctx, int key_bits) : ctx_(ctx), key_bits_(key_bits) 
 
 namespace {
 // Waits for a stage's event: polls briefly (most stages are nearly done
-// when asked), then sleeps in the driver so that a waiting engine thread
+// when asked), then sleeps in the CUDA driver so that a waiting engine thread
 // leaves its core to the host workers.
 void wait_event(cudaEvent_t ev) {
   for (int i = 0; i < 100; ++i) {
