@@ -590,7 +590,12 @@ vg_status vg_batch_free(vg_batch* b) {
   // it is destroyed, before its memory statistics are read, and before its
   // arena reports that it is out of memory
   b->r.serial = true;
-  return guard([&] { vg::post_background([](void* p) { delete static_cast<vg_batch*>(p); }, b); });
+  return guard([&] {
+    // the page-locked result copies go back to the context's pool at once,
+    // so that the next batch reuses them instead of pinning new memory
+    b->r.host.reset();
+    vg::post_background([](void* p) { delete static_cast<vg_batch*>(p); }, b);
+  });
 }
 
 vg_status vg_ingest_ntriples(vg_ctx* ctx, const char* text, uint64_t len, int literal_dict, uint32_t** s,
