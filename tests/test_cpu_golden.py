@@ -218,3 +218,16 @@ def test_worker_pools_run_every_item_once(built):
     assert L.vg_selfcheck_pools(4, 4, 3000, ctypes.byref(errors)) == 0
     assert errors.value == 0
     assert L.vg_selfcheck_pools(0, 4, 10, ctypes.byref(errors)) != 0   # invalid arguments
+
+
+def test_query_texts_packed_for_the_c_abi(built):
+    """The Python binding hands query texts to the C-ABI as one array of
+    NUL-terminated strings built from a joined buffer: every text, empty and
+    non-ASCII ones included, reads back unchanged."""
+    import vedas_gb300 as vg
+    qs = ["SELECT ?x WHERE { ?x <1> ?y . }", "", "SELECT ?s WHERE { ?s <p> \"é\" . }", b"raw bytes"]
+    arr, keep = vg._pack_texts(qs)
+    for i, q in enumerate(qs):
+        assert arr[i] == (q if isinstance(q, bytes) else q.encode())
+    arr, keep = vg._pack_texts([])
+    assert keep[1].size == 0
