@@ -92,10 +92,34 @@ int main(int argc, char** argv) {
   const size_t used_after_shrink = ar.used();
   ar.free(big);
   const bool oom_ok = ar.try_alloc(cap + 1) == nullptr;
+  // an allocation that does not fit first lets deferred releases run (the
+  // reclaim hook), then retries: here the hook frees a block that fills the slab
+  static vg::Arena* g_ar = nullptr;
+  static void* g_held = nullptr;
+  g_ar = &ar;
+  const size_t lf = ar.largest_free();
+  g_held = ar.alloc(lf);
+  const bool setup_ok = ar.largest_free() < lf;   // a second request of lf bytes cannot fit now
+  vg::set_arena_reclaim([] {
+    if (g_held) g_ar->free(g_held);
+    g_held = nullptr;
+  });
+  bool reclaim_ok = false;
+  try {
+    void* p = ar.alloc(lf);   // fits only after the hook ran
+    reclaim_ok = setup_ok && p != nullptr && g_held == nullptr;
+    ar.free(p);
+  } catch (...) {
+  }
+  vg::set_arena_reclaim(nullptr);
+  const bool peak_ok = ar.peak() >= lf;
   int fails = 0;
   for (int f : failures) fails += f;
-  std::printf("blocks=%zu overlaps_or_out_of_range=%d used_end=%zu shrink_used=%zu oom_ok=%d alloc_failures=%d\n",
-              all.size(), bad, ar.used(), used_after_shrink, oom_ok ? 1 : 0, fails);
-  const bool ok = bad == 0 && ar.used() == 0 && used_after_shrink == (size_t{1} << 20) && oom_ok && fails == 0;
+  std::printf("blocks=%zu overlaps_or_out_of_range=%d used_end=%zu shrink_used=%zu oom_ok=%d alloc_failures=%d "
+              "reclaim_ok=%d peak_ok=%d\n",
+              all.size(), bad, ar.used(), used_after_shrink, oom_ok ? 1 : 0, fails, reclaim_ok ? 1 : 0,
+              peak_ok ? 1 : 0);
+  const bool ok = bad == 0 && ar.used() == 0 && used_after_shrink == (size_t{1} << 20) && oom_ok && fails == 0 &&
+                  reclaim_ok && peak_ok;
   return ok ? 0 : 1;
 }
