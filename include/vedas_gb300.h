@@ -43,6 +43,8 @@ typedef struct vg_ctx vg_ctx;
  * thrust::device_vector allocations of FullRelationIR
  * (src/FullRelationIR.cu:19-31) with one up-front slab. */
 vg_status vg_ctx_create(int device, size_t arena_bytes, vg_ctx** out);
+/* Waits for the context's queued releases, then frees the context.  Indexes,
+ * results, batches and servers made on it must be freed before. */
 vg_status vg_ctx_destroy(vg_ctx* ctx);
 /* Arena accounting: bytes in use, peak, capacity. */
 vg_status vg_ctx_memory(vg_ctx* ctx, size_t* used, size_t* peak, size_t* capacity);
