@@ -335,6 +335,13 @@ vg_status vg_selfcheck_bounded_wait(vg_ctx* ctx, int which);
  * tasks that never ran. */
 vg_status vg_selfcheck_pools(uint32_t pools, uint32_t threads, uint32_t loops, uint64_t* errors);
 
+/* No reference counterpart, no device use: on `graphs` random level-1/level-2
+ * index arrays, `lookups` random (predicate, key) lookups through the
+ * per-predicate level-2 range table give what the reference's searches give
+ * (src/QueryExecutor.cu:596-646), out-of-bounds cases included.
+ * *mismatches = lookups that differ. */
+vg_status vg_selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups, uint64_t* mismatches);
+
 /* ---- serving (continuous batching) -------------------------------------- */
 typedef struct vg_server vg_server;
 

@@ -231,3 +231,16 @@ def test_query_texts_packed_for_the_c_abi(built):
         assert arr[i] == (q if isinstance(q, bytes) else q.encode())
     arr, keep = vg._pack_texts([])
     assert keep[1].size == 0
+
+
+def test_level2_lookup_table_matches_reference_searches(built):
+    """The select lookups through the per-predicate level-2 range table (and
+    the upper bound searched forward from the lower one) give the reference's
+    std::lower_bound / std::upper_bound results on random index arrays, the
+    out-of-bounds cases included.  No device is used."""
+    import vedas_gb300 as vg
+    L = vg.lib()
+    bad = ctypes.c_uint64(1)
+    for seed in (1, 2, 3):
+        assert L.vg_selfcheck_l2_lookup(seed, 200, 400, ctypes.byref(bad)) == 0
+        assert bad.value == 0

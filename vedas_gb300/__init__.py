@@ -130,6 +130,7 @@ def lib():
             "vg_ingest_set_hash_bits": (None, [ctypes.c_int]),
             "vg_selfcheck_bounded_wait": (i32, [vp, ctypes.c_int]),
             "vg_selfcheck_pools": (i32, [u32, u32, u32, ctypes.POINTER(u64)]),
+            "vg_selfcheck_l2_lookup": (i32, [u32, u32, u32, ctypes.POINTER(u64)]),
             "vg_serve_submit_many": (i32, [vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(ctypes.c_uint64)]),
             "vg_serve_wait": (i32, [vp, u64, ctypes.c_double, ctypes.POINTER(i32)]),
             "vg_serve_query_status": (i32, [vp, u64]),

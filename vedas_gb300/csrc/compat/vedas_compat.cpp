@@ -53,16 +53,8 @@ const char* const VedasStorage::kMirrorName[VedasStorage::kMirrors] = {
 void VedasStorage::prepareMirrors() {
   std::call_once(mirrors_once_, [this] {
     for (int m = 0; m < kMirrors; ++m) h(static_cast<Mirror>(m));
-    const TYPEID_HOST_VEC& l1o = *mirror_[kPIdxO];
-    for (int po = 0; po < 2; ++po) {
-      const TYPEID_HOST_VEC& l2o = *mirror_[po ? kPOIdxO : kPSIdxO];
-      std::vector<size_t>& r = l2r_[po];
-      r.resize(l1o.size() + 1);
-      for (size_t s = 0; s <= l1o.size(); ++s) {
-        const TYPEID v = s < l1o.size() ? l1o[s] : static_cast<TYPEID>(ix_.n);
-        r[s] = static_cast<size_t>(std::lower_bound(l2o.begin(), l2o.end(), v) - l2o.begin());
-      }
-    }
+    for (int po = 0; po < 2; ++po)
+      l2r_[po] = QueryExecutor::l2RangesOfL1(*mirror_[kPIdxO], *mirror_[po ? kPOIdxO : kPSIdxO], ix_.n);
   });
 }
 
@@ -431,14 +423,34 @@ std::pair<size_t, size_t> QueryExecutor::findDataOffsetFromL2(const TYPEID_HOST_
   return {s, upper_from(d->data(), s, hi, id2)};
 }
 
+std::vector<size_t> QueryExecutor::l2RangesOfL1(const TYPEID_HOST_VEC& l1o, const TYPEID_HOST_VEC& l2o,
+                                                size_t n) {
+  std::vector<size_t> r(l1o.size() + 1);
+  for (size_t s = 0; s <= l1o.size(); ++s) {
+    const TYPEID v = s < l1o.size() ? l1o[s] : static_cast<TYPEID>(n);
+    r[s] = static_cast<size_t>(std::lower_bound(l2o.begin(), l2o.end(), v) - l2o.begin());
+  }
+  return r;
+}
+
 std::pair<size_t, size_t> QueryExecutor::findDataOffsetForKey(VedasStorage* st, bool po, TYPEID id1, TYPEID id2,
                                                               size_t n) {
   TYPEID_HOST_VEC* l1v = st->getPredicateIndexValues();
   TYPEID_HOST_VEC* l1o = st->getPredicateIndexOffsets();
   TYPEID_HOST_VEC* l2v = po ? st->getPredicateObjectIndexValues() : st->getPredicateSubjectIndexValues();
   TYPEID_HOST_VEC* l2o = po ? st->getPredicateObjectIndexOffsets() : st->getPredicateSubjectIndexOffsets();
-  const std::vector<size_t>& r = st->l2RangeOfL1(po);
-  if (l1v->empty() || l2o->empty() || r.size() != l1o->size() + 1 || n != st->getTripleSize()) {
+  if (n != st->getTripleSize()) {   // the table is made for the triple count
+    auto r1 = findL2OffsetFromL1(l1v, l1o, id1, n);
+    return findDataOffsetFromL2(l2v, l2o, static_cast<TYPEID>(r1.first), static_cast<TYPEID>(r1.second), id2);
+  }
+  return findDataOffsetForKey(l1v, l1o, l2v, l2o, st->l2RangeOfL1(po), id1, id2, n);
+}
+
+std::pair<size_t, size_t> QueryExecutor::findDataOffsetForKey(const TYPEID_HOST_VEC* l1v, const TYPEID_HOST_VEC* l1o,
+                                                              const TYPEID_HOST_VEC* l2v, const TYPEID_HOST_VEC* l2o,
+                                                              const std::vector<size_t>& r, TYPEID id1, TYPEID id2,
+                                                              size_t n) {
+  if (l1v->empty() || l2o->empty() || r.size() != l1o->size() + 1) {
     auto r1 = findL2OffsetFromL1(l1v, l1o, id1, n);
     return findDataOffsetFromL2(l2v, l2o, static_cast<TYPEID>(r1.first), static_cast<TYPEID>(r1.second), id2);
   }
@@ -1185,6 +1197,105 @@ PlanTreeNode* QueryGraph::generateQueryPlan() {
     root = generateJoinPlanForNode(st.first, st.second);
   }
   return root;
+}
+
+// ---------------------------------------------------------------------------
+// Self-check of the index lookups against the reference's searches
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Lookup {
+  bool ub = false;   // the reference would read out of bounds (ReferenceUB)
+  size_t a = 0, b = 0;
+};
+
+template <typename F>
+Lookup run_lookup(F&& f) {
+  Lookup r;
+  try {
+    auto p = f();
+    r.a = p.first;
+    r.b = p.second;
+  } catch (const ReferenceUB&) {
+    r.ub = true;
+  }
+  return r;
+}
+
+// findL2OffsetFromL1 followed by the index form of findDataOffsetFromL2, as
+// the reference writes them (src/QueryExecutor.cu:596-633).
+std::pair<size_t, size_t> reference_key_lookup(const TYPEID_HOST_VEC& l1v, const TYPEID_HOST_VEC& l1o,
+                                               const TYPEID_HOST_VEC& l2v, const TYPEID_HOST_VEC& l2o, TYPEID id1,
+                                               TYPEID id2, size_t n) {
+  if (l1v.empty()) return {0, 0};
+  const size_t s = std::lower_bound(l1v.begin(), l1v.end(), id1) - l1v.begin();
+  if (s >= l1o.size()) throw ReferenceUB("level 1");
+  const size_t lo = l1o[s], hi = (s + 1 == l1o.size()) ? n : l1o[s + 1];
+  if (l2o.empty()) return {0, 0};
+  const size_t b = std::lower_bound(l2o.begin(), l2o.end(), static_cast<TYPEID>(lo)) - l2o.begin();
+  const size_t e = std::lower_bound(l2o.begin(), l2o.end(), static_cast<TYPEID>(hi)) - l2o.begin();
+  const size_t s2 = std::lower_bound(l2v.begin() + b, l2v.begin() + e, id2) - l2v.begin();
+  const size_t e2 = std::upper_bound(l2v.begin() + b, l2v.begin() + e, id2) - l2v.begin();
+  if (s2 >= l2o.size() || e2 >= l2o.size()) throw ReferenceUB("level 2");
+  return {l2o[s2], l2o[e2]};
+}
+
+}  // namespace
+
+uint64_t selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups) {
+  uint64_t x = 0x9E3779B97F4A7C15ull ^ seed;
+  auto rnd = [&x](uint64_t m) {
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    return m ? x % m : 0;
+  };
+  uint64_t bad = 0;
+  for (uint32_t gi = 0; gi < graphs; ++gi) {
+    // predicates with runs of level-2 keys, each key a run of data rows; some
+    // graphs repeat level-2 keys within a predicate, which real indexes never do
+    const bool dups = gi % 4 == 3;
+    const size_t np = rnd(40);
+    TYPEID_HOST_VEC l1v, l1o, l2v, l2o, data;
+    TYPEID pid = 0;
+    for (size_t p = 0; p < np; ++p) {
+      pid += 1 + static_cast<TYPEID>(rnd(3));
+      l1v.push_back(pid);
+      l1o.push_back(static_cast<TYPEID>(data.size()));
+      const size_t nk = 1 + rnd(60);
+      TYPEID key = static_cast<TYPEID>(rnd(5));
+      for (size_t k = 0; k < nk; ++k) {
+        key += (dups && rnd(4) == 0) ? 0 : 1 + static_cast<TYPEID>(rnd(4));
+        l2v.push_back(key);
+        l2o.push_back(static_cast<TYPEID>(data.size()));
+        const size_t rows = 1 + rnd(4);
+        for (size_t r = 0; r < rows; ++r) data.push_back(key);
+      }
+    }
+    const size_t n = data.size();
+    const std::vector<size_t> l2r = QueryExecutor::l2RangesOfL1(l1o, l2o, n);
+    for (uint32_t li = 0; li < lookups; ++li) {
+      const TYPEID id1 = static_cast<TYPEID>(rnd(pid + 3));
+      const TYPEID id2 = static_cast<TYPEID>(rnd(l2v.empty() ? 8 : l2v.back() + 3));
+      const Lookup want = run_lookup([&] { return reference_key_lookup(l1v, l1o, l2v, l2o, id1, id2, n); });
+      const Lookup got = run_lookup(
+          [&] { return QueryExecutor::findDataOffsetForKey(&l1v, &l1o, &l2v, &l2o, l2r, id1, id2, n); });
+      if (want.ub != got.ub || (!want.ub && (want.a != got.a || want.b != got.b))) ++bad;
+      // the data form over a random range of one predicate's rows
+      if (n > 0) {
+        size_t lo = rnd(n + 1), hi = rnd(n + 1);
+        if (lo > hi) std::swap(lo, hi);
+        const size_t ps = l1o.empty() ? 0 : std::upper_bound(l1o.begin(), l1o.end(), lo) - l1o.begin();
+        const size_t pend = ps < l1o.size() ? l1o[ps] : n;   // stay inside one predicate's sorted rows
+        hi = std::min(hi, std::max(lo, pend));
+        const auto d = QueryExecutor::findDataOffsetFromL2(&data, lo, hi, id2);
+        const size_t ws = std::lower_bound(data.begin() + lo, data.begin() + hi, id2) - data.begin();
+        const size_t we = std::upper_bound(data.begin() + lo, data.begin() + hi, id2) - data.begin();
+        if (d.first != ws || d.second != we) ++bad;
+      }
+    }
+  }
+  return bad;
 }
 
 }  // namespace vedas

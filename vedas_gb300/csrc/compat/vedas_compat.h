@@ -466,6 +466,13 @@ class QueryExecutor {
   // storage's per-predicate table; the same result (and the same errors).
   static std::pair<size_t, size_t> findDataOffsetForKey(VedasStorage* st, bool po, TYPEID id1, TYPEID id2,
                                                         size_t n);
+  // The same on plain arrays: l2r is l2RangesOfL1(l1o, l2o, n).
+  static std::pair<size_t, size_t> findDataOffsetForKey(const TYPEID_HOST_VEC* l1v, const TYPEID_HOST_VEC* l1o,
+                                                        const TYPEID_HOST_VEC* l2v, const TYPEID_HOST_VEC* l2o,
+                                                        const std::vector<size_t>& l2r, TYPEID id1, TYPEID id2,
+                                                        size_t n);
+  // Entry s: lower_bound(l2o, l1o[s]); the last entry: lower_bound(l2o, n).
+  static std::vector<size_t> l2RangesOfL1(const TYPEID_HOST_VEC& l1o, const TYPEID_HOST_VEC& l2o, size_t n);
 
   // Execution log of the current query (QueryExecutor::exe_log).
   std::vector<ExecuteLogRecord> exe_log;
@@ -499,5 +506,13 @@ class QueryExecutor {
 struct ReferenceUB : vg::Error {
   explicit ReferenceUB(const std::string& m) : vg::Error(VG_ERR_UNSUPPORTED, m) {}
 };
+
+// Host-only self-check of the index lookups: on random level-1/level-2
+// arrays, QueryExecutor::findDataOffsetForKey (per-predicate table, upper
+// bound searched forward) and the data-form findDataOffsetFromL2 give what the
+// reference's searches give (src/QueryExecutor.cu:596-646: std::lower_bound
+// and std::upper_bound over the whole ranges), errors included.  Returns the
+// number of lookups that differ.
+uint64_t selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups);
 
 }  // namespace vedas

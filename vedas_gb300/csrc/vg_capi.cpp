@@ -741,6 +741,11 @@ vg_status vg_selfcheck_bounded_wait(vg_ctx* ctx, int which) {
   return guard([&] { vg::selfcheck_bounded_wait(ctx->c, which); });
 }
 
+vg_status vg_selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups, uint64_t* mismatches) {
+  if (!mismatches) return VG_ERR_INVALID;
+  return guard([&] { *mismatches = vedas::selfcheck_l2_lookup(seed, graphs, lookups); });
+}
+
 vg_status vg_selfcheck_pools(uint32_t pools, uint32_t threads, uint32_t loops, uint64_t* errors) {
   if (!errors || pools == 0 || pools > 16 || threads == 0 || threads > 32) return VG_ERR_INVALID;
   return guard([&] { *errors = vg::selfcheck_pools(pools, threads, loops); });
