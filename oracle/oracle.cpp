@@ -569,6 +569,8 @@ struct Planner {
   // QueryGraph::mergeEdge (src/QueryGraph.cu:97-117)
   void merge(const std::string end1, const std::string end2) {  // by value: the callers pass elements of a list this mutates
     for (auto l : adj[end2]) {
+      // a self-loop: the reference would erase from the list it walks
+      if (l.first == end2) throw OracleUB("planner: merging a variable joined to itself");
       if (!edge_exists(end1, l.first)) add_edge(end1, l.first, l.second);
       auto& other = adj[l.first];
       for (auto it = other.rbegin(); it != other.rend(); ++it) {
@@ -671,10 +673,16 @@ struct Planner {
         for (auto v : e2->vars) e1->vars.insert(v);
       }
     }
+    // a merge can remove entries of this very list (two patterns between the
+    // same two variables): the reference then reads past its end
+    // (src/QueryGraph.cu:268-274), or erases the list itself (self-loop)
     for (int i = static_cast<int>(L.size()) - 1; i > static_cast<int>(first); --i) {
+      if (static_cast<size_t>(i) >= L.size()) throw OracleUB("planner: a merge removed edges of its own star");
       if (!L[i].second->has(jv)) continue;
+      if (L[i].first == vertex) throw OracleUB("planner: a star merges its own vertex");
       merge(L[first].first, L[i].first);
     }
+    if (first >= L.size()) throw OracleUB("planner: a merge removed edges of its own star");
     L[first].second->iv1 = jv;
     L[first].second->iv2 = "";
     return L[first].second->node;

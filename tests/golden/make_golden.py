@@ -16,6 +16,13 @@ Fixtures:
                 and what the reference code actually returns) plus random
                 update sequences
   plans.json    plans the reference's QueryGraph builds for random estimates
+  plans_multiedge.json
+                plans for random queries over few variables, with patterns that
+                share both variables (several edges between two vertices) and
+                equal estimates: the star-centre choice then falls to the
+                iteration order of the reference's std::unordered_map
+
+  python tests/golden/make_golden.py --only plans_multiedge   # one fixture
 """
 from __future__ import annotations
 
@@ -180,16 +187,60 @@ def gen_plans(td):
     return cases
 
 
+def gen_plans_multiedge(td):
+    """Random basic graph patterns over two to four variables, so that
+    patterns often share both of their variables, with estimates drawn from
+    {5, 7, 1000} (ties).  Queries on which the reference's planner loops
+    forever (a star step that merges nothing) are left out: the oracle's
+    planner reports them, and the reference run is bounded by a timeout."""
+    import ctypes
+    from oracle import oracle_py
+    O = oracle_py.lib()
+    O.vo_plan_describe.restype = ctypes.c_int
+    O.vo_plan_describe.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                   ctypes.c_char_p, ctypes.c_uint64]
+    rng = np.random.Generator(np.random.PCG64(61))
+    names = ["?a", "?b", "?c", "?d"]
+    cases = []
+    while len(cases) < 300:
+        npat = int(rng.integers(2, 6))
+        pats = []
+        for _ in range(npat):
+            nv = int(rng.integers(2, 5))
+            s, o = rng.choice(names[:nv], size=2, replace=False)
+            pats.append(f"{s} <{int(rng.integers(1, 10))}> {o}")
+        q = "SELECT * WHERE { " + " . ".join(pats) + " . }"
+        est = [int(x) for x in rng.choice([5, 5, 7, 1000], size=npat)]
+        e = np.array(est, dtype=np.uint64)
+        buf = ctypes.create_string_buffer(8192)
+        if O.vo_plan_describe(q.encode(), e.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), len(est), buf,
+                              8192) == 0:
+            cases.append({"query": q, "estimates": est})
+    inp = os.path.join(td, "plan_me.in")
+    outp = os.path.join(td, "plan_me.out")
+    with open(inp, "w") as f:
+        for c in cases:
+            f.write(" ".join(str(x) for x in c["estimates"]) + "|" + c["query"] + "\n")
+    subprocess.run([ref_runner.REF_BIN, "plan", inp, outp], check=True, timeout=120)
+    for c, ln in zip(cases, open(outp).read().split("\n")):
+        c["reference_plan"] = ln
+    return cases
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-src", default="/root/reference")
+    ap.add_argument("--only", default=None, help="write only this fixture (its file name without .json)")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref_src}"],
                    check=True)
     with tempfile.TemporaryDirectory() as td:
         for name, fn in (("index", lambda: gen_index(td)), ("queries", lambda: gen_queries(td)),
                          ("c1", lambda: gen_c1(td)), ("eid", lambda: gen_eid(a.ref_src, td)),
-                         ("plans", lambda: gen_plans(td))):
+                         ("plans", lambda: gen_plans(td)),
+                         ("plans_multiedge", lambda: gen_plans_multiedge(td))):
+            if a.only and name != a.only:
+                continue
             data = fn()
             with open(os.path.join(HERE, name + ".json"), "w") as f:
                 json.dump(data, f, separators=(",", ":"))

@@ -146,6 +146,52 @@ def test_planner_matches_reference(oracle_built):
     assert swaps > 0
 
 
+def test_planner_multiedge_ties_match_reference(oracle_built):
+    """Queries whose patterns share both variables (several edges between two
+    vertices) with tied estimates: the star-centre choice falls to the
+    iteration order of the reference's std::unordered_map, and merges reshape
+    the list being walked.  Plans equal the reference's own."""
+    import vedas_gb300 as vg
+    L = vg.lib()
+    L.vg_plan_describe.restype = ctypes.c_int
+    L.vg_plan_describe.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                   ctypes.c_char_p, ctypes.c_size_t]
+    O = oracle_py.lib()
+    O.vo_plan_describe.restype = ctypes.c_int
+    O.vo_plan_describe.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                   ctypes.c_char_p, ctypes.c_uint64]
+    for c in load("plans_multiedge"):
+        est = np.array(c["estimates"], dtype=np.uint64)
+        ep = est.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+        b1 = ctypes.create_string_buffer(8192)
+        b2 = ctypes.create_string_buffer(8192)
+        vg.check(L.vg_plan_describe(c["query"].encode(), ep, len(est), b1, 8192))
+        assert O.vo_plan_describe(c["query"].encode(), ep, len(est), b2, 8192) == 0
+        assert b1.value.decode() == c["reference_plan"], c
+        assert b2.value.decode() == c["reference_plan"], c
+
+
+def test_planner_refuses_merges_the_reference_cannot_do(oracle_built):
+    """A merge that removes edges of the star being walked makes the
+    reference read past a list's end (it aborts on this query): the core
+    refuses the query instead (VG_ERR_UNSUPPORTED), and so does the oracle."""
+    import vedas_gb300 as vg
+    L = vg.lib()
+    L.vg_plan_describe.restype = ctypes.c_int
+    L.vg_plan_describe.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                   ctypes.c_char_p, ctypes.c_size_t]
+    O = oracle_py.lib()
+    O.vo_plan_describe.restype = ctypes.c_int
+    O.vo_plan_describe.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                   ctypes.c_char_p, ctypes.c_uint64]
+    q = b"SELECT * WHERE { ?d <3> ?c . ?c <9> ?b . ?a <7> ?c . ?b <4> ?a . ?b <1> ?a . }"
+    est = np.array([5, 5, 1000, 1000, 5], dtype=np.uint64)
+    ep = est.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    buf = ctypes.create_string_buffer(8192)
+    assert L.vg_plan_describe(q, ep, len(est), buf, 8192) == 5   # VG_ERR_UNSUPPORTED
+    assert O.vo_plan_describe(q, ep, len(est), buf, 8192) == 2   # the oracle's "cannot answer"
+
+
 def test_library_exports_every_declared_symbol(built):
     import vedas_gb300 as vg
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

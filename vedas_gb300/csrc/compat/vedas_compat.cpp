@@ -1074,6 +1074,9 @@ bool QueryGraph::edgeExist(const std::string& a, const std::string& b) {
 
 void QueryGraph::mergeEdge(const std::string end1, const std::string end2) {
   for (auto edge : adjacencyList[end2]) {
+    // a pattern whose subject and object are one variable: the reference
+    // would erase from the list it is walking (src/QueryGraph.cu:101-113)
+    if (edge.first == end2) throw ReferenceUB("planner: merging a variable joined to itself");
     if (!edgeExist(end1, edge.first)) addEdge(end1, edge.first, edge.second);
     auto& other = adjacencyList[edge.first];
     for (auto it = other.rbegin(); it != other.rend(); ++it) {
@@ -1088,24 +1091,23 @@ void QueryGraph::mergeEdge(const std::string end1, const std::string end2) {
 
 std::tuple<size_t, size_t, std::string> QueryGraph::sameMaxDegAndTotalCard(
     std::vector<std::pair<std::string, GraphEdge*>>& links) {
-  std::unordered_map<std::string, size_t> varCount, varEstCard;
+  // One map holds both the reference's varCount and varEstCard: the same keys
+  // go in in the same order, so it iterates in varCount's order, on which the
+  // tie-break depends.
+  std::unordered_map<std::string, std::pair<size_t, size_t>> var;   // count, estimated cardinality
   for (const auto& node : links) {
-    for (const auto& var : node.second->vars) {
-      if (varCount.count(var)) {
-        varCount[var] += 1;
-        varEstCard[var] += node.second->estimateCardinality;
-      } else {
-        varCount[var] = 1;
-        varEstCard[var] = node.second->estimateCardinality;
-      }
+    for (const auto& v : node.second->vars) {
+      auto ins = var.try_emplace(v, 0, 0);
+      ins.first->second.first += 1;
+      ins.first->second.second += node.second->estimateCardinality;
     }
   }
   size_t maxDeg = 0, maxDegMinCard = 0;
   std::string bestVar;
-  for (const auto& v : varCount) {
-    const size_t est = varEstCard[v.first];
-    if (v.second > maxDeg || (v.second == maxDeg && est < maxDegMinCard)) {
-      maxDeg = v.second;
+  for (const auto& v : var) {
+    const size_t deg = v.second.first, est = v.second.second;
+    if (deg > maxDeg || (deg == maxDeg && est < maxDegMinCard)) {
+      maxDeg = deg;
       maxDegMinCard = est;
       bestVar = v.first;
     }
@@ -1179,10 +1181,17 @@ PlanTreeNode* QueryGraph::generateJoinPlanForNode(const std::string& vertex, con
       for (const auto& v : e2->vars) e1->vars.insert(v);
     }
   }
+  // A merge can remove entries of this very list (two patterns between the
+  // same two variables): the reference then reads past the list's end
+  // (src/QueryGraph.cu:268-274), or erases the list itself (a pattern whose
+  // subject and object are one variable).
   for (int i = static_cast<int>(adj.size()) - 1; i > static_cast<int>(first); --i) {
+    if (static_cast<size_t>(i) >= adj.size()) throw ReferenceUB("planner: a merge removed edges of its own star");
     if (!adj[i].second->hasVariable(joinVar)) continue;
+    if (adj[i].first == vertex) throw ReferenceUB("planner: a star merges its own vertex");
     mergeEdge(adj[first].first, adj[i].first);
   }
+  if (first >= adj.size()) throw ReferenceUB("planner: a merge removed edges of its own star");
   adj[first].second->indexVar1 = joinVar;
   adj[first].second->indexVar2 = "";
   return adj[first].second->treeNode;
