@@ -5,12 +5,16 @@ import hashlib
 import json
 import os
 import re
+import subprocess
+import sys
 
 import numpy as np
 import pytest
 
 from oracle import oracle_py
 from vedas_gb300 import workloads
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -290,3 +294,33 @@ def test_level2_lookup_table_matches_reference_searches(built):
     for seed in (1, 2, 3):
         assert L.vg_selfcheck_l2_lookup(seed, 200, 400, ctypes.byref(bad)) == 0
         assert bad.value == 0
+
+
+NULL_CHILD = r'''
+import ctypes, re, sys
+sys.path.insert(0, sys.argv[1])
+import vedas_gb300 as vg
+L = vg.lib()
+src = open(sys.argv[1] + "/vedas_gb300/__init__.py").read()
+for name in re.findall(r'"(vg_[a-z0-9_]+)":\s*\(', src):
+    f = getattr(L, name)
+    args = []
+    for t in (f.argtypes or []):
+        if t in (ctypes.c_double, ctypes.c_float):
+            args.append(0.0)
+        elif t is ctypes.c_char_p or t is ctypes.c_void_p or (isinstance(t, type) and issubclass(t, ctypes._Pointer)):
+            args.append(None)
+        else:
+            args.append(0)
+    print(name, flush=True)
+    f(*args)
+print("all returned")
+'''
+
+
+def test_every_entry_point_survives_null_arguments(built):
+    """Every C-ABI entry point bound by the Python package, called with null
+    handles and pointers and zero sizes, returns (an error status or nothing)
+    instead of crashing; no device is needed for that."""
+    r = subprocess.run([sys.executable, "-c", NULL_CHILD, ROOT], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "all returned" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
