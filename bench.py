@@ -66,6 +66,12 @@ def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pg = None
+    local_world = int(os.environ.get("LOCAL_WORLD_SIZE", str(world)))
+    if local_world > 1 and "VG_HOST_THREADS" not in os.environ:
+        # replicas on one node share its cores: each process's host worker
+        # threads (read once, when the library makes its pools) get a share
+        cpus = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        os.environ["VG_HOST_THREADS"] = str(max(2, cpus // local_world))
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")

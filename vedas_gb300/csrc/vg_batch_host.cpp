@@ -21,6 +21,8 @@
 #include <mutex>
 #include <thread>
 
+#include <sched.h>
+
 #include "vg_batch.h"
 #include "vg_pool.h"
 
@@ -65,9 +67,14 @@ class WorkerPool {
     return p;
   }
   // VG_HOST_THREADS sets the number of host threads of the process-wide pool,
-  // the calling thread included (default: the hardware threads, at most 32).
+  // the calling thread included (default: the CPUs this process may run on,
+  // at most 32).
   static unsigned host_threads() {
     unsigned total = std::thread::hardware_concurrency();
+    cpu_set_t set;
+    CPU_ZERO(&set);
+    if (sched_getaffinity(0, sizeof(set), &set) == 0 && CPU_COUNT(&set) > 0)
+      total = static_cast<unsigned>(CPU_COUNT(&set));
     if (const char* e = std::getenv("VG_HOST_THREADS")) {
       const long v = std::strtol(e, nullptr, 10);
       if (v >= 1) total = static_cast<unsigned>(v);
