@@ -60,6 +60,15 @@ def parse():
     return ap.parse_args()
 
 
+def triples_label(n: int) -> str:
+    """100000000 -> '100M', 200000 -> '200k'."""
+    if n % 1_000_000 == 0:
+        return f"{n // 1_000_000}M"
+    if n % 1_000 == 0:
+        return f"{n // 1_000}k"
+    return str(n)
+
+
 # ---------------------------------------------------------------------------
 def dist_setup(args):
     rank = int(os.environ.get("RANK", "0"))
@@ -239,7 +248,7 @@ def cpu_baseline_run(g, queries, sample: int, steps: int = 1):
 def batch_config(args, nq: int, world: int) -> dict:
     """The workload both arms report (the reference arm times a sample of it)."""
     return {"workload": f"{nq}-query mixed batch (20 star/chain/snowflake templates, "
-                        f"1-8 patterns) on the {args.triples // 1_000_000}M-triple chain graph",
+                        f"1-8 patterns) on the {triples_label(args.triples)}-triple chain graph",
             "mode": "batch", "triples": args.triples, "entities": args.entities, "queries": nq,
             "parallelism": f"replicas{world}", "l2": "inputs larger than L2"}
 
@@ -510,7 +519,7 @@ def bench_serve(args, rank, world, local, pg):
             "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": f"Poisson arrivals at {args.rate:.0f} q/s for {args.duration:.0f} s, "
                                    f"60/30/10 star/chain/snowflake templates, on the "
-                                   f"{args.triples // 1_000_000}M-triple hub graph",
+                                   f"{triples_label(args.triples)}-triple hub graph",
                        "budget_gb": args.budget_gb, "queries": n_q, "failed_or_rejected": rej,
                        "waves": stats["waves"], "peak_inflight": stats["peak_inflight"]},
             "latency_ms": {"p50": 1000 * float(np.percentile(lat, 50)),

@@ -1,10 +1,15 @@
-"""The multi-replica path of bench.py on CPU: two gloo ranks meet only at the
-barriers and in the max/sum reductions of their step times and query counts
-(no collective on the data path)."""
+"""bench.py on CPU: the multi-replica path (two gloo ranks meet only at the
+barriers and in the max/sum reductions of their step times and query counts;
+no collective on the data path), and the reference arm's JSON line."""
+import json
 import os
 import socket
+import subprocess
+import sys
 
 import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _free_port():
@@ -47,3 +52,20 @@ def test_two_replicas_reduce_max_time_and_sum_queries():
     for r in range(2):
         mx, total, w, loc = out[r]
         assert mx == 20.0 and total == 8192.0 and w == 2 and loc == r
+
+
+def test_reference_arm_json_line_on_cpu(built):
+    """bench.py --impl reference runs on the host cores alone: one JSON line
+    with the contract's keys, on the same workload description as the GPU arm."""
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--triples", "200000",
+                        "--entities", "20000", "--queries", "64", "--steps", "1", "--warmup", "1"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "queries/s" and line["value"] > 0
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 1
+    assert "200k-triple chain graph" in line["config"]["workload"]
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
