@@ -4,7 +4,8 @@ itself (oracle/_ref/vedas_ref: the reference's own sources compiled for the
 host, see oracle/Makefile).  Needs the reference sources to build that binary;
 the fixtures it writes are small JSON files that every other machine reads.
 
-  python tests/golden/make_golden.py [--ref-src /path/to/reference]
+  python tests/golden/make_golden.py --ref-src /path/to/reference
+  (or VEDAS_REF_SRC=/path/to/reference python tests/golden/make_golden.py)
 
 Fixtures:
   index.json    sha256 and length of every index array (partial and full)
@@ -229,9 +230,12 @@ def gen_plans_multiedge(td):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default="/root/reference")
+    ap.add_argument("--ref-src", default=os.environ.get("VEDAS_REF_SRC"),
+                    help="the reference checkout (default: $VEDAS_REF_SRC; required)")
     ap.add_argument("--only", default=None, help="write only this fixture (its file name without .json)")
     a = ap.parse_args()
+    if not a.ref_src:
+        ap.error("give the reference checkout with --ref-src or VEDAS_REF_SRC")
     subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={a.ref_src}"],
                    check=True)
     with tempfile.TemporaryDirectory() as td:

@@ -231,6 +231,7 @@ __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
     if (first + k < g.nl) offs[g.row0 + first + k] = run;
     run += cnt[k];
   }
+  if (threadIdx.x == 0) jc_drain_window(sm, err);
 }
 
 struct JoinOut {

@@ -15,6 +15,7 @@
 #include <atomic>
 #include <condition_variable>
 #include <cstdlib>
+#include <cstring>
 #include <deque>
 #include <exception>
 #include <functional>
@@ -599,7 +600,8 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
   const size_t c0_words = (col0_words(swap_rels) + 1) / 2;
   off_tot_ = 0;
   off_fin_ = off_tot_ + jl.size();
-  off_c0_ = off_fin_ + fin_seg_.size();
+  off_err_ = off_fin_ + fin_seg_.size();
+  off_c0_ = off_err_ + 1;
   uint64_t* ha = h_a_.reserve(off_c0_ + c0_words + 1);
   bool any = false;
   if (!to_sort.empty()) {
@@ -616,6 +618,10 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
   }
   if (!jl.empty()) {
     batched_join_count(ctx_, jl, jr, jb_, ha + off_tot_);
+    // the device error record comes back with the totals: a look-back that
+    // gave up leaves the offsets wrong, and stage B must then not write
+    VG_CUDA(cudaMemcpyAsync(ha + off_err_, ctx_.d_err, sizeof(DeviceErrors), cudaMemcpyDeviceToHost,
+                            ctx_.stream));
     any = true;
   }
   if (!fin_seg_.empty()) {
@@ -691,6 +697,9 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   // device half 2: join outputs
   t0 = Clock::now();
   if (!joins_.empty()) {
+    DeviceErrors he;
+    std::memcpy(&he, ha + off_err_, sizeof(he));
+    if (he.timeout) ctx_.raise_device_errors(he);
     const uint64_t* tot = ha + off_tot_;
     std::vector<const Rel*> small;
     std::vector<size_t> who;

@@ -164,7 +164,7 @@ class WaveEngine {
   std::vector<vedas::FullRelationIR*> fin_res_;
   // device -> host results of each stage and the events that mark them
   PinnedWords h_a_{ctx_}, h_b_{ctx_};
-  size_t off_tot_ = 0, off_fin_ = 0, off_c0_ = 0;   // words into h_a_
+  size_t off_tot_ = 0, off_fin_ = 0, off_c0_ = 0, off_err_ = 0;   // words into h_a_
   size_t off_fl_ = 0, off_jc0_ = 0;                               // words into h_b_
   cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;
   bool a_pending_ = false, b_pending_ = false;

@@ -329,7 +329,7 @@ vg_status vg_join2(vg_ctx* ctx, const vg_ir* l, const vg_ir* r, vg_ir* out) {
     vg::Rel o;
     vg::join(ctx->c, to_rel(l), to_rel(r), true, o);
     from_rel(o, out);
-    ctx->c.sync();
+    ctx->c.check_device_errors();
   });
 }
 

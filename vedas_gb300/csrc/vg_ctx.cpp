@@ -434,6 +434,10 @@ void Ctx::check_device_errors() {
   DeviceErrors h{};
   VG_CUDA(cudaMemcpyAsync(&h, d_err, sizeof(h), cudaMemcpyDeviceToHost, stream));
   sync();
+  raise_device_errors(h);
+}
+
+void Ctx::raise_device_errors(const DeviceErrors& h) {
   if (h.timeout || h.overflow) {
     VG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(DeviceErrors), stream));
     if (h.timeout) fail(VG_ERR_TIMEOUT, "a bounded device wait expired");

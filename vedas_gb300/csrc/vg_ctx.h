@@ -201,6 +201,9 @@ struct Ctx {
   void sync() { VG_CUDA(cudaStreamSynchronize(stream)); }
   // Raises VG_ERR_TIMEOUT / VG_ERR_OVERFLOW if a kernel recorded one (syncs).
   void check_device_errors();
+  // The same for a copy of the record the caller already read back: clears
+  // the device record and raises when `h` holds an error.
+  void raise_device_errors(const DeviceErrors& h);
 };
 
 // RAII scratch buffer from the arena.

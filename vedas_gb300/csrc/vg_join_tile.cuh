@@ -242,6 +242,14 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
   }
 }
 
+// Called by one thread after the block's last use of the window: a bulk copy
+// whose wait gave up may still be in flight into this block's shared memory,
+// and must land before the block exits (bounded again; a copy that still has
+// not landed is recorded as one more timeout).
+__device__ __forceinline__ void jc_drain_window(JoinCountSmem& sm, DeviceErrors* err) {
+  if (sm.staged == 2 && sm.failed) (void)mbar_wait_bounded(&sm.bar, 0, err);
+}
+
 // The tile's window: lower bound of its first key and upper bound of its
 // last key in R, found by one warp each (every lane of the warp calls it).
 __device__ __forceinline__ uint64_t jc_window_bound(const uint32_t* __restrict__ L, uint64_t nl,

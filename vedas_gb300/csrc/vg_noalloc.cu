@@ -67,8 +67,8 @@ extern "C" vg_status vg_join_noalloc(const uint32_t* const* l_cols, uint32_t l_n
                                      const uint32_t* const* r_cols, uint32_t r_ncols, uint64_t r_rows,
                                      uint32_t* const* out_cols, uint64_t out_capacity, uint64_t* out_rows,
                                      void* stream) {
-  if (!l_cols || !r_cols || !out_rows || l_ncols == 0 || r_ncols == 0 ||
-      l_ncols + r_ncols - 1 > VG_MAX_COLS || (out_capacity && !out_cols))
+  if (!l_cols || !r_cols || !out_rows || l_ncols == 0 || r_ncols == 0 || l_ncols > VG_MAX_COLS ||
+      r_ncols > VG_MAX_COLS || l_ncols + r_ncols - 1 > VG_MAX_COLS || (out_capacity && !out_cols))
     return VG_ERR_INVALID;
   *out_rows = 0;
   if (l_rows > kMaxLeftRows) {

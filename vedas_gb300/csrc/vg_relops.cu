@@ -2,6 +2,8 @@
 // join (count -> scan -> load-balanced write), gathers and relation sorts.
 #include "vg_relops.h"
 
+#include <cstring>
+
 #include <algorithm>
 
 #include "vg_join_tile.cuh"
@@ -179,6 +181,7 @@ __global__ void __launch_bounds__(kJcBlock, 4) join_count_tiled_kernel(const uin
                                                                     uint32_t* __restrict__ cnt, DeviceErrors* err) {
   __shared__ JoinCountSmem sm;
   join_count_tile(L, nl, R, nr, static_cast<uint64_t>(blockIdx.x) * kJcTile, lo, cnt, sm, err);
+  if (threadIdx.x == 0) jc_drain_window(sm, err);
 }
 
 // Exclusive scan of uint32 counts into uint64 offsets (+ total).
@@ -384,9 +387,17 @@ void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
         cnt.get(), offs.get(), l.nrows, status.get(), ticket.get(), total.get(), tiles, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
+  // the total and the error record come back together: a look-back that gave
+  // up leaves the offsets wrong, and the write must then not run
   VG_CUDA(cudaMemcpyAsync(ctx.h_small, total.get(), sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  VG_CUDA(cudaMemcpyAsync(ctx.h_small + 1, ctx.d_err, sizeof(DeviceErrors), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.sync();
   const uint64_t t = ctx.h_small[0];
+  {
+    DeviceErrors he;
+    std::memcpy(&he, ctx.h_small + 1, sizeof(he));
+    ctx.raise_device_errors(he);
+  }
   if (t > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
   out = rel_alloc(ctx, ncols, t);
   if (t == 0) return;
@@ -412,17 +423,20 @@ uint64_t join_into(cudaStream_t stream, int num_sms, const Rel& l, const Rel& r,
   (void)num_sms;
   if (l.nrows == 0 || r.nrows == 0) return 0;
   const uint32_t ncols = l.ncols + r.ncols - 1;
-  KeyOf<false> kl{l.cols[0], nullptr}, kr{r.cols[0], nullptr};
-  join_count_kernel<false><<<static_cast<unsigned>(div_up(l.nrows, kBlock)), kBlock, 0, stream>>>(
-      kl, l.nrows, kr, r.nrows, lo, cnt);
+  join_count_tiled_kernel<<<static_cast<unsigned>(div_up(l.nrows, kJcTile)), kJcBlock, 0, stream>>>(
+      l.cols[0], l.nrows, r.cols[0], r.nrows, lo, cnt, err);
   VG_CUDA(cudaGetLastError());
   const uint64_t tiles = div_up(l.nrows, kTileRows);
   scan_counts_kernel<<<static_cast<unsigned>(tiles), kBlock, 0, stream>>>(cnt, offs, l.nrows, status, ticket,
                                                                          total, tiles, err);
   VG_CUDA(cudaGetLastError());
   uint64_t t = 0;
+  DeviceErrors he{};
   VG_CUDA(cudaMemcpyAsync(&t, total, sizeof(uint64_t), cudaMemcpyDeviceToHost, stream));
+  VG_CUDA(cudaMemcpyAsync(&he, err, sizeof(he), cudaMemcpyDeviceToHost, stream));
   VG_CUDA(cudaStreamSynchronize(stream));
+  // a look-back that gave up leaves the offsets wrong: no write then
+  if (he.timeout) fail(VG_ERR_TIMEOUT, "join_into: a bounded device wait expired");
   if (t == 0 || t > capacity) return t;
   JoinWriteArgs a{};
   a.offs = offs;
