@@ -183,7 +183,7 @@ def make_workload(args, rank: int):
     g = workloads.graph_chain(n=args.triples, n_entities=args.entities, seed=args.seed)
     cs = workloads.ConstantSampler(g)
     queries = workloads.query_mix(g, args.queries, seed=args.seed + 1000 * rank, cs=cs)
-    return g, queries
+    return g, queries, cs
 
 
 def run_plain(ix, queries, download=False):
@@ -256,7 +256,7 @@ def batch_config(args, nq: int, world: int) -> dict:
 def bench_reference(args, rank, world, pg):
     if rank != 0:
         return
-    g, queries = make_workload(args, 0)
+    g, queries, _ = make_workload(args, 0)
     n, times, cores = cpu_baseline_run(g, queries, args.cpu_sample, steps=args.warmup + args.steps)
     timed = times[args.warmup:] if len(times) > args.warmup else times
     total = sum(timed)
@@ -312,8 +312,9 @@ def bench_ingest(args, ctx, g):
 def bench_ours(args, rank, world, local, pg):
     import torch
     import vedas_gb300 as vg
+    from vedas_gb300 import workloads as wl
 
-    g, queries = make_workload(args, rank)
+    g, queries, cs = make_workload(args, rank)
     ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
     t0 = time.perf_counter()
     ix = vg.Index(ctx, g.s, g.p, g.o)
@@ -337,8 +338,7 @@ def bench_ours(args, rank, world, local, pg):
     ingest = bench_ingest(args, ctx, g) if args.ingest_triples > 0 else None
     chain = None
     try:
-        from vedas_gb300 import workloads as wl
-        cq = wl.chain_query(g)
+        cq = wl.chain_query(g, cs=cs)
         ix.query(cq).close()
         ts = []
         for _ in range(5):
@@ -347,15 +347,21 @@ def bench_ours(args, rank, world, local, pg):
             r = ix.query(cq)
             ts.append(time.perf_counter() - t1)
             rows = r.nrows
+            log = r.log()
             r.close()
-        chain = {"query": cq, "rows": rows, "ms_min": 1000 * min(ts), "ms_median": 1000 * float(np.median(ts))}
+        chain = {"query": cq, "rows": rows, "ms_min": 1000 * min(ts), "ms_median": 1000 * float(np.median(ts)),
+                 "log": [list(x) for x in log]}
     except vg.VgError as e:
         chain = {"error": str(e)}
     # The core refuses queries on which the reference itself would read out of
     # bounds or trip an assert; drop those before timing (counted below).
     b = vg.Batch(ix, queries)
     kept = [q for i, q in enumerate(queries) if b.status(i) == 0]
+    qrows = b.rows()
     b.close()
+    # share of each template's instances that return rows
+    nt = len(wl.TEMPLATES)
+    nonempty = [round(float(np.mean([qrows[i] > 0 for i in range(k, len(queries), nt)])), 3) for k in range(nt)]
     refused = len(queries) - len(kept)
     run = run_batch if args.mode == "batch" else run_plain
     # the batch API takes UTF-8 query text; encode it once, as a client would
@@ -438,7 +444,9 @@ def bench_ours(args, rank, world, local, pg):
             "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (seeded generator, no dataset)",
             "config": dict(batch_config(args, len(kept), world), mode=args.mode, queries_refused=refused,
-                           result_rows_per_step=rows // max(args.steps, 1), index_build_s=round(build_s, 3)),
+                           result_rows_per_step=rows // max(args.steps, 1), index_build_s=round(build_s, 3),
+                           template_nonempty_share=nonempty),
+            "result_rows_per_s": rows / max(args.steps, 1) / (step_ms_max / 1000.0),
             "roofline": roof,
             "plain_per_query": plain,
             "speedup_vs_plain": value / (world * plain["queries_per_s"]),

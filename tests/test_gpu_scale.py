@@ -24,32 +24,63 @@ def _same(res, ref):
         np.testing.assert_array_equal(a, b)
 
 
-def test_c2_100m_index_chain_and_batch_match_oracle(big_ctx):
+@pytest.fixture(scope="module")
+def c2(big_ctx):
+    """The 100M-triple chain graph (seed 0), its index on the device and the
+    oracle's on the host, and the constant sampler the bench uses."""
     import vedas_gb300 as vg
     g = workloads.graph_chain()                      # 100M triples, seed 0
     ix = vg.Index(big_ctx, g.s, g.p, g.o)
     ox = oracle_py.OracleIndex(g.s, g.p, g.o)
+    cs = workloads.ConstantSampler(g)
+    yield g, ix, ox, cs
+    ix.close()
+
+
+def test_c2_100m_index_matches_oracle(c2):
+    g, ix, ox, _ = c2
     for name in ("p_idx_values", "p_idx_offsets", "ps_s_idx_values", "ps_idx_offsets", "po_o_idx_values",
                  "po_idx_offsets", "ps_data", "po_data", "pso_data", "pos_data"):
         np.testing.assert_array_equal(ix.array(name), ox.array(name), err_msg=name)
-    q = workloads.chain_query(g)                     # ?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 c
+
+
+def test_c2_100m_chain_query_matches_oracle(c2):
+    g, ix, ox, cs = c2
+    q = workloads.chain_query(g, cs=cs)              # ?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 c
     r = ox.query(q)
-    assert r.status == 0
+    assert r.status == 0 and r.nrows > 0             # c ends a path that exists
     res = ix.query(q)
     _same(res, r)
-    assert [x[0] for x in res.log()].count("SWAP") >= 2          # index swaps between the joins
-    qs = workloads.query_mix(g, 96, seed=3)
+    log = res.log()
+    assert [x[:4] for x in log] == [tuple(x[:4]) for x in r.log]
+    # index swaps between the joins, on relations of at least a million rows
+    assert sum(1 for x in log if x[0] == "SWAP" and x[1] >= 1_000_000) >= 2
+
+
+def test_c2_100m_whole_bench_batch_matches_oracle(c2):
+    """Every query of the bench's 4096-query batch (same generator, seed and
+    sampler): status, headers, rows in order and execution log."""
+    import vedas_gb300 as vg
+    g, ix, ox, cs = c2
+    qs = workloads.query_mix(g, 4096, seed=0, cs=cs)
     b = vg.Batch(ix, qs)
+    nonempty = [0] * len(workloads.TEMPLATES)
     for i, qq in enumerate(qs):
         rr = ox.query(qq)
         if rr.status != 0:
-            assert b.status(i) != 0
+            assert b.status(i) != 0, qq
             continue
-        assert b.headers(i) == rr.headers
-        for x, y in zip(b.columns(i), rr.columns):
-            np.testing.assert_array_equal(x, y)
+        assert b.status(i) == 0, (qq, b.error(i))
+        assert b.headers(i) == rr.headers, qq
+        cols = b.columns(i)
+        assert len(cols) == len(rr.columns)
+        for x, y in zip(cols, rr.columns):
+            np.testing.assert_array_equal(x, y, err_msg=qq)
+        assert [x[:4] for x in b.log(i)] == [tuple(x[:4]) for x in rr.log], qq
+        nonempty[i % len(workloads.TEMPLATES)] += rr.nrows > 0
     b.close()
-    ix.close()
+    per = len(qs) // len(workloads.TEMPLATES)
+    assert min(nonempty) >= per // 2, nonempty       # every template mostly returns rows
 
 
 def _gpu_dedup(g):

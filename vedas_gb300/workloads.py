@@ -133,11 +133,12 @@ def graph_chain(n: int = 100_000_000, n_entities: int = 2_000_000, n_predicates:
 
 # ---------------------------------------------------------------------------
 # Query templates: star (S), chain (C) and snowflake (F), 1-8 patterns.
-# Placeholders: P<k> a predicate, O<k> an existing object of P<k>,
-# S<k> an existing subject of P<k>.  Variable-only patterns draw their
-# predicate from the rarer half of the ranks to bound result sizes; the
-# globally-last predicate is never used (the reference's own lookups read past
-# its index there, so no workload sends it).
+# Placeholders: P<k> a predicate, O<k> an object and S<k> a subject constant.
+# instantiate() fills them along a path that exists in the graph, so every
+# query has at least one answer.  Variable-only patterns take predicates from
+# the rarer half of the ranks to bound result sizes; the globally-last
+# predicate is never used (the reference's own lookups read past its index
+# there, so no workload sends it).
 # ---------------------------------------------------------------------------
 TEMPLATES = [
     ("S", "SELECT ?x WHERE { ?x P1 O1 . }"),
@@ -164,49 +165,217 @@ TEMPLATES = [
 ]
 
 
+def _packed_order(keys: np.ndarray):
+    """(sorted keys, original positions) of a uint32 array: a stable sort done
+    as one sort of (key << 32 | position) words, several times faster than a
+    stable argsort."""
+    n = keys.shape[0]
+    if n >= (1 << 32):
+        order = np.argsort(keys, kind="stable")
+        return keys[order], order
+    w = (keys.astype(np.uint64) << np.uint64(32)) | np.arange(n, dtype=np.uint64)
+    w.sort()
+    return (w >> np.uint64(32)).astype(np.uint32), (w & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+
+
 class ConstantSampler:
-    """Per-predicate subjects/objects of a graph, for sampling query constants."""
+    """A graph's triples grouped by predicate, subject and object, for drawing
+    query constants along paths that exist in the graph."""
 
     def __init__(self, g: Graph):
-        order = np.argsort(g.p, kind="stable")
-        self.p_sorted = g.p[order]
-        self.s_sorted = g.s[order]
-        self.o_sorted = g.o[order]
+        self.g = g
+        self.p_sorted, self.p_pos = _packed_order(g.p)
         self.preds = np.unique(self.p_sorted)
         self.start = np.searchsorted(self.p_sorted, self.preds, side="left")
         self.end = np.searchsorted(self.p_sorted, self.preds, side="right")
         self.count = {int(p): int(e - b) for p, b, e in zip(self.preds, self.start, self.end)}
         self.span = {int(p): (int(b), int(e)) for p, b, e in zip(self.preds, self.start, self.end)}
+        self._by_s = None
+        self._by_o = None
 
     def usable_predicates(self):
         return [int(p) for p in self.preds[:-1]]   # never the last predicate id
 
-    def obj(self, rng, p: int) -> int:
+    def by_subject(self):
+        if self._by_s is None:
+            self._by_s = _packed_order(self.g.s)
+        return self._by_s
+
+    def by_object(self):
+        if self._by_o is None:
+            self._by_o = _packed_order(self.g.o)
+        return self._by_o
+
+    def out_edges(self, node: int):
+        """Positions of the triples whose subject is `node`."""
+        keys, pos = self.by_subject()
+        k = np.uint32(node)      # a uint32 key: a Python int would convert the whole array
+        return pos[keys.searchsorted(k, "left"):keys.searchsorted(k, "right")]
+
+    def in_edges(self, node: int):
+        """Positions of the triples whose object is `node`."""
+        keys, pos = self.by_object()
+        k = np.uint32(node)
+        return pos[keys.searchsorted(k, "left"):keys.searchsorted(k, "right")]
+
+    def has_out(self, node: int) -> bool:
+        keys, _ = self.by_subject()
+        i = keys.searchsorted(np.uint32(node), "left")
+        return bool(i < keys.shape[0] and keys[i] == node)
+
+    def has_in(self, node: int) -> bool:
+        keys, _ = self.by_object()
+        i = keys.searchsorted(np.uint32(node), "left")
+        return bool(i < keys.shape[0] and keys[i] == node)
+
+    def triple_of(self, rng, p: int) -> int:
+        """Position of a uniformly drawn triple of predicate p."""
         b, e = self.span[p]
-        return int(self.o_sorted[rng.integers(b, e)])
+        return int(self.p_pos[rng.integers(b, e)])
+
+    def obj(self, rng, p: int) -> int:
+        return int(self.g.o[self.triple_of(rng, p)])
 
     def subj(self, rng, p: int) -> int:
-        b, e = self.span[p]
-        return int(self.s_sorted[rng.integers(b, e)])
+        return int(self.g.s[self.triple_of(rng, p)])
+
+
+def _patterns(template: str):
+    body = template.split("{", 1)[1].rsplit("}", 1)[0]
+    return [tuple(t.strip().rstrip(" .").split()) for t in body.split(" . ") if t.strip()]
+
+
+def _walk_order(pats):
+    """Pattern order for a walk: each pattern after the first shares a
+    variable with one placed before it (the templates are trees)."""
+    order, seen = [0], {v for v in (pats[0][0], pats[0][2]) if v.startswith("?")}
+    while len(order) < len(pats):
+        for i, (s, _, o) in enumerate(pats):
+            if i not in order and (s in seen or o in seen):
+                order.append(i)
+                seen.update(v for v in (s, o) if v.startswith("?"))
+                break
+        else:
+            raise ValueError("template patterns are not connected")
+    return order
+
+
+_TRIES_PER_EDGE = 64
+_TRIES_PER_QUERY = 200
+
+
+def _walk(pats, cs: ConstantSampler, rng, pools):
+    """One embedding of the patterns in the graph: a triple for every
+    pattern, consistent on shared variables, found by a random walk from a
+    random triple of the first pattern.  pools[i] is the set of predicates
+    pattern i may use.  Returns {pattern: triple position} or None."""
+    g = cs.g
+    order = _walk_order(pats)
+    subj_of = {}
+    obj_of = {}
+    for i, (s, _, o) in enumerate(pats):
+        if s.startswith("?"):
+            subj_of.setdefault(s, []).append(i)
+        if o.startswith("?"):
+            obj_of.setdefault(o, []).append(i)
+
+    def fits(i, t, assign):
+        """Triple t for pattern i: its predicate is allowed and every variable
+        it binds afresh can continue the walk (edges out of it where a later
+        pattern has it as subject, edges into it where as object)."""
+        if int(g.p[t]) not in pools[i]:
+            return False
+        s, _, o = pats[i]
+        for v, node in ((s, int(g.s[t])), (o, int(g.o[t]))):
+            if not v.startswith("?"):
+                continue
+            if v in assign:
+                if assign[v] != node:
+                    return False
+                continue
+            if any(j != i for j in subj_of.get(v, ())) and not cs.has_out(node):
+                return False
+            if any(j != i for j in obj_of.get(v, ())) and not cs.has_in(node):
+                return False
+        if s.startswith("?") and s == o and int(g.s[t]) != int(g.o[t]):
+            return False
+        return True
+
+    def pick(i, cand, assign, taken):
+        """A fitting triple among cand, preferring a predicate that no
+        placed pattern at the same variable uses (stars then look like the
+        benchmark suites' ones: one predicate per branch)."""
+        m = cand.shape[0]
+        if m == 0:
+            return None
+        idx = rng.permutation(m)[:_TRIES_PER_EDGE] if m <= 4 * _TRIES_PER_EDGE \
+            else rng.integers(0, m, size=_TRIES_PER_EDGE)
+        second = None
+        for k in idx:
+            t = int(cand[k])
+            if fits(i, t, assign):
+                if int(g.p[t]) not in taken:
+                    return t
+                if second is None:
+                    second = t
+        return second
+
+    for _ in range(_TRIES_PER_QUERY):
+        assign, chosen = {}, {}
+        for i in order:
+            s, _, o = pats[i]
+            if s in assign:
+                taken = {int(g.p[chosen[j]]) for j in chosen if pats[j][0] == s}
+                t = pick(i, cs.out_edges(assign[s]), assign, taken)
+            elif o in assign:
+                taken = {int(g.p[chosen[j]]) for j in chosen if pats[j][2] == o}
+                t = pick(i, cs.in_edges(assign[o]), assign, taken)
+            else:
+                pool = sorted(pools[i])
+                t = None
+                for _ in range(_TRIES_PER_EDGE):
+                    p = pool[rng.integers(0, len(pool))]
+                    c = cs.triple_of(rng, p)
+                    if fits(i, c, assign):
+                        t = c
+                        break
+            if t is None:
+                break
+            chosen[i] = t
+            if s.startswith("?"):
+                assign[s] = int(g.s[t])
+            if o.startswith("?"):
+                assign[o] = int(g.o[t])
+        else:
+            return chosen
+    return None
 
 
 def instantiate(template: str, cs: ConstantSampler, rng) -> str:
-    """Fills a template's placeholders with predicates and existing constants."""
+    """Fills a template's placeholders along a path of the graph: every
+    pattern gets the predicate and constants of one triple, and the triples
+    agree on every shared variable, so the query has at least that answer.
+    Patterns whose ends are both variables take predicates from the rarer
+    half of the ranks, which bounds result sizes; the globally-last predicate
+    is never used (the reference's own lookups read past its index there, so
+    no workload sends it)."""
     preds = cs.usable_predicates()
-    rare = preds[len(preds) // 2:] or preds
-    pats = [t.strip() for t in template.split("{", 1)[1].rsplit("}", 1)[0].split(" . ") if t.strip()]
-    chosen = {}
-    for t in pats:
-        s, p, o = t.rstrip(" .").split()
-        k = p[1:]
-        bound = not (s.startswith("?") and o.startswith("?"))
-        pool = preds if bound else rare
-        chosen[k] = int(pool[rng.integers(0, len(pool))])
+    rare = set(preds[len(preds) // 2:] or preds)
+    every = set(preds)
+    pats = _patterns(template)
+    pools = [rare if (s.startswith("?") and o.startswith("?")) else every for s, _, o in pats]
+    chosen = _walk(pats, cs, rng, pools)
+    if chosen is None:
+        # no embedding found: constants drawn per pattern (may have no answer)
+        chosen = {i: cs.triple_of(rng, sorted(pools[i])[rng.integers(0, len(pools[i]))])
+                  for i in range(len(pats))}
     out = template
-    for k in sorted(chosen, key=lambda x: -int(x)):
-        p = chosen[k]
-        out = out.replace(f"O{k}", f"<{cs.obj(rng, p)}>").replace(f"S{k}", f"<{cs.subj(rng, p)}>")
-        out = out.replace(f"P{k}", f"<{p}>")
+    g = cs.g
+    for i in sorted(chosen, key=lambda i: -int(pats[i][1][1:])):
+        k = pats[i][1][1:]
+        t = chosen[i]
+        out = out.replace(f"O{k}", f"<{int(g.o[t])}>").replace(f"S{k}", f"<{int(g.s[t])}>")
+        out = out.replace(f"P{k}", f"<{int(g.p[t])}>")
     return out
 
 
@@ -288,13 +457,19 @@ def star_query(pa: int = 3, pb: int = 7) -> str:
     return f"SELECT * WHERE {{ ?x <{pa}> ?a . ?x <{pb}> ?b . }}"
 
 
-def chain_query(g: Graph, preds=(1, 2, 5, 9), seed: int = 0) -> str:
-    """Four-pattern chain (?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 c), where c is
-    a sampled existing object of the last predicate."""
+def chain_query(g: Graph, preds=(1, 2, 5, 9), seed: int = 0, cs: ConstantSampler | None = None) -> str:
+    """Four-pattern chain (?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 c), where c
+    is the end of a four-hop path p1, p2, p5, p9 that exists in the graph (so
+    the query has at least one answer)."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    objs = g.o[g.p == preds[-1]]
-    c = int(objs[rng.integers(0, objs.shape[0])])
+    cs = cs or ConstantSampler(g)
     a, b, cc, d = preds
+    pats = [("?a", "P1", "?b"), ("?b", "P2", "?c"), ("?c", "P3", "?d"), ("?d", "P4", "O4")]
+    chosen = _walk(pats, cs, rng, [{a}, {b}, {cc}, {d}])
+    if chosen is None:
+        c = cs.obj(rng, d)
+    else:
+        c = int(g.o[chosen[3]])
     return (f"SELECT * WHERE {{ ?a <{a}> ?b . ?b <{b}> ?c . ?c <{cc}> ?d . "
             f"?d <{d}> <{c}> . }}")
 
