@@ -43,12 +43,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="batch", choices=["batch", "plain", "serve"])
+    ap.add_argument("--mode", default="batch", choices=["batch", "plain", "serve", "c3"],
+                    help="batch: the 4096-query batch (default); plain: the same queries one at a "
+                         "time; serve: Poisson arrivals on the hub graph; c3: the large snowflake "
+                         "query on the 500M-triple hub graph")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (q/s)")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: relation memory budget")
-    ap.add_argument("--triples", type=int, default=100_000_000)
-    ap.add_argument("--entities", type=int, default=2_000_000)
+    ap.add_argument("--triples", type=int, default=None,
+                    help="graph size (default: 100M; 500M for --mode c3 and serve)")
+    ap.add_argument("--entities", type=int, default=None,
+                    help="entities (default: 2M; 10M for --mode c3 and serve)")
     ap.add_argument("--queries", type=int, default=4096)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample", type=int, default=256, help="queries per CPU-baseline step")
@@ -57,7 +62,13 @@ def parse():
                     help="triples of the N-Triples ingest measurement (0: skip)")
     ap.add_argument("--arena-gb", type=float, default=0.0,
                     help="HBM arena size (0: 90%% of free memory; profilers need room to replay)")
-    return ap.parse_args()
+    a = ap.parse_args()
+    hub = a.mode in ("c3", "serve")
+    if a.triples is None:
+        a.triples = 500_000_000 if hub else 100_000_000
+    if a.entities is None:
+        a.entities = 10_000_000 if hub else 2_000_000
+    return a
 
 
 def triples_label(n: int) -> str:
@@ -218,15 +229,12 @@ def run_batch(ix, queries, download=False, profile=None):
 
 
 def plain_latencies(ix, queries):
-    """One pass of the one-query-at-a-time loop: per-query wall latencies."""
-    lat = []
+    """One pass of the one-query-at-a-time loop (the reference's vdBench
+    pattern), run in C by vg_query_loop: wall time of the pass and per-query
+    latencies."""
     t_all = time.perf_counter()
-    for q in queries:
-        t0 = time.perf_counter()
-        r = ix.query(q)
-        r.close()
-        lat.append(time.perf_counter() - t0)
-    return time.perf_counter() - t_all, lat
+    sec, _, _ = ix.query_loop(queries)
+    return time.perf_counter() - t_all, list(sec)
 
 
 def cpu_baseline_run(g, queries, sample: int, steps: int = 1):
@@ -468,6 +476,118 @@ def bench_ours(args, rank, world, local, pg):
     ctx.close()
 
 
+def dedup_on_device(g, device: int):
+    """The triples made a set (sorted by p, s, o), deduplicated with torch on
+    the device; input preparation outside every timed region."""
+    import torch
+    from vedas_gb300 import workloads
+    bs = int(g.s.max()).bit_length()
+    bo = int(g.o.max()).bit_length()
+    key = (torch.from_numpy(g.p.astype(np.int64)) << (bs + bo)) | (torch.from_numpy(g.s.astype(np.int64)) << bo) \
+        | torch.from_numpy(g.o.astype(np.int64))
+    u = torch.unique(key.cuda(device)).cpu().numpy()
+    del key
+    torch.cuda.empty_cache()
+    o = (u & ((1 << bo) - 1)).astype(np.uint32)
+    s = ((u >> bo) & ((1 << bs) - 1)).astype(np.uint32)
+    p = (u >> (bs + bo)).astype(np.uint32)
+    return workloads.Graph(s, p, o, g.name + "_set")
+
+
+def roofline_of(stats):
+    """Roofline entry of the kernel with the most device time."""
+    peak, peak_kind = peak_hbm()
+    if not stats:
+        return None
+    name, (n_l, bytes_, ms) = max(stats.items(), key=lambda kv: kv[1][2])
+    achieved = bytes_ / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": f"of {peak_kind}", "traffic": traffic_table().get(name),
+            "algorithmic_bytes_per_launch": bytes_ / max(n_l, 1), "launches": n_l,
+            "avg_launch_us": 1000.0 * ms / max(n_l, 1)}
+
+
+def bench_c3(args, rank, world, local, pg):
+    """The large single query: the seven-pattern snowflake on the 500M-triple
+    hub graph (relations of about 1.6e8 rows, a result of about 4.6e8 rows x
+    8 columns).  One step = one vg_query with the result left in HBM;
+    `value` is result rows/s; e2e adds the download of every result column to
+    page-locked host memory."""
+    import torch
+    import vedas_gb300 as vg
+    from vedas_gb300 import workloads
+    g = dedup_on_device(workloads.graph_hub(n=args.triples, n_entities=args.entities, seed=args.seed,
+                                            dedup=False), local)
+    q = workloads.snowflake_query(workloads.C3_SNOWFLAKE)
+    ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+    rows = 0
+    for _ in range(args.warmup):
+        r = ix.query(q)
+        rows = r.nrows
+        log = r.log()
+        r.close()
+    clocks = ClockSampler(local)
+    ctx.stats_reset(timing=True)
+    barrier(pg)
+    ctx.sync()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r = ix.query(q)
+        rows = r.nrows
+        r.close()
+    ev1.record(stream)
+    ctx.sync()
+    clk = clocks.stop()
+    barrier(pg)
+    stats = ctx.stats()
+    launches = ctx.launches()
+    step_ms = max_over_ranks(pg, ev0.elapsed_time(ev1) / args.steps)
+    total_rows = sum_over_ranks(pg, float(rows))
+    # end to end: the same query, every result column copied to pinned host memory
+    ctx.stats_reset(timing=False)
+    ncols = 8
+    host = torch.empty((ncols, max(rows, 1)), dtype=torch.int32, pin_memory=True)
+    e2e = []
+    for it in range(args.warmup + args.steps):
+        ctx.sync()
+        t0 = time.perf_counter()
+        r = ix.query(q)
+        for c in range(ncols):
+            r.download_into(c, host[c].data_ptr())
+        r.close()
+        if it >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(pg, float(np.mean(e2e)))
+    if rank == 0:
+        line = {
+            "metric": "large-query result rows/s", "value": total_rows / (step_ms / 1000.0), "unit": "rows/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": f"seven-pattern snowflake {workloads.C3_SNOWFLAKE} on the "
+                                   f"{triples_label(args.triples)}-triple hub graph",
+                       "mode": "c3", "triples": g.n, "entities": args.entities, "result_rows": rows,
+                       "result_cols": ncols, "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2", "query": q},
+            "execution_log": [list(x) for x in log],
+            "roofline": roofline_of(stats),
+            "e2e": {"value": total_rows / e2e_s, "unit": "rows/s", "h2d_bytes_per_step": len(q),
+                    "d2h_bytes_per_step": 4 * rows * ncols, "ms_per_step": 1000 * e2e_s},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "kernels": {k: {"launches": v[0], "ms": round(v[2], 3),
+                            "GBps": round(v[1] / v[2] / 1e6, 1) if v[2] else None} for k, v in stats.items()},
+        }
+        print(json.dumps(line), flush=True)
+    ix.close()
+    ctx.close()
+
+
 def bench_serve(args, rank, world, local, pg):
     """Serving: the hub graph resident in HBM, Poisson arrivals, continuous
     batching with memory-budget admission; p50/p95/p99 latency and sustained
@@ -547,6 +667,8 @@ def main():
         bench_reference(args, rank, world, pg)
     elif args.mode == "serve":
         bench_serve(args, rank, world, local, pg)
+    elif args.mode == "c3":
+        bench_c3(args, rank, world, local, pg)
     else:
         bench_ours(args, rank, world, local, pg)
     if pg is not None:

@@ -210,6 +210,13 @@ uint32_t vg_result_nlog(const vg_result* r);
 void vg_result_log(const vg_result* r, uint32_t i, uint32_t* op, uint64_t* p1, uint64_t* p2,
                    uint64_t* p3);
 vg_status vg_result_free(vg_result* r);
+/* The reference's one-query-at-a-time benchmark loop (vdBench,
+ * src/VedasBench.cu:144-176) in C: for each query in order, vg_query then
+ * vg_result_free, timed per query on the host clock.  seconds[i], rows[i]
+ * and status[i] (each optional, nq entries) receive query i's wall time,
+ * result rows and status; the call itself fails only on bad arguments. */
+vg_status vg_query_loop(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, double* seconds,
+                        uint64_t* rows, vg_status* status);
 
 /* ---- host planning logic (no device needed) ----------------------------- */
 /* The job list QueryGraph::generateQueryPlan (src/QueryGraph.cu:64-74) and

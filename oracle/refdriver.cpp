@@ -7,6 +7,9 @@
 //   vedas_ref index <graph.bin> <out.bin> [full]
 //       VedasStorage(RdfData&, preload=false, fullIndex) (src/VedasStorage.cu:25-73)
 //       then dumps every index array through the VedasStorage getters.
+//   vedas_ref time <graph.bin> <queries.txt> <reps>
+//       Wall seconds of each timed pass of QueryExecutor::query over the
+//       queries (the CPU-baseline calibration of the restatement).
 //   vedas_ref query <graph.bin> <queries.txt> <out.bin> [first_query] [full]
 //       For each query line: SparqlQuery + QueryExecutor::query, as vdQuery's
 //       REPL does (src/VedasQuery.cu:136-205), with ENABLE_UPDATE_BOUND_AFTER_JOIN
@@ -17,6 +20,7 @@
 // Graph file: "VGRAPH1\0", u64 n, u32 s[n], u32 p[n], u32 o[n].
 // Query text: SELECT * | ?v.. WHERE { t t t . ... } with constants written as
 // <ID> (subject/predicate/object IDs) or "ID" (literal object IDs).
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -184,6 +188,50 @@ int do_query(const char* graph, const char* qpath, const char* outp, size_t firs
   return 0;
 }
 
+// Wall time of the reference's query path over a query file, as vdBench
+// times it (src/VedasBench.cu:144-176: one QueryExecutor::query per query,
+// in order, after the index is built): one untimed pass, then `reps` timed
+// passes; prints "TIME <pass> <seconds> <result rows>" per timed pass to
+// stderr (the reference's own messages go to stdout).
+int do_time(const char* graph, const char* qpath, int reps) {
+  TYPEID_HOST_VEC s, p, o;
+  if (!read_graph(graph, s, p, o)) return 2;
+  RdfData rdf(s, p, o);
+  VedasStorage st(rdf, false, false);
+  std::vector<std::string> lines;
+  {
+    std::ifstream qin(qpath);
+    std::string line;
+    while (std::getline(qin, line))
+      if (!line.empty()) lines.push_back(line);
+  }
+  std::vector<int> gpu_ids{0};
+  ExecutionWorker worker(gpu_ids);
+  mgpu::standard_context_t context(false);
+  QueryExecutor::ENABLE_UPDATE_BOUND_AFTER_JOIN = true;
+  QueryExecutor::ENABLE_FULL_INDEX = false;
+  QueryExecutor::ENABLE_LITERAL_DICT = false;
+  QueryExecutor::ENABLE_BOUND_DICT_AFTER_JOIN = false;
+  std::vector<DICTTYPE> so(lines.size()), pm(lines.size()), lm(lines.size());
+  for (size_t qi = 0; qi < lines.size(); ++qi) register_constants(lines[qi], so[qi], pm[qi], lm[qi]);
+  for (int pass = -1; pass < reps; ++pass) {
+    uint64_t rows = 0;
+    auto t0 = std::chrono::steady_clock::now();
+    for (size_t qi = 0; qi < lines.size(); ++qi) {
+      QueryExecutor::initTime();
+      SparqlQuery sq(lines[qi].c_str(), so[qi], pm[qi], lm[qi]);
+      SparqlResult sr;
+      QueryExecutor qe(&st, &worker, &context);
+      qe.query(sq, sr);
+      std::vector<std::vector<TYPEID>> cols = sr.get();
+      rows += cols.empty() ? 0 : cols[0].size();
+    }
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (pass >= 0) std::fprintf(stderr, "TIME %d %.6f %llu\n", pass, sec, static_cast<unsigned long long>(rows));
+  }
+  return 0;
+}
+
 // Plan of one query line "<e0> <e1> ... | <query>" with the given per-pattern
 // estimate_rows, through the reference's QueryGraph::generateQueryPlan
 // (src/QueryGraph.cu:64-74), printed in the post-order that
@@ -263,6 +311,7 @@ int main(int argc, char** argv) {
     bool full = argc >= 5 && std::string(argv[4]) == "full";
     return do_index(argv[2], argv[3], full);
   }
+  if (argc >= 5 && std::string(argv[1]) == "time") return do_time(argv[2], argv[3], std::atoi(argv[4]));
   if (argc >= 5 && std::string(argv[1]) == "query") {
     size_t first = argc >= 6 ? std::strtoull(argv[5], nullptr, 10) : 0;
     bool full = argc >= 7 && std::string(argv[6]) == "full";

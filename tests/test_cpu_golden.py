@@ -324,3 +324,20 @@ def test_every_entry_point_survives_null_arguments(built):
     instead of crashing; no device is needed for that."""
     r = subprocess.run([sys.executable, "-c", NULL_CHILD, ROOT], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "all returned" in r.stdout, r.stdout[-2000:] + r.stderr[-2000:]
+
+
+def test_noalloc_join_refuses_wrapping_column_counts_without_device(built):
+    """vg_join_noalloc checks each side's column count before their sum, so
+    counts whose 32-bit sum wraps are refused before any column is read."""
+    import ctypes
+    import vedas_gb300 as vg
+    L = vg.lib()
+    fn = L.vg_join_noalloc
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [pp, ctypes.c_uint32, ctypes.c_uint64, pp, ctypes.c_uint32, ctypes.c_uint64, pp,
+                   ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p]
+    cols = (ctypes.c_void_p * 2)(None, None)
+    rows = ctypes.c_uint64()
+    for lc, rc in ((0xFFFFFFFF, 2), (2, 0xFFFFFFFF), (10, 1), (5, 6)):
+        assert fn(cols, lc, 10, cols, rc, 10, None, 0, ctypes.byref(rows), None) == 1   # VG_ERR_INVALID

@@ -91,6 +91,8 @@ def lib():
             "vg_result_log": (None, [vp, u32, pu32, ctypes.POINTER(u64), ctypes.POINTER(u64),
                                      ctypes.POINTER(u64)]),
             "vg_result_free": (i32, [vp]),
+            "vg_query_loop": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(u64), ctypes.POINTER(i32)]),
             "vg_batch_run": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(vp)]),
             "vg_batch_run_host": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(vp)]),
             "vg_batch_host_column": (vp, [vp, u32, u32]),
@@ -268,6 +270,21 @@ class Index:
         check(lib().vg_query(self.ctx.h, self.h, sparql.encode(), ctypes.byref(r)))
         return Result(r)
 
+    def query_loop(self, queries):
+        """The queries one at a time in a C loop (vg_query_loop): per-query
+        wall seconds, result rows and status as numpy arrays."""
+        n = len(queries)
+        arr, keep = _pack_texts(queries)
+        sec = np.zeros(n, dtype=np.float64)
+        rows = np.zeros(n, dtype=np.uint64)
+        st = np.zeros(n, dtype=np.int32)
+        check(lib().vg_query_loop(self.ctx.h, self.h, arr, n,
+                                  sec.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  rows.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                  st.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+        del keep
+        return sec, rows, st
+
 
 class Result:
     OPS = {0: "JOIN", 1: "UPLOAD", 2: "SWAP"}
@@ -292,16 +309,21 @@ class Result:
     def nrows(self) -> int:
         return int(lib().vg_result_nrows(self.h))
 
-    def columns(self):
-        L = lib()
+    def column(self, c: int) -> np.ndarray:
+        """One result column, copied to host memory."""
         n = self.nrows
-        out = []
-        for c in range(L.vg_result_ncols(self.h)):
-            a = np.zeros(n, dtype=np.uint32)
-            if n:
-                check(L.vg_result_download(self.h, c, _p32(a)))
-            out.append(a)
-        return out
+        a = np.zeros(n, dtype=np.uint32)
+        if n:
+            check(lib().vg_result_download(self.h, c, _p32(a)))
+        return a
+
+    def columns(self):
+        return [self.column(c) for c in range(lib().vg_result_ncols(self.h))]
+
+    def download_into(self, c: int, host_ptr: int) -> None:
+        """Copies column c to host memory at host_ptr (nrows uint32 words)."""
+        if self.nrows:
+            check(lib().vg_result_download(self.h, c, ctypes.cast(host_ptr, ctypes.POINTER(ctypes.c_uint32))))
 
     def log(self):
         L = lib()

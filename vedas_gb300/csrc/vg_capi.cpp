@@ -1,5 +1,6 @@
 // The C-ABI (include/vedas_gb300.h): status codes at the boundary, no
 // exceptions across it.
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -423,6 +424,22 @@ void vg_result_log(const vg_result* r, uint32_t i, uint32_t* op, uint64_t* p1, u
 }
 vg_status vg_result_free(vg_result* r) {
   delete r;
+  return VG_OK;
+}
+
+vg_status vg_query_loop(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, double* seconds,
+                        uint64_t* rows, vg_status* status) {
+  if (!ctx || !ix || (nq && !queries)) return VG_ERR_INVALID;
+  for (uint32_t i = 0; i < nq; ++i) {
+    const auto t0 = std::chrono::steady_clock::now();
+    vg_result* r = nullptr;
+    const vg_status st = queries[i] ? vg_query(ctx, ix, queries[i], &r) : VG_ERR_INVALID;
+    const uint64_t n = r ? r->rel.nrows : 0;
+    if (r) vg_result_free(r);
+    if (seconds) seconds[i] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rows) rows[i] = n;
+    if (status) status[i] = st;
+  }
   return VG_OK;
 }
 

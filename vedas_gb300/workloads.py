@@ -444,9 +444,18 @@ def graph_hub(n: int = 500_000_000, n_entities: int = 10_000_000, n_predicates: 
     return Graph(s, p, o, f"hub_n{n}")
 
 
+# Predicates of the large single query on the 500M-triple hub graph: stars
+# (p4, p8, p11) at ?x and (p6, p9, p10) at ?y joined by ?x p1 ?y.  On that
+# graph the reference's plan builds intermediate relations of up to about
+# 1.6e8 rows and a result of about 4.6e8 rows x 8 columns (measured with the
+# oracle on the same generator at 50M triples, where every size is a tenth).
+C3_SNOWFLAKE = (4, 8, 11, 1, 6, 9, 10)
+
+
 def snowflake_query(preds=(1, 2, 3, 4, 5, 6, 7)) -> str:
     """Seven-pattern snowflake: two three-pattern stars (?x, ?y) joined by one
-    object-subject edge (?x p4 ?y)."""
+    object-subject edge (?x p4 ?y), with preds = (a, b, c, d, e, f, g) giving
+    ?x a/b/c, ?x d ?y and ?y e/f/g."""
     a, b, c, d, e, f, g = preds
     return (f"SELECT * WHERE {{ ?x <{a}> ?a . ?x <{b}> ?b . ?x <{c}> ?c . ?x <{d}> ?y . "
             f"?y <{e}> ?e . ?y <{f}> ?f . ?y <{g}> ?g . }}")
