@@ -71,6 +71,14 @@ def parse():
     return a
 
 
+T_START = time.perf_counter()
+
+
+def note(msg: str) -> None:
+    """Progress line on stderr (stdout carries only the JSON line)."""
+    print(f"[bench {time.perf_counter() - T_START:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def triples_label(n: int) -> str:
     """100000000 -> '100M', 200000 -> '200k'."""
     if n % 1_000_000 == 0:
@@ -323,6 +331,7 @@ def bench_ours(args, rank, world, local, pg):
     from vedas_gb300 import workloads as wl
 
     g, queries, cs = make_workload(args, rank)
+    note(f"workload: {g.n} triples, {len(queries)} queries")
     ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
     t0 = time.perf_counter()
     ix = vg.Index(ctx, g.s, g.p, g.o)
@@ -343,7 +352,9 @@ def bench_ours(args, rank, world, local, pg):
         build = {"triples": g.n, "device_ms": kms, "rows_per_s": g.n / (kms / 1000.0),
                  "algorithmic_GBps": 2 * 24.0 * g.n / (kms / 1000.0) / 1e9,
                  "kernels": {k: round(v[2], 3) for k, v in kst.items()}}
+    note("index built")
     ingest = bench_ingest(args, ctx, g) if args.ingest_triples > 0 else None
+    note("ingest leg done")
     chain = None
     try:
         cq = wl.chain_query(g, cs=cs)
@@ -359,10 +370,24 @@ def bench_ours(args, rank, world, local, pg):
             r.close()
         chain = {"query": cq, "rows": rows, "ms_min": 1000 * min(ts), "ms_median": 1000 * float(np.median(ts)),
                  "log": [list(x) for x in log]}
+        oq = wl.chain_query_open()
+        ix.query(oq).close()
+        ts = []
+        for _ in range(5):
+            ctx.sync()
+            t1 = time.perf_counter()
+            r = ix.query(oq)
+            ts.append(time.perf_counter() - t1)
+            orows = r.nrows
+            olog = r.log()
+            r.close()
+        chain["open_end"] = {"query": oq, "rows": orows, "ms_min": 1000 * min(ts),
+                             "ms_median": 1000 * float(np.median(ts)), "log": [list(x) for x in olog]}
     except vg.VgError as e:
         chain = {"error": str(e)}
     # The core refuses queries on which the reference itself would read out of
     # bounds or trip an assert; drop those before timing (counted below).
+    note("chain queries done")
     b = vg.Batch(ix, queries)
     kept = [q for i, q in enumerate(queries) if b.status(i) == 0]
     qrows = b.rows()
@@ -378,7 +403,9 @@ def bench_ours(args, rank, world, local, pg):
 
     for _ in range(args.warmup):
         run(ix, batch_in)
+    note("batch warm-up done")
     plain_s, plain_lat = plain_latencies(ix, kept)
+    note("plain loop done")
     plain = {"queries_per_s": len(kept) / plain_s,
              "p50_ms": 1000 * float(np.percentile(plain_lat, 50)),
              "p99_ms": 1000 * float(np.percentile(plain_lat, 99))}
@@ -407,6 +434,7 @@ def bench_ours(args, rank, world, local, pg):
     total_q = sum_over_ranks(pg, float(len(kept)))
     value = total_q / (step_ms_max / 1000.0)
 
+    note("timed batch steps done")
     # end to end: results copied to host memory inside the timed region (after
     # warm-up steps of the same path: page-locked result buffers are made once)
     for _ in range(args.warmup):
@@ -422,6 +450,7 @@ def bench_ours(args, rank, world, local, pg):
     ctx.sync()
     e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
     e2e_value = total_q / e2e_s
+    note("end-to-end steps done")
     h2d = sum(len(q) for q in kept)
 
     peak, peak_kind = peak_hbm()

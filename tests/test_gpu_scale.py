@@ -53,8 +53,25 @@ def test_c2_100m_chain_query_matches_oracle(c2):
     _same(res, r)
     log = res.log()
     assert [x[:4] for x in log] == [tuple(x[:4]) for x in r.log]
-    # index swaps between the joins, on relations of at least a million rows
+    assert sum(1 for x in log if x[0] == "SWAP") >= 2        # index swaps between the joins
+    res.close()
+
+
+def test_c2_100m_open_chain_matches_oracle(c2):
+    """The chain with its end a variable too: two index swaps on relations of
+    millions of rows and a result of tens of millions of rows, all in order."""
+    g, ix, ox, _ = c2
+    q = workloads.chain_query_open()                 # ?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 ?e
+    r = ox.query(q)
+    assert r.status == 0 and r.nrows > 1_000_000
+    res = ix.query(q)
+    log = res.log()
+    assert [x[:4] for x in log] == [tuple(x[:4]) for x in r.log]
     assert sum(1 for x in log if x[0] == "SWAP" and x[1] >= 1_000_000) >= 2
+    assert res.headers == r.headers
+    for c in range(len(r.columns)):
+        np.testing.assert_array_equal(res.column(c), r.columns[c])
+    res.close()
 
 
 def test_c2_100m_whole_bench_batch_matches_oracle(c2):
@@ -63,7 +80,7 @@ def test_c2_100m_whole_bench_batch_matches_oracle(c2):
     import vedas_gb300 as vg
     g, ix, ox, cs = c2
     qs = workloads.query_mix(g, 4096, seed=0, cs=cs)
-    b = vg.Batch(ix, qs)
+    b = vg.Batch(ix, qs, to_host=True)         # results also copied to host while the batch runs
     nonempty = [0] * len(workloads.TEMPLATES)
     for i, qq in enumerate(qs):
         rr = ox.query(qq)
@@ -75,6 +92,8 @@ def test_c2_100m_whole_bench_batch_matches_oracle(c2):
         cols = b.columns(i)
         assert len(cols) == len(rr.columns)
         for x, y in zip(cols, rr.columns):
+            np.testing.assert_array_equal(x, y, err_msg=qq)
+        for x, y in zip(b.host_columns(i), rr.columns):
             np.testing.assert_array_equal(x, y, err_msg=qq)
         assert [x[:4] for x in b.log(i)] == [tuple(x[:4]) for x in rr.log], qq
         nonempty[i % len(workloads.TEMPLATES)] += rr.nrows > 0

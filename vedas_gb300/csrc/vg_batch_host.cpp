@@ -753,9 +753,10 @@ void HostResults::add(const std::vector<BatchQuery*>& qs) {
   for (const BatchQuery* q : qs) words += q->rel.nrows * q->rel.ncols;
   if (words == 0) return;
   const size_t bytes = words * sizeof(uint32_t);
-  if (chunks_.empty() || chunks_.back().cap - chunks_.back().used < bytes) {
+  const size_t span = (bytes + 255) / 256 * 256;   // what the chunk gives up (the next start stays aligned)
+  if (chunks_.empty() || chunks_.back().used + span > chunks_.back().cap) {
     size_t got = 0;
-    void* p = ctx_.take_pinned(std::max<size_t>(bytes, size_t{256} << 20), &got);
+    void* p = ctx_.take_pinned(std::max<size_t>(span, size_t{256} << 20), &got);
     chunks_.push_back({static_cast<char*>(p), got, 0});
   }
   Chunk& ch = chunks_.back();
@@ -780,7 +781,7 @@ void HostResults::add(const std::vector<BatchQuery*>& qs) {
   VG_CUDA(cudaEventRecord(done, dl));
   cudaEventDestroy(packed);
   pending_.push_back({stage, done});
-  ch.used += (bytes + 255) / 256 * 256;
+  ch.used += span;
   bytes_ += bytes;
 }
 

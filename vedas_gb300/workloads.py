@@ -466,6 +466,15 @@ def star_query(pa: int = 3, pb: int = 7) -> str:
     return f"SELECT * WHERE {{ ?x <{pa}> ?a . ?x <{pb}> ?b . }}"
 
 
+def chain_query_open(preds=(1, 2, 5, 9)) -> str:
+    """The same four-pattern chain with its end a variable too
+    (?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 ?e): on the 100M-triple chain
+    graph the reference's plan re-sorts relations of millions of rows twice
+    (two index swaps) and returns about 7e7 rows."""
+    a, b, c, d = preds
+    return f"SELECT * WHERE {{ ?a <{a}> ?b . ?b <{b}> ?c . ?c <{c}> ?d . ?d <{d}> ?e . }}"
+
+
 def chain_query(g: Graph, preds=(1, 2, 5, 9), seed: int = 0, cs: ConstantSampler | None = None) -> str:
     """Four-pattern chain (?a p1 ?b . ?b p2 ?c . ?c p5 ?d . ?d p9 c), where c
     is the end of a four-hop path p1, p2, p5, p9 that exists in the graph (so
