@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
@@ -490,12 +491,15 @@ void WaveEngine::finish_wave() {
 }
 
 void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
+  Trace tr{'A', 0, 0, 0, 0, 0, 0, 0, 0};
+  if (tracing) tr.t0 = since(trace_origin);
   if (b_pending_) {
     auto t0 = Clock::now();
     wait_event(ev_b_);
     b_pending_ = false;
     prof.device_s += since(t0);
   }
+  if (tracing) tr.t_wait = since(trace_origin);
   if (!run_.empty()) finish_wave();
 
   // queries with a next job run it; the others finish (or have failed)
@@ -633,14 +637,25 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     a_pending_ = true;
   }
   prof.device_s += since(t0);
+  if (tracing) {
+    tr.t_end = since(trace_origin);
+    tr.items = static_cast<uint32_t>(items_.size());
+    tr.joins = static_cast<uint32_t>(jl.size());
+    tr.sorted_rels = static_cast<uint32_t>(to_sort.size());
+    for (const Rel* r : jl) tr.join_left_rows += r->nrows;
+    trace.push_back(tr);
+  }
 }
 
 void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   if (!a_pending_) return;
+  Trace tr{'B', 0, 0, 0, 0, 0, 0, 0, 0};
+  if (tracing) tr.t0 = since(trace_origin);
   auto t0 = Clock::now();
   wait_event(ev_a_);
   a_pending_ = false;
   prof.device_s += since(t0);
+  if (tracing) tr.t_wait = since(trace_origin);
   const uint64_t* ha = h_a_.data();
 
   // staged columns of the wave in flight
@@ -719,10 +734,19 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
     jsmall_ = std::move(who);
     VG_CUDA(cudaEventRecord(ev_b_, ctx_.stream));
     b_pending_ = true;
+    if (tracing) {
+      tr.joins = static_cast<uint32_t>(J);
+      for (size_t m = 0; m < J; ++m) tr.join_out_rows += tot[m];
+    }
   } else {
     jsmall_.clear();
   }
   prof.device_s += since(t0);
+  if (tracing) {
+    tr.t_end = since(trace_origin);
+    tr.items = static_cast<uint32_t>(items_.size());
+    trace.push_back(tr);
+  }
 }
 
 HostResults::~HostResults() {
@@ -817,6 +841,11 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
     out.host = std::make_unique<HostResults>(ctx);
     for (auto& e : eng) e->set_host_results(out.host.get());
   }
+  const char* trace_path = std::getenv("VG_WAVE_TRACE");
+  for (auto& e : eng) {
+    e->tracing = trace_path != nullptr;
+    e->trace_origin = t_all;
+  }
   for (size_t i = 0; i < pq.size(); ++i) eng[i % ne]->add(&pq[i]);
   std::vector<std::exception_ptr> err(ne);
   auto drive = [&](size_t e) {
@@ -844,6 +873,18 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
     out.prof.final_s += e->prof.final_s;
   }
   out.prof.plan_s = plan_s;
+  if (trace_path) {
+    // one line per stage: engine stage t0 t_wait t_end items joins sorted_rels join_left_rows join_out_rows
+    if (FILE* f = std::fopen(trace_path, "a")) {
+      std::fprintf(f, "# batch of %zu queries, planned in %.6f s\n", n, plan_s);
+      for (size_t e = 0; e < eng.size(); ++e)
+        for (const auto& t : eng[e]->trace)
+          std::fprintf(f, "%zu %c %.6f %.6f %.6f %u %u %u %llu %llu\n", e, t.stage, t.t0, t.t_wait, t.t_end, t.items,
+                       t.joins, t.sorted_rels, static_cast<unsigned long long>(t.join_left_rows),
+                       static_cast<unsigned long long>(t.join_out_rows));
+      std::fclose(f);
+    }
+  }
   if (out.host) out.host->finish();
   ctx.check_device_errors();
   // plans, parsed queries and executors (bounds, empty intervals, logs) are

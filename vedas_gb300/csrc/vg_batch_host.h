@@ -124,6 +124,20 @@ class WaveEngine {
   uint32_t waves() const { return waves_; }
   BatchProfile prof;
 
+  // Per-stage timeline, kept when tracing is on (VG_WAVE_TRACE names a file
+  // that run_batch appends it to): seconds since the batch started at the
+  // stage's start, after its wait for the device, and at its end, with the
+  // stage's work.
+  struct Trace {
+    char stage;              // 'A' or 'B'
+    double t0, t_wait, t_end;
+    uint32_t items, joins, sorted_rels;
+    uint64_t join_left_rows, join_out_rows;
+  };
+  bool tracing = false;
+  std::chrono::steady_clock::time_point trace_origin;
+  std::vector<Trace> trace;
+
   // Host state of one job of the wave in flight.
   struct Item {
     enum Kind { kNone, kSelect, kJoin, kSwap } kind = kNone;
