@@ -10,6 +10,9 @@
 //   vedas_ref time <graph.bin> <queries.txt> <reps>
 //       Wall seconds of each timed pass of QueryExecutor::query over the
 //       queries (the CPU-baseline calibration of the restatement).
+//   vedas_ref vds-write <graph.bin> <out.vds> [full]
+//       VedasStorage(RdfData&, ...) then VedasStorage::write: the reference's
+//       own .vds file of the graph.
 //   vedas_ref query <graph.bin> <queries.txt> <out.bin> [first_query] [full]
 //       For each query line: SparqlQuery + QueryExecutor::query, as vdQuery's
 //       REPL does (src/VedasQuery.cu:136-205), with ENABLE_UPDATE_BOUND_AFTER_JOIN
@@ -130,6 +133,17 @@ int do_index(const char* graph, const char* outp, bool full) {
   }
   put_str(out, "");
   return out ? 0 : 3;
+}
+
+// The reference's own .vds file of a graph: VedasStorage(RdfData&, ...) then
+// VedasStorage::write (src/VedasStorage.cu:486-516).
+int do_vds_write(const char* graph, const char* outp, bool full) {
+  TYPEID_HOST_VEC s, p, o;
+  if (!read_graph(graph, s, p, o)) return 2;
+  RdfData rdf(s, p, o);
+  VedasStorage st(rdf, false, full);
+  st.write(outp);
+  return 0;
 }
 
 int do_query(const char* graph, const char* qpath, const char* outp, size_t first, bool full) {
@@ -312,6 +326,10 @@ int main(int argc, char** argv) {
     return do_index(argv[2], argv[3], full);
   }
   if (argc >= 5 && std::string(argv[1]) == "time") return do_time(argv[2], argv[3], std::atoi(argv[4]));
+  if (argc >= 4 && std::string(argv[1]) == "vds-write") {
+    bool full = argc >= 5 && std::string(argv[4]) == "full";
+    return do_vds_write(argv[2], argv[3], full);
+  }
   if (argc >= 5 && std::string(argv[1]) == "query") {
     size_t first = argc >= 6 ? std::strtoull(argv[5], nullptr, 10) : 0;
     bool full = argc >= 7 && std::string(argv[6]) == "full";

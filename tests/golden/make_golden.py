@@ -17,6 +17,9 @@ Fixtures:
                 and what the reference code actually returns) plus random
                 update sequences
   plans.json    plans the reference's QueryGraph builds for random estimates
+  vds.json      the reference's own .vds files of a small graph
+                (vds_partial.vds, vds_full.vds, written by VedasStorage::write)
+                and their sha256
   plans_multiedge.json
                 plans for random queries over few variables, with patterns that
                 share both variables (several edges between two vertices) and
@@ -90,6 +93,27 @@ def gen_index(td):
                 k: {"len": int(v.shape[0]), "sha256": hashlib.sha256(v.tobytes()).hexdigest()}
                 for k, v in arrs.items()}
     return {"graphs": INDEX_GRAPHS, "arrays": out}
+
+
+VDS_GRAPH = dict(kind="star", n=3_000, n_subjects=300, seed=13)
+
+
+def gen_vds(td):
+    """The reference's own .vds files (VedasStorage::write) of a small graph,
+    with the partial and the full index: vds_partial.vds, vds_full.vds."""
+    g = make_graph(VDS_GRAPH)
+    p = os.path.join(td, "vds.graph")
+    g.save(p)
+    files = {}
+    for full in (False, True):
+        name = f"vds_{'full' if full else 'partial'}.vds"
+        out = os.path.join(HERE, name)
+        # the full-index build writes histogram files into its working directory
+        subprocess.run([ref_runner.REF_BIN, "vds-write", p, out] + (["full"] if full else []), check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, cwd=td)
+        with open(out, "rb") as f:
+            files[name] = hashlib.sha256(f.read()).hexdigest()
+    return {"graph": VDS_GRAPH, "files": files}
 
 
 def gen_queries(td):
@@ -242,7 +266,8 @@ def main():
         for name, fn in (("index", lambda: gen_index(td)), ("queries", lambda: gen_queries(td)),
                          ("c1", lambda: gen_c1(td)), ("eid", lambda: gen_eid(a.ref_src, td)),
                          ("plans", lambda: gen_plans(td)),
-                         ("plans_multiedge", lambda: gen_plans_multiedge(td))):
+                         ("plans_multiedge", lambda: gen_plans_multiedge(td)),
+                         ("vds", lambda: gen_vds(td))):
             if a.only and name != a.only:
                 continue
             data = fn()

@@ -341,3 +341,32 @@ def test_noalloc_join_refuses_wrapping_column_counts_without_device(built):
     rows = ctypes.c_uint64()
     for lc, rc in ((0xFFFFFFFF, 2), (2, 0xFFFFFFFF), (10, 1), (5, 6)):
         assert fn(cols, lc, 10, cols, rc, 10, None, 0, ctypes.byref(rows), None) == 1   # VG_ERR_INVALID
+
+
+def test_reference_vds_fixtures_hold_the_oracle_arrays(built):
+    """The reference-written .vds fixtures are [u64 n][n x u32] arrays in
+    VedasStorage::write order (src/VedasStorage.cu:486-516) holding exactly
+    the oracle's index arrays; the GPU tests open them with the core."""
+    import hashlib
+    from oracle import oracle_py
+    meta = json.load(open(os.path.join(GOLD, "vds.json")))
+    spec = meta["graph"]
+    g = workloads.graph_small_star(n=spec["n"], n_subjects=spec["n_subjects"], seed=spec["seed"])
+    order = ["p_idx_values", "p_idx_offsets", "ps_s_idx_values", "ps_idx_offsets", "po_o_idx_values",
+             "po_idx_offsets", "ps_data", "po_data", "pso_data", "pos_data"]
+    full_order = ["s_idx_values", "s_idx_offsets", "sp_p_idx_values", "sp_idx_offsets", "so_o_idx_values",
+                  "so_idx_offsets", "o_idx_values", "o_idx_offsets", "os_data", "op_p_idx_values",
+                  "op_idx_offsets", "spo_data", "sop_data", "ops_data", "osp_data"]
+    for full in (False, True):
+        name = f"vds_{'full' if full else 'partial'}.vds"
+        buf = open(os.path.join(GOLD, name), "rb").read()
+        assert hashlib.sha256(buf).hexdigest() == meta["files"][name]
+        ox = oracle_py.OracleIndex(g.s, g.p, g.o, full=full)
+        off = 0
+        for a in order + (full_order if full else []):
+            n = int(np.frombuffer(buf, dtype=np.uint64, count=1, offset=off)[0])
+            off += 8
+            arr = np.frombuffer(buf, dtype=np.uint32, count=n, offset=off)
+            off += 4 * n
+            np.testing.assert_array_equal(arr, ox.array(a), err_msg=a)
+        assert off == len(buf)

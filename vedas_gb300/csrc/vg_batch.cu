@@ -190,21 +190,23 @@ struct JoinSeg {
 };
 
 // One block per tile of kJcTile left keys of one join, tiles taken in ticket
-// order.  The tile's match counts stay in registers (the right-key window is
-// staged by a bulk copy when it fits); their block scan and a segmented
-// decoupled look-back over the join's earlier tiles give every left key its
-// output offset directly, and the join's last tile writes its total.
+// order (the tile's join from a per-tile table, one load instead of a search
+// of the join starts).  The tile's match counts stay in registers (the
+// right-key window is staged by a bulk copy when it fits); their block scan
+// and a segmented decoupled look-back over the join's earlier tiles give
+// every left key its output offset directly, and the join's last tile writes
+// its total.
 __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
-    const JoinSeg* __restrict__ js, const uint64_t* __restrict__ bstart, uint32_t J, uint32_t* __restrict__ lo,
-    uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket, uint64_t* __restrict__ totals,
-    DeviceErrors* err) {
+    const JoinSeg* __restrict__ js, const uint64_t* __restrict__ bstart, const uint32_t* __restrict__ tile_join,
+    uint32_t* __restrict__ lo, uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket,
+    uint64_t* __restrict__ totals, DeviceErrors* err) {
   __shared__ JoinCountSmem sm;
   __shared__ uint64_t s_scan[kJcBlock / 32 + 1];
   __shared__ uint64_t s_b;
   __shared__ uint32_t s_tile, s_j;
   if (threadIdx.x == 0) {
     s_tile = atomicAdd(ticket, 1u);
-    s_j = seg_of(bstart, J, s_tile);
+    s_j = tile_join[s_tile];
   }
   __syncthreads();
   const uint64_t tile = s_tile;
@@ -244,72 +246,81 @@ struct JoinOut {
   uint32_t nlc, nrc;
 };
 
-// Output rows [kb, kb + kTileRows) of one join per block.  Output row k comes
-// from the left row i with offs[i] <= k < offs[i + 1] and the right row
-// lo[i] + (k - offs[i]).  Two warps find the tile's left-row range at once;
-// when it holds at most kTileRows + 1 rows, its offsets and lower bounds are
-// staged in shared memory, and each thread walks its rows (k increasing)
-// from the previous one's left row.  Hub keys thus spread over many blocks.
+// Output rows [kb, kb + kTileRows) of one join per tile (the tile's join
+// from a per-tile table).  Blocks loop over tiles [blockIdx.x, T) with
+// stride gridDim.x; T is read from the device when ostart_end is given (a
+// device-side placement wrote it there).  Output row k comes from the left
+// row i with offs[i] <= k < offs[i + 1] and the right row lo[i] + (k -
+// offs[i]).  Two warps find the tile's left-row range at once; when it holds
+// at most kTileRows + 1 rows, its offsets and lower bounds are staged in
+// shared memory, and each thread walks its rows (k increasing, consecutive
+// threads on consecutive rows, so loads and stores coalesce) from the
+// previous one's left row.  Hub keys thus spread over many blocks.
 __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __restrict__ jo,
-                                                             const uint64_t* __restrict__ ostart, uint32_t J) {
+                                                             const uint64_t* __restrict__ ostart,
+                                                             const uint32_t* __restrict__ tile_join,
+                                                             uint64_t T_host, const uint64_t* ostart_end) {
   constexpr int kStage = kTileRows + 1;
   __shared__ JoinOut s_o;
   __shared__ uint64_t s_off[kStage];
   __shared__ uint32_t s_lo[kStage];
   __shared__ uint64_t s_i[2];
-  __shared__ uint32_t s_j;
-  if (threadIdx.x == 0) s_j = seg_of(ostart, J, blockIdx.x);
-  __syncthreads();
-  {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(&jo[s_j]);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(&s_o);
-    for (uint32_t w = threadIdx.x; w < sizeof(JoinOut) / 4; w += kBlock) dst[w] = src[w];
-  }
-  __syncthreads();
-  const uint64_t kb = (blockIdx.x - ostart[s_j]) * static_cast<uint64_t>(kTileRows);
-  const uint64_t kend = (kb + kTileRows < s_o.total) ? kb + kTileRows : s_o.total;
-  if (threadIdx.x < 32) {
-    const uint64_t f = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kb) - 1;
-    if (threadIdx.x == 0) s_i[0] = f;
-  } else if (threadIdx.x < 64) {
-    const uint64_t e = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kend - 1);
-    if (threadIdx.x == 32) s_i[1] = e;
-  }
-  __syncthreads();
-  const uint64_t ib = s_i[0], ie = s_i[1];
-  const uint64_t m = ie - ib;
-  const bool staged = m <= static_cast<uint64_t>(kStage);
-  if (staged)
-    for (uint32_t e = threadIdx.x; e < m; e += kBlock) {
-      s_off[e] = s_o.offs[ib + e];
-      s_lo[e] = s_o.lo[ib + e];
+  const uint64_t T = ostart_end ? *ostart_end : T_host;
+#pragma unroll 1
+  for (uint64_t tile = blockIdx.x; tile < T; tile += gridDim.x) {
+    __syncthreads();   // the previous tile's readers of the shared arrays are done
+    const uint32_t jn = tile_join[tile];
+    {
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(&jo[jn]);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&s_o);
+      for (uint32_t w = threadIdx.x; w < sizeof(JoinOut) / 4; w += kBlock) dst[w] = src[w];
     }
-  __syncthreads();
-  uint32_t p = 0;   // staged: the current left row, relative to ib
-  for (int it = 0; it < kRows; ++it) {
-    const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
-    if (k >= kend) break;
-    uint64_t i, jj;
-    if (staged) {
-      // last p with s_off[p] <= k, moving forward from the previous row's p
-      uint32_t step = 1;
-      while (p + step < m && s_off[p + step] <= k) {
-        p += step;
-        step <<= 1;
-      }
-      while (step > 1) {
-        step >>= 1;
-        if (p + step < m && s_off[p + step] <= k) p += step;
-      }
-      i = ib + p;
-      jj = s_lo[p] + (k - s_off[p]);
-    } else {
-      i = upper_bound_dev(s_o.offs, ib, ie, k) - 1;
-      jj = s_o.lo[i] + (k - s_o.offs[i]);
+    __syncthreads();
+    const uint64_t kb = (tile - ostart[jn]) * static_cast<uint64_t>(kTileRows);
+    const uint64_t kend = (kb + kTileRows < s_o.total) ? kb + kTileRows : s_o.total;
+    if (threadIdx.x < 32) {
+      const uint64_t f = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kb) - 1;
+      if (threadIdx.x == 0) s_i[0] = f;
+    } else if (threadIdx.x < 64) {
+      const uint64_t e = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kend - 1);
+      if (threadIdx.x == 32) s_i[1] = e;
     }
-    uint32_t c = 0;
-    for (uint32_t x = 0; x < s_o.nlc; ++x) s_o.oc[c++][k] = s_o.lc[x][i];
-    for (uint32_t x = 0; x < s_o.nrc; ++x) s_o.oc[c++][k] = s_o.rc[x][jj];
+    __syncthreads();
+    const uint64_t ib = s_i[0], ie = s_i[1];
+    const uint64_t m = ie - ib;
+    const bool staged = m <= static_cast<uint64_t>(kStage);
+    if (staged)
+      for (uint32_t e = threadIdx.x; e < m; e += kBlock) {
+        s_off[e] = s_o.offs[ib + e];
+        s_lo[e] = s_o.lo[ib + e];
+      }
+    __syncthreads();
+    uint32_t p = 0;   // staged: the current left row, relative to ib
+    for (int it = 0; it < kRows; ++it) {
+      const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
+      if (k >= kend) break;
+      uint64_t i, jj;
+      if (staged) {
+        // last p with s_off[p] <= k, moving forward from the previous row's p
+        uint32_t step = 1;
+        while (p + step < m && s_off[p + step] <= k) {
+          p += step;
+          step <<= 1;
+        }
+        while (step > 1) {
+          step >>= 1;
+          if (p + step < m && s_off[p + step] <= k) p += step;
+        }
+        i = ib + p;
+        jj = s_lo[p] + (k - s_off[p]);
+      } else {
+        i = upper_bound_dev(s_o.offs, ib, ie, k) - 1;
+        jj = s_o.lo[i] + (k - s_o.offs[i]);
+      }
+      uint32_t c = 0;
+      for (uint32_t x = 0; x < s_o.nlc; ++x) s_o.oc[c++][k] = s_o.lc[x][i];
+      for (uint32_t x = 0; x < s_o.nrc; ++x) s_o.oc[c++][k] = s_o.rc[x][jj];
+    }
   }
 }
 
@@ -499,50 +510,59 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
     bstart[j + 1] = bstart[j] + div_up(l[j]->nrows, kJcTile);
     cbytes += 4.0 * (l[j]->nrows + r[j]->nrows);
   }
+  const uint64_t T = bstart[J];
+  if (T > 0x7FFFFFFFull) fail(VG_ERR_OVERFLOW, "batched join count: too many tiles");
+  std::vector<uint32_t> tile_join(T);
+  for (uint32_t j = 0; j < J; ++j)
+    for (uint64_t t = bstart[j]; t < bstart[j + 1]; ++t) tile_join[t] = j;
   JoinSeg* djs = upload(ctx, js);
   uint64_t* dbs = upload(ctx, bstart);
+  uint32_t* dtj = upload(ctx, tile_join);
   jb.lo = ctx.alloc<uint32_t>(rows);
   jb.offs = ctx.alloc<uint64_t>(rows);
-  uint64_t* status = ctx.alloc<uint64_t>(bstart[J]);
+  uint64_t* status = ctx.alloc<uint64_t>(T);
   uint64_t* totals = ctx.alloc<uint64_t>(J);
   uint32_t* ticket = ctx.alloc<uint32_t>(1);
-  VG_CUDA(cudaMemsetAsync(status, 0, bstart[J] * sizeof(uint64_t), ctx.stream));
+  VG_CUDA(cudaMemsetAsync(status, 0, T * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), ctx.stream));
   ctx.launch("join_count_scan", cbytes + 12.0 * rows, [&] {
-    bjoin_count_scan_kernel<<<static_cast<unsigned>(bstart[J]), kJcBlock, 0, ctx.stream>>>(
-        djs, dbs, J, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);
+    bjoin_count_scan_kernel<<<static_cast<unsigned>(T), kJcBlock, 0, ctx.stream>>>(
+        djs, dbs, dtj, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaMemcpyAsync(totals_host, totals, J * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  jb.d_totals = totals;   // for a device-side placement; released with lo and offs
   // the stream orders every later use of these blocks after the kernel above
   ctx.free(status);
-  ctx.free(totals);
   ctx.free(ticket);
   ctx.free(djs);
   ctx.free(dbs);
+  ctx.free(dtj);
 }
 
 void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::vector<Rel>& out,
-                        uint32_t* first_last_host) {
+                        uint32_t* first_last_host, const uint8_t* skip) {
   const uint32_t J = jb.J;
-  out.assign(J, Rel());
+  if (!skip) out.assign(J, Rel());
   if (J == 0) return;
   std::vector<JoinOut> jo(J);
   std::vector<uint64_t> ostart(J + 1, 0);
   double wbytes = 0;
+  auto rows = [&](uint32_t j) -> uint64_t { return (skip && skip[j]) ? 0 : totals[j]; };
   for (uint32_t j = 0; j < J; ++j) {
-    if (totals[j] > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
-    ostart[j + 1] = ostart[j] + div_up(totals[j], kTileRows);
-    wbytes += 4.0 * totals[j] * (2.0 * (jb.l[j]->ncols + jb.r[j]->ncols - 1) - 1);
+    if (rows(j) > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
+    ostart[j + 1] = ostart[j] + div_up(rows(j), kTileRows);
+    wbytes += 4.0 * rows(j) * (2.0 * (jb.l[j]->ncols + jb.r[j]->ncols - 1) - 1);
   }
   // the outputs of a wave's joins are allocated and described on the host pool
   parallel_for(J, [&](size_t j) {
+    JoinOut& o = jo[j];
+    std::memset(&o, 0, sizeof(o));
+    if (skip && skip[j]) return;                // written already: out[j] stays as it is
     const Rel* l = jb.l[j];
     const Rel* r = jb.r[j];
     const uint32_t ncols = l->ncols + r->ncols - 1;
     out[j] = rel_alloc(ctx, ncols, totals[j]);
-    JoinOut& o = jo[j];
-    std::memset(&o, 0, sizeof(o));
     o.offs = jb.offs + jb.row0[j];
     o.lo = jb.lo + jb.row0[j];
     o.nl = l->nrows;
@@ -557,12 +577,19 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
   uint32_t* dfl = ctx.alloc<uint32_t>(2 * J);
   VG_CUDA(cudaMemsetAsync(dfl, 0, 2 * J * sizeof(uint32_t), ctx.stream));
   if (ostart[J] > 0) {
+    if (ostart[J] > 0x7FFFFFFFull) fail(VG_ERR_OVERFLOW, "batched join write: too many tiles");
+    std::vector<uint32_t> tile_join(ostart[J]);
+    for (uint32_t j = 0; j < J; ++j)
+      for (uint64_t t = ostart[j]; t < ostart[j + 1]; ++t) tile_join[t] = j;
     uint64_t* dos = upload(ctx, ostart);
+    uint32_t* dtj = upload(ctx, tile_join);
     ctx.launch("join_write", wbytes, [&] {
-      bjoin_write_kernel<<<static_cast<unsigned>(ostart[J]), kBlock, 0, ctx.stream>>>(djo, dos, J);
+      bjoin_write_kernel<<<static_cast<unsigned>(ostart[J]), kBlock, 0, ctx.stream>>>(djo, dos, dtj, ostart[J],
+                                                                                      nullptr);
     });
     VG_CUDA(cudaGetLastError());
     ctx.free(dos);
+    ctx.free(dtj);
   }
   ctx.launch("join_first_last", 8.0 * J, [&] {
     first_last_kernel<<<static_cast<unsigned>(div_up(J, 128)), 128, 0, ctx.stream>>>(djo, J, dfl);
@@ -571,10 +598,16 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
   VG_CUDA(cudaMemcpyAsync(first_last_host, dfl, 2 * J * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.free(dfl);
   ctx.free(djo);
-  ctx.free(jb.lo);
-  ctx.free(jb.offs);
-  jb.lo = nullptr;
-  jb.offs = nullptr;
+  jb.release(ctx);
+}
+
+void JoinBatch::release(Ctx& ctx) {
+  ctx.free(lo);
+  ctx.free(offs);
+  ctx.free(d_totals);
+  lo = nullptr;
+  offs = nullptr;
+  d_totals = nullptr;
 }
 
 void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r,
@@ -585,8 +618,20 @@ void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<
   if (J == 0) return;
   PinnedWords tot(ctx), fl(ctx);
   JoinBatch jb;
-  batched_join_count(ctx, l, r, jb, tot.reserve(J));
+  uint64_t* ht = tot.reserve(J + 1);
+  batched_join_count(ctx, l, r, jb, ht);
+  // the error record comes back with the totals: a look-back that gave up
+  // leaves the offsets wrong, and the write must then not run
+  VG_CUDA(cudaMemcpyAsync(ht + J, ctx.d_err, sizeof(DeviceErrors), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.sync();
+  {
+    DeviceErrors he;
+    std::memcpy(&he, ht + J, sizeof(he));
+    if (he.timeout) {
+      jb.release(ctx);
+      ctx.raise_device_errors(he);
+    }
+  }
   batched_join_write(ctx, jb, tot.data(), out, reinterpret_cast<uint32_t*>(fl.reserve(J)));
   ctx.sync();
   const uint32_t* f = reinterpret_cast<const uint32_t*>(fl.data());

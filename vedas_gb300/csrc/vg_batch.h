@@ -71,11 +71,16 @@ struct JoinBatch {
   std::vector<uint64_t> row0;   // offset of each join's left rows in lo/offs
   uint32_t* lo = nullptr;       // lower bound in r of every left key
   uint64_t* offs = nullptr;     // exclusive scan of the match counts
+  uint64_t* d_totals = nullptr; // every join's output rows, on the device
+  // Frees lo, offs and d_totals (in stream order).
+  void release(Ctx& ctx);
 };
 void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r, JoinBatch& jb,
                         uint64_t* totals_host);
+// skip (optional, J flags): joins whose outputs are in out[] already; the
+// others are allocated and written.  Releases jb's device arrays.
 void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::vector<Rel>& out,
-                        uint32_t* first_last_host);
+                        uint32_t* first_last_host, const uint8_t* skip = nullptr);
 void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r,
                   std::vector<Rel>& out, std::vector<uint32_t>& first_last);
 

@@ -1,5 +1,6 @@
 // Resident index: build orchestration, host mirrors and the .vds format.
 #include <algorithm>
+#include <cstring>
 #include <cstdio>
 #include <fstream>
 
@@ -130,33 +131,91 @@ void write_vds(Index& ix, const char* path) {
   if (!out) fail(VG_ERR_INVALID, std::string("write failed: ") + path);
 }
 
+// Reads the file in chunks into two page-locked buffers taken in turn: while
+// one chunk's host-to-device copy runs, the next chunk is read into the
+// other buffer (a buffer is refilled only after its copy's event).  The
+// level-1/level-2 index arrays and the level-2 key columns, which the
+// host-side lookups search, are kept as host mirrors from the same chunks;
+// the other data columns go to the device only (a mirror is copied back on
+// request).
 void open_vds(Ctx& ctx, const char* path, bool full, Index& ix) {
   std::ifstream in(path, std::ios::binary);
   if (!in) fail(VG_ERR_INVALID, std::string("cannot open ") + path);
   ix.ctx = &ctx;
   ix.full = full;
-  auto r = [&](const char* name) {
-    uint64_t n = 0;
-    in.read(reinterpret_cast<char*>(&n), sizeof(n));
-    if (!in || n > (1ull << 36)) fail(VG_ERR_INVALID, std::string("corrupt .vds array ") + name);
-    std::vector<uint32_t>& v = ix.host[name];
-    v.resize(n);
-    in.read(reinterpret_cast<char*>(v.data()), static_cast<std::streamsize>(n * 4));
-    if (!in) fail(VG_ERR_INVALID, std::string("truncated .vds array ") + name);
-    DevArray d(n ? ctx.alloc<uint32_t>(n) : nullptr, n);
-    if (n)
-      VG_CUDA(cudaMemcpyAsync(d.ptr, v.data(), n * 4, cudaMemcpyHostToDevice, ctx.stream));
-    ix.dev[name] = d;
+  constexpr size_t kStageBytes = size_t{64} << 20;
+  struct Stage {
+    char* p = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+  } st[2];
+  auto release = [&] {
+    for (Stage& x : st) {
+      if (x.done) {
+        cudaEventSynchronize(x.done);
+        cudaEventDestroy(x.done);
+      }
+      if (x.p) ctx.give_pinned(x.p, x.cap);
+      x = Stage();
+    }
   };
-  for (const char* n : kVdsOrder) r(n);
-  if (full)
-    for (const char* n : kVdsFullOrder) r(n);
+  try {
+    for (Stage& x : st) {
+      x.p = static_cast<char*>(ctx.take_pinned(kStageBytes, &x.cap));
+      VG_CUDA(cudaEventCreateWithFlags(&x.done, cudaEventDisableTiming));
+    }
+    int turn = 0;
+    auto r = [&](const char* name, bool mirror) {
+      uint64_t n = 0;
+      in.read(reinterpret_cast<char*>(&n), sizeof(n));
+      if (!in || n > (1ull << 36)) fail(VG_ERR_INVALID, std::string("corrupt .vds array ") + name);
+      std::vector<uint32_t>* v = nullptr;
+      if (mirror) {
+        v = &ix.host[name];
+        v->resize(n);
+      }
+      DevArray d(n ? ctx.alloc<uint32_t>(n) : nullptr, n);
+      ix.dev[name] = d;
+      const size_t bytes = n * 4;
+      for (size_t off = 0; off < bytes;) {
+        Stage& x = st[turn];
+        turn ^= 1;
+        if (x.busy) VG_CUDA(cudaEventSynchronize(x.done));
+        const size_t len = std::min(bytes - off, x.cap);
+        in.read(x.p, static_cast<std::streamsize>(len));
+        if (!in) fail(VG_ERR_INVALID, std::string("truncated .vds array ") + name);
+        VG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(d.ptr) + off, x.p, len, cudaMemcpyHostToDevice,
+                                ctx.stream));
+        VG_CUDA(cudaEventRecord(x.done, ctx.stream));
+        x.busy = true;
+        if (v) std::memcpy(reinterpret_cast<char*>(v->data()) + off, x.p, len);
+        off += len;
+      }
+    };
+    // the host-side lookups search the level-1/level-2 arrays and the
+    // level-2 key columns (ps_data, po_data); the last data column of each
+    // permutation stays on the device
+    for (const char* n : kVdsOrder)
+      r(n, std::strcmp(n, "pso_data") != 0 && std::strcmp(n, "pos_data") != 0);
+    if (full)
+      for (const char* n : kVdsFullOrder) r(n, std::strstr(n, "_idx_") != nullptr);
+    ctx.sync();
+  } catch (...) {
+    release();
+    throw;
+  }
+  release();
   ix.n = ix.get("pso_data").len;
-  // subjects and objects are the level-2 keys and data of PSO; predicates the level-1 keys
+  // subjects and objects are the level-2 keys and data of PSO (their maxima
+  // taken on the device); predicates the level-1 keys
   ix.max_id = 0;
-  for (const char* name : {"ps_data", "pso_data", "p_idx_values"})
-    for (uint32_t v : ix.host[name]) ix.max_id = std::max(ix.max_id, v);
-  ctx.sync();
+  if (ix.n) {
+    uint32_t m3[3] = {0, 0, 0};
+    column_max3(ctx, ix.get("ps_data").ptr, ix.get("pso_data").ptr, ix.get("ps_data").ptr, ix.n, m3);
+    ix.max_id = std::max(m3[0], m3[1]);
+  }
+  for (uint32_t v : ix.host_array("p_idx_values")) ix.max_id = std::max(ix.max_id, v);
 }
 
 }  // namespace vg
