@@ -1,8 +1,9 @@
 // Host-side check of the HBM arena's bookkeeping: many threads allocate,
 // hand blocks to each other and free them; no two live blocks may overlap,
 // every block lies inside the slab with the arena's alignment, and the used
-// byte count returns to zero.  The slab is a fake address range the arena
-// never dereferences.
+// byte count returns to zero; regions (blocks whose interior another
+// allocator hands out) return to the arena with their last reference.  The
+// slab is a fake address range the arena never dereferences.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -113,13 +114,44 @@ int main(int argc, char** argv) {
   }
   vg::set_arena_reclaim(nullptr);
   const bool peak_ok = ar.peak() >= lf;
+  // regions: interior blocks handed out from a region are freed by many
+  // threads (as relations are, on the host workers) while the opener closes
+  // it; the region's block returns to the arena with the last reference, and
+  // a block carved from the same bytes afterwards is freed normally
+  bool region_ok = true;
+  {
+    const size_t used0 = ar.used();
+    for (int round = 0; round < 20 && region_ok; ++round) {
+      vg::Arena::Region* r = ar.region_open(size_t{256} << 20);
+      if (!r) {
+        region_ok = false;
+        break;
+      }
+      const int per = 2000;
+      std::vector<void*> interior;
+      for (int i = 0; i < threads * per; ++i) interior.push_back(r->begin + size_t(i) * 4096);
+      ar.region_adopt(r, static_cast<int64_t>(interior.size()));
+      std::vector<std::thread> fr;
+      for (int t = 0; t < threads; ++t)
+        fr.emplace_back([&, t] {
+          for (int i = t; i < static_cast<int>(interior.size()); i += threads) ar.free(interior[i]);
+        });
+      if (round & 1) ar.region_close(r);            // closed while its blocks are being freed
+      for (auto& x : fr) x.join();
+      if (!(round & 1)) ar.region_close(r);         // closed after every block was freed
+      if (ar.used() != used0) region_ok = false;
+      void* again = ar.alloc(size_t{64} << 20);     // reuses the region's bytes; a plain free
+      ar.free(again);
+      if (ar.used() != used0) region_ok = false;
+    }
+  }
   int fails = 0;
   for (int f : failures) fails += f;
   std::printf("blocks=%zu overlaps_or_out_of_range=%d used_end=%zu shrink_used=%zu oom_ok=%d alloc_failures=%d "
-              "reclaim_ok=%d peak_ok=%d\n",
+              "reclaim_ok=%d peak_ok=%d region_ok=%d\n",
               all.size(), bad, ar.used(), used_after_shrink, oom_ok ? 1 : 0, fails, reclaim_ok ? 1 : 0,
-              peak_ok ? 1 : 0);
+              peak_ok ? 1 : 0, region_ok ? 1 : 0);
   const bool ok = bad == 0 && ar.used() == 0 && used_after_shrink == (size_t{1} << 20) && oom_ok && fails == 0 &&
-                  reclaim_ok && peak_ok;
+                  reclaim_ok && peak_ok && region_ok;
   return ok ? 0 : 1;
 }

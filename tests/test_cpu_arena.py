@@ -2,7 +2,8 @@
 is touched): blocks never overlap, stay aligned inside the slab, can be freed
 by another thread, and the used count returns to zero.  An allocation that
 does not fit runs the reclaim hook (deferred releases) before it fails, and the
-peak covers the largest use seen."""
+peak covers the largest use seen.  Regions return to the arena with their
+last reference, whichever thread drops it."""
 import os
 import shutil
 import subprocess
@@ -31,4 +32,4 @@ def test_arena_concurrent_bookkeeping(arena_check, threads, ops):
     r = subprocess.run([arena_check, str(threads), str(ops)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "overlaps_or_out_of_range=0" in r.stdout
-    assert "reclaim_ok=1 peak_ok=1" in r.stdout
+    assert "reclaim_ok=1 peak_ok=1 region_ok=1" in r.stdout

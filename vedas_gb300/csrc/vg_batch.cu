@@ -324,6 +324,83 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
   }
 }
 
+// ---------------------------------------------------------------------------
+// Device-side placement of a wave's join outputs in a region (no host round
+// trip between the count and the write).  One block: every join's output
+// size comes from its count, each column is rounded up to 256 bytes, and the
+// outputs are laid out back to back after the bytes the region handed out in
+// earlier waves (*bump).  A join whose output does not fit is left unplaced
+// (total 0, no columns; the host writes it itself); the offsets only grow,
+// so every later join with rows is unplaced too.  The same arithmetic on the
+// host (place_outputs_on_host) reproduces every placement from the totals.
+constexpr int kPlaceBlock = 1024;
+
+__host__ __device__ inline uint64_t place_stride(uint64_t rows) { return (rows * 4 + 255) / 256 * 256; }
+
+struct JoinPlace {
+  char* base;            // the region
+  uint64_t cap;          // its bytes
+  uint64_t* bump;        // bytes handed out before this wave (updated)
+  uint64_t* ostart;      // J + 1 output-tile starts (written)
+};
+
+__global__ void __launch_bounds__(kPlaceBlock) join_place_kernel(JoinOut* __restrict__ jo,
+                                                                 const uint64_t* __restrict__ totals, uint32_t J,
+                                                                 JoinPlace pl) {
+  __shared__ uint64_t s_scan[kPlaceBlock / 32 + 1];
+  const uint64_t bump0 = *pl.bump;
+  uint64_t carry_b = 0, carry_t = 0, fit_b = 0;
+  for (uint32_t c0 = 0; c0 < J; c0 += kPlaceBlock) {
+    const uint32_t j = c0 + threadIdx.x;
+    const uint64_t t = j < J ? totals[j] : 0;
+    const uint32_t ncols = j < J ? jo[j].nlc + jo[j].nrc : 0;
+    const uint64_t stride = place_stride(t);
+    const uint64_t bytes = t ? ncols * stride : 0;
+    uint64_t tot_b, tot_t, fb_sum;
+    const uint64_t eb = block_excl_scan64<kPlaceBlock>(bytes, tot_b, s_scan);
+    const uint64_t off = bump0 + carry_b + eb;
+    const bool fits = off + bytes <= pl.cap;
+    const uint64_t tiles = (fits && t) ? div_up(t, kTileRows) : 0;
+    const uint64_t et = block_excl_scan64<kPlaceBlock>(tiles, tot_t, s_scan);
+    (void)block_excl_scan64<kPlaceBlock>(fits ? bytes : 0, fb_sum, s_scan);
+    if (j < J) {
+      JoinOut& o = jo[j];
+      o.total = fits ? t : 0;
+      for (uint32_t c = 0; c < VG_MAX_COLS; ++c)
+        o.oc[c] = (fits && t && c < ncols) ? reinterpret_cast<uint32_t*>(pl.base + off + c * stride) : nullptr;
+      pl.ostart[j] = carry_t + et;
+    }
+    carry_b += tot_b;
+    carry_t += tot_t;
+    fit_b += fb_sum;
+  }
+  if (threadIdx.x == 0) {
+    pl.ostart[J] = carry_t;
+    *pl.bump = bump0 + fit_b;
+  }
+}
+
+// tile_join[ostart[j] .. ostart[j + 1]) = j.
+__global__ void tile_join_fill_kernel(const uint64_t* __restrict__ ostart, uint32_t J,
+                                      uint32_t* __restrict__ tile_join) {
+  for (uint32_t j = blockIdx.x; j < J; j += gridDim.x)
+    for (uint64_t t = ostart[j] + threadIdx.x; t < ostart[j + 1]; t += blockDim.x) tile_join[t] = j;
+}
+
+// Column 0 of small join outputs (2 < rows < kSmallC0Words) into stage slots
+// of kSmallC0Words words, for the joins whose slot is not negative (their
+// host-side completion scans it for empty intervals).
+__global__ void small_c0_kernel(const JoinOut* __restrict__ jo, uint32_t J, const int32_t* __restrict__ slot,
+                                uint32_t* __restrict__ stage) {
+  for (uint32_t j = blockIdx.x; j < J; j += gridDim.x) {
+    const int32_t s = slot[j];
+    const uint64_t t = jo[j].total;
+    if (s < 0 || t <= 2 || t >= kSmallC0Words) continue;
+    for (uint32_t i = threadIdx.x; i < t; i += blockDim.x)
+      stage[static_cast<uint64_t>(s) * kSmallC0Words + i] = jo[j].oc[0][i];
+  }
+}
+
 __global__ void first_last_kernel(const JoinOut* __restrict__ jo, uint32_t J, uint32_t* __restrict__ fl) {
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= J) return;
@@ -599,6 +676,99 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
   ctx.free(dfl);
   ctx.free(djo);
   jb.release(ctx);
+}
+
+uint64_t place_outputs_on_host(const JoinBatch& jb, const uint64_t* totals, const Arena::Region* region,
+                               uint64_t bump, std::vector<Rel>& out, std::vector<uint8_t>& placed,
+                               int64_t& blocks) {
+  const uint32_t J = jb.J;
+  out.assign(J, Rel());
+  placed.assign(J, 0);
+  blocks = 0;
+  uint64_t off = bump, fit = 0;
+  for (uint32_t j = 0; j < J; ++j) {
+    const uint64_t t = totals[j];
+    const uint32_t ncols = jb.l[j]->ncols + jb.r[j]->ncols - 1;
+    const uint64_t stride = place_stride(t);
+    const uint64_t bytes = t ? ncols * stride : 0;
+    const bool fits = off + bytes <= region->bytes;
+    if (fits && t) {
+      Rel& r = out[j];
+      r.ncols = ncols;
+      r.nrows = t;
+      for (uint32_t c = 0; c < ncols; ++c) r.cols[c] = reinterpret_cast<uint32_t*>(region->begin + off + c * stride);
+      placed[j] = 1;
+      blocks += ncols;
+    }
+    if (fits) fit += bytes;
+    off += bytes;
+  }
+  return bump + fit;
+}
+
+void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* region, uint64_t* d_bump,
+                              const std::vector<int32_t>& c0_slot, uint32_t nslots, uint32_t* first_last_host,
+                              uint32_t* c0_host, uint64_t* bump_host) {
+  const uint32_t J = jb.J;
+  if (J == 0) return;
+  std::vector<JoinOut> jo(J);
+  parallel_for(J, [&](size_t j) {
+    const Rel* l = jb.l[j];
+    const Rel* r = jb.r[j];
+    JoinOut& o = jo[j];
+    std::memset(&o, 0, sizeof(o));
+    o.offs = jb.offs + jb.row0[j];
+    o.lo = jb.lo + jb.row0[j];
+    o.nl = l->nrows;
+    for (uint32_t c = 0; c < l->ncols; ++c) o.lc[c] = l->cols[c];
+    for (uint32_t c = 1; c < r->ncols; ++c) o.rc[c - 1] = r->cols[c];
+    o.nlc = l->ncols;
+    o.nrc = r->ncols - 1;
+  });
+  JoinOut* djo = upload(ctx, jo);
+  int32_t* dslot = upload(ctx, c0_slot);
+  uint64_t* dos = ctx.alloc<uint64_t>(J + 1);
+  // every placed output tile covers kTileRows rows of at least one 4-byte column
+  const uint64_t tile_cap = region->bytes / (4ull * kTileRows) + J + 1;
+  uint32_t* dtj = ctx.alloc<uint32_t>(tile_cap);
+  uint32_t* dfl = ctx.alloc<uint32_t>(2 * J);
+  uint32_t* dstage = ctx.alloc<uint32_t>(static_cast<uint64_t>(nslots ? nslots : 1) * kSmallC0Words);
+  VG_CUDA(cudaMemsetAsync(dfl, 0, 2 * J * sizeof(uint32_t), ctx.stream));
+  JoinPlace pl{region->begin, region->bytes, d_bump, dos};
+  ctx.launch("join_place", 16.0 * J, [&] {
+    join_place_kernel<<<1, kPlaceBlock, 0, ctx.stream>>>(djo, jb.d_totals, J, pl);
+  });
+  VG_CUDA(cudaGetLastError());
+  const unsigned jgrid = static_cast<unsigned>(std::min<uint64_t>(J, static_cast<uint64_t>(ctx.num_sms) * 8));
+  ctx.launch("join_tile_map", 0.0, [&] { tile_join_fill_kernel<<<jgrid, 128, 0, ctx.stream>>>(dos, J, dtj); });
+  VG_CUDA(cudaGetLastError());
+  // the tile count is on the device: a fixed grid loops over the tiles (the
+  // algorithmic bytes are added when the host reads the totals)
+  ctx.launch("join_write", 0.0, [&] {
+    bjoin_write_kernel<<<static_cast<unsigned>(ctx.num_sms) * 8, kBlock, 0, ctx.stream>>>(djo, dos, dtj, 0,
+                                                                                           dos + J);
+  });
+  VG_CUDA(cudaGetLastError());
+  ctx.launch("join_first_last", 8.0 * J, [&] {
+    first_last_kernel<<<static_cast<unsigned>(div_up(J, 128)), 128, 0, ctx.stream>>>(djo, J, dfl);
+  });
+  VG_CUDA(cudaGetLastError());
+  if (nslots) {
+    ctx.launch("col0_stage", 8.0 * nslots * kSmallC0Words, [&] {
+      small_c0_kernel<<<jgrid, 128, 0, ctx.stream>>>(djo, J, dslot, dstage);
+    });
+    VG_CUDA(cudaGetLastError());
+    VG_CUDA(cudaMemcpyAsync(c0_host, dstage, static_cast<size_t>(nslots) * kSmallC0Words * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, ctx.stream));
+  }
+  VG_CUDA(cudaMemcpyAsync(first_last_host, dfl, 2 * J * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
+  VG_CUDA(cudaMemcpyAsync(bump_host, d_bump, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.free(djo);
+  ctx.free(dslot);
+  ctx.free(dos);
+  ctx.free(dtj);
+  ctx.free(dfl);
+  ctx.free(dstage);
 }
 
 void JoinBatch::release(Ctx& ctx) {

@@ -81,6 +81,26 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
 // others are allocated and written.  Releases jb's device arrays.
 void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::vector<Rel>& out,
                         uint32_t* first_last_host, const uint8_t* skip = nullptr);
+
+constexpr uint32_t kSmallC0Words = 100;   // staged column-0 words per small join output
+
+// The join write without a host round trip after the count: the outputs are
+// placed on the device in `region` (its bump pointer at d_bump, whose value
+// after the wave is copied to *bump_host), written, and their first/last
+// values copied to first_last_host and, for the joins with c0_slot[j] >= 0
+// and 2 < rows < kSmallC0Words, column 0 to c0_host + slot * kSmallC0Words.
+// Outputs that do not fit stay unplaced.  jb's device arrays stay alive:
+// place_outputs_on_host then tells which joins were placed (the same
+// arithmetic on the copied totals), and the caller writes the others with
+// batched_join_write(..., skip = placed), or releases jb.
+void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* region, uint64_t* d_bump,
+                              const std::vector<int32_t>& c0_slot, uint32_t nslots, uint32_t* first_last_host,
+                              uint32_t* c0_host, uint64_t* bump_host);
+// Returns the region's bump after the wave; out[j] is the placed output of
+// join j (placed[j] = 1) and `blocks` the number of its columns in the region.
+uint64_t place_outputs_on_host(const JoinBatch& jb, const uint64_t* totals, const Arena::Region* region,
+                               uint64_t bump, std::vector<Rel>& out, std::vector<uint8_t>& placed,
+                               int64_t& blocks);
 void batched_join(Ctx& ctx, const std::vector<const Rel*>& l, const std::vector<const Rel*>& r,
                   std::vector<Rel>& out, std::vector<uint32_t>& first_last);
 

@@ -408,8 +408,21 @@ WaveEngine::~WaveEngine() {
   bury();
   if (a_pending_ || b_pending_) cudaStreamSynchronize(ctx_.stream);
   for (auto& r : jouts_) rel_free(ctx_, r);
+  if (jb_.lo || jb_.offs || jb_.d_totals) jb_.release(ctx_);
+  if (d_bump_) ctx_.free(d_bump_);
+  // the region goes back to the arena when its last output is freed
+  if (region_) ctx_.arena.region_close(region_);
   if (ev_a_) cudaEventDestroy(ev_a_);
   if (ev_b_) cudaEventDestroy(ev_b_);
+}
+
+void WaveEngine::use_region(size_t bytes) {
+  if (region_ || bytes == 0) return;
+  region_ = ctx_.arena.region_open(bytes);
+  if (!region_) return;
+  d_bump_ = ctx_.alloc<uint64_t>(1);
+  VG_CUDA(cudaMemsetAsync(d_bump_, 0, sizeof(uint64_t), ctx_.stream));
+  region_bump_ = 0;
 }
 
 void WaveEngine::add(PlannedQuery* pq) { active_.push_back(pq); }
@@ -454,7 +467,18 @@ void WaveEngine::finish_wave() {
   const uint32_t* jfl = nullptr;
   if (!joins_.empty()) {
     const uint64_t* hb = h_b_.data();
-    jfl = reinterpret_cast<const uint32_t*>(hb + off_fl_);
+    if (placed_wave_) {
+      // placed joins' first/last came with stage A; the others' with stage B
+      const uint32_t* fb = reinterpret_cast<const uint32_t*>(hb + off_fl_);
+      for (size_t m = 0; m < joins_.size(); ++m)
+        if (!placed_[m]) {
+          jfl_[2 * m] = fb[2 * m];
+          jfl_[2 * m + 1] = fb[2 * m + 1];
+        }
+      jfl = jfl_.data();
+    } else {
+      jfl = reinterpret_cast<const uint32_t*>(hb + off_fl_);
+    }
     const uint32_t* c0 = reinterpret_cast<const uint32_t*>(hb + off_jc0_);
     uint64_t off = 0;
     for (size_t m : jsmall_) {
@@ -602,11 +626,24 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     }
   }
   const size_t c0_words = (col0_words(swap_rels) + 1) / 2;
+  // joins placed on the device: the small outputs whose column 0 the host
+  // scans get staging slots
+  placed_wave_ = region_ != nullptr && !jl.empty();
+  uint32_t nslots = 0;
+  if (placed_wave_) {
+    c0_slot_.assign(jl.size(), -1);
+    for (size_t m = 0; m < joins_.size(); ++m)
+      if (!items_[joins_[m]].jj->isLastJoinForVar()) c0_slot_[m] = static_cast<int32_t>(nslots++);
+  }
   off_tot_ = 0;
   off_fin_ = off_tot_ + jl.size();
   off_err_ = off_fin_ + fin_seg_.size();
   off_c0_ = off_err_ + 1;
-  uint64_t* ha = h_a_.reserve(off_c0_ + c0_words + 1);
+  off_fla_ = off_c0_ + c0_words;
+  off_bump_ = off_fla_ + (placed_wave_ ? jl.size() : 0);
+  off_c0a_ = off_bump_ + 1;
+  const size_t c0a_words = placed_wave_ ? (static_cast<size_t>(nslots) * kSmallC0Words + 1) / 2 : 0;
+  uint64_t* ha = h_a_.reserve(off_c0a_ + c0a_words + 1);
   bool any = false;
   if (!to_sort.empty()) {
     batched_sort_by_first(ctx_, to_sort, key_bits_);
@@ -626,6 +663,10 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     // gave up leaves the offsets wrong, and stage B must then not write
     VG_CUDA(cudaMemcpyAsync(ha + off_err_, ctx_.d_err, sizeof(DeviceErrors), cudaMemcpyDeviceToHost,
                             ctx_.stream));
+    if (placed_wave_)
+      batched_join_place_write(ctx_, jb_, region_, d_bump_, c0_slot_, nslots,
+                               reinterpret_cast<uint32_t*>(ha + off_fla_), reinterpret_cast<uint32_t*>(ha + off_c0a_),
+                               ha + off_bump_);
     any = true;
   }
   if (!fin_seg_.empty()) {
@@ -711,7 +752,68 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
 
   // device half 2: join outputs
   t0 = Clock::now();
-  if (!joins_.empty()) {
+  if (!joins_.empty() && placed_wave_) {
+    DeviceErrors he;
+    std::memcpy(&he, ha + off_err_, sizeof(he));
+    if (he.timeout) ctx_.raise_device_errors(he);
+    const uint64_t* tot = ha + off_tot_;
+    const size_t J = joins_.size();
+    int64_t blocks = 0;
+    const uint64_t nb = place_outputs_on_host(jb_, tot, region_, region_bump_, jouts_, placed_, blocks);
+    if (nb != ha[off_bump_]) fail(VG_ERR_CUDA, "join output placement differs between device and host");
+    region_bump_ = nb;
+    ctx_.arena.region_adopt(region_, blocks);
+    const uint32_t* fla = reinterpret_cast<const uint32_t*>(ha + off_fla_);
+    const uint32_t* c0a = reinterpret_cast<const uint32_t*>(ha + off_c0a_);
+    jfl_.assign(2 * J, 0);
+    std::vector<size_t> fb_small;
+    bool fallback = false;
+    double wbytes = 0;
+    for (size_t m = 0; m < J; ++m) {
+      if (tot[m] > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
+      const uint32_t ncols = jb_.l[m]->ncols + jb_.r[m]->ncols - 1;
+      if (placed_[m]) {
+        wbytes += 4.0 * tot[m] * (2.0 * ncols - 1);
+        jfl_[2 * m] = fla[2 * m];
+        jfl_[2 * m + 1] = fla[2 * m + 1];
+        if (c0_slot_[m] >= 0 && tot[m] > 2 && tot[m] < kSmallC0Words) {
+          Item& it = items_[joins_[m]];
+          const uint32_t* src = c0a + static_cast<size_t>(c0_slot_[m]) * kSmallC0Words;
+          it.c0.assign(src, src + tot[m]);
+          it.has_c0 = true;
+        }
+      } else if (tot[m] == 0) {
+        jouts_[m] = rel_alloc(ctx_, ncols, 0);
+        placed_[m] = 1;                     // nothing to write
+      } else {
+        fallback = true;
+        if (c0_slot_[m] >= 0 && tot[m] > 2 && tot[m] < kSmallC0Words) fb_small.push_back(m);
+      }
+    }
+    ctx_.add_bytes("join_write", wbytes);
+    if (!fallback) {
+      jb_.release(ctx_);
+      jsmall_.clear();
+    } else {
+      // outputs that did not fit the region: allocated and written after this round trip
+      uint64_t small_rows = 0;
+      for (size_t m : fb_small) small_rows += tot[m];
+      off_fl_ = 0;
+      off_jc0_ = (2 * J + 1) / 2;
+      uint64_t* hb = h_b_.reserve(off_jc0_ + (small_rows + 1) / 2 + 1);
+      batched_join_write(ctx_, jb_, tot, jouts_, reinterpret_cast<uint32_t*>(hb + off_fl_), placed_.data());
+      std::vector<const Rel*> small;
+      for (size_t m : fb_small) small.push_back(&jouts_[m]);
+      batched_col0_enqueue(ctx_, small, reinterpret_cast<uint32_t*>(hb + off_jc0_));
+      jsmall_ = std::move(fb_small);
+      VG_CUDA(cudaEventRecord(ev_b_, ctx_.stream));
+      b_pending_ = true;
+    }
+    if (tracing) {
+      tr.joins = static_cast<uint32_t>(J);
+      for (size_t m = 0; m < J; ++m) tr.join_out_rows += tot[m];
+    }
+  } else if (!joins_.empty()) {
     DeviceErrors he;
     std::memcpy(&he, ha + off_err_, sizeof(he));
     if (he.timeout) ctx_.raise_device_errors(he);
@@ -841,6 +943,9 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
     out.host = std::make_unique<HostResults>(ctx);
     for (auto& e : eng) e->set_host_results(out.host.get());
   }
+  // each engine places its join outputs on the device, in a region of its own
+  const size_t region_bytes = join_region_bytes(ctx, ne);
+  for (auto& e : eng) e->use_region(region_bytes);
   const char* trace_path = std::getenv("VG_WAVE_TRACE");
   for (auto& e : eng) {
     e->tracing = trace_path != nullptr;
@@ -912,6 +1017,17 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
 }
 
 void parallel_for(size_t n, const std::function<void(size_t)>& f) { WorkerPool::get().run(n, f); }
+
+size_t join_region_bytes(const Ctx& ctx, size_t engines) {
+  // VG_JOIN_REGION_MB per engine (default 4096; 0 turns device-side placement
+  // off), at most an eighth of the arena shared by the engines
+  long mb = 4096;
+  if (const char* e = std::getenv("VG_JOIN_REGION_MB")) mb = std::strtol(e, nullptr, 10);
+  if (mb <= 0) return 0;
+  const size_t want = static_cast<size_t>(mb) << 20;
+  const size_t cap = ctx.arena.capacity() / (8 * std::max<size_t>(engines, 1));
+  return std::min(want, cap);
+}
 
 size_t batch_engines() {
   static const size_t n = [] {

@@ -84,6 +84,9 @@ void release_later(std::vector<PlannedQuery>& pq);
 // Wave engines of one run_batch, each on its own host thread with its own
 // share of the host worker threads (VG_BATCH_ENGINES, 1..8; default 4).
 size_t batch_engines();
+// Bytes of the region in which each of `engines` wave engines places its join
+// outputs on the device (0: no region).
+size_t join_region_bytes(const Ctx& ctx, size_t engines);
 void prepare_mirrors(vedas::VedasStorage* storage);
 
 // Advances every added query by one job per wave; the device work of a wave
@@ -119,6 +122,11 @@ class WaveEngine {
   void step(std::vector<PlannedQuery*>& completed);
   // Copies each finished query's result to the host as it finishes.
   void set_host_results(HostResults* h) { host_ = h; }
+  // Places the join outputs of every wave on the device, in a region of
+  // `bytes` of the arena (when one is free), so that a wave's join write
+  // follows its count without a host round trip; outputs that do not fit
+  // are written after one, as without a region.
+  void use_region(size_t bytes);
   // Destroys the plans of handed-back queries that are still pending.
   void bury();
   uint32_t waves() const { return waves_; }
@@ -179,7 +187,16 @@ class WaveEngine {
   // device -> host results of each stage and the events that mark them
   PinnedWords h_a_{ctx_}, h_b_{ctx_};
   size_t off_tot_ = 0, off_fin_ = 0, off_c0_ = 0, off_err_ = 0;   // words into h_a_
+  size_t off_fla_ = 0, off_bump_ = 0, off_c0a_ = 0;               // words into h_a_ (placed joins)
   size_t off_fl_ = 0, off_jc0_ = 0;                               // words into h_b_
+  // device-side placement of join outputs (use_region)
+  Arena::Region* region_ = nullptr;
+  uint64_t* d_bump_ = nullptr;     // device: region bytes handed out
+  uint64_t region_bump_ = 0;       // the same on the host, as of the last wave read back
+  bool placed_wave_ = false;       // the wave in flight placed its joins on the device
+  std::vector<int32_t> c0_slot_;   // per join of the wave: its small column-0 slot, or -1
+  std::vector<uint8_t> placed_;    // per join: written by the device-side placement
+  std::vector<uint32_t> jfl_;      // per join: first and last key of the output
   cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;
   bool a_pending_ = false, b_pending_ = false;
 };

@@ -237,6 +237,16 @@ void* Arena::alloc(size_t bytes) {
 
 void Arena::free(void* p) {
   if (!p) return;
+  if (nregions_.load(std::memory_order_acquire) > 0) {
+    char* c = static_cast<char*>(p);
+    for (int i = 0; i < kRegions; ++i) {
+      char* lo = region_lo_[i].load(std::memory_order_acquire);
+      if (lo && c >= lo && c < region_hi_[i].load(std::memory_order_acquire)) {
+        region_unref(i);
+        return;
+      }
+    }
+  }
   const size_t off = static_cast<size_t>(static_cast<char*>(p) - base_);
   if (!base_ || off >= cap_) fail(VG_ERR_INVALID, "arena free of a pointer outside the slab");
   const int c = small_class(off);
@@ -270,6 +280,52 @@ void Arena::free(void* p) {
   live_.erase(it);
   big_used_ -= sz;
   big_free(off, sz);
+}
+
+Arena::Region* Arena::region_open(size_t bytes) {
+  bytes = std::max(bytes, kSmallMax + kAlign);      // always a large block
+  void* p = try_alloc(bytes);
+  if (!p) return nullptr;
+  std::lock_guard<std::mutex> lk(region_mu_);
+  for (int i = 0; i < kRegions; ++i) {
+    if (region_lo_[i].load(std::memory_order_acquire) || regions_[i].refs.load() != 0) continue;
+    Region& r = regions_[i];
+    r.begin = static_cast<char*>(p);
+    r.bytes = bytes;
+    r.refs.store(1);
+    region_hi_[i].store(r.begin + bytes, std::memory_order_release);
+    region_lo_[i].store(r.begin, std::memory_order_release);
+    nregions_.fetch_add(1, std::memory_order_acq_rel);
+    return &r;
+  }
+  free(p);
+  return nullptr;
+}
+
+void Arena::region_adopt(Region* r, int64_t blocks) {
+  if (r && blocks > 0) r->refs.fetch_add(blocks, std::memory_order_acq_rel);
+}
+
+void Arena::region_close(Region* r) {
+  if (!r) return;
+  region_unref(static_cast<int>(r - regions_));
+}
+
+void Arena::region_unref(int slot) {
+  Region& r = regions_[slot];
+  if (r.refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
+  // the last reference: the slot is cleared before the block goes back, so no
+  // later free of a block carved from the same bytes is taken for the region's
+  char* b = r.begin;
+  {
+    std::lock_guard<std::mutex> lk(region_mu_);
+    region_lo_[slot].store(nullptr, std::memory_order_release);
+    region_hi_[slot].store(nullptr, std::memory_order_release);
+    nregions_.fetch_sub(1, std::memory_order_acq_rel);
+    r.begin = nullptr;
+    r.bytes = 0;
+  }
+  free(b);
 }
 
 void Arena::shrink(void* p, size_t new_bytes) {

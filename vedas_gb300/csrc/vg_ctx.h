@@ -62,6 +62,22 @@ class Arena {
   size_t peak() const;
   size_t largest_free() const;
 
+  // Regions: one large block whose interior another allocator hands out (a
+  // bump pointer on the device, which places every join output of a wave
+  // without a host round trip).  The region holds one reference for its
+  // opener; region_adopt adds one per interior block the host learns was
+  // handed out, free() of an interior pointer drops one, and region_close
+  // drops the opener's.  The block returns to the arena with the last
+  // reference, so interior blocks may outlive the opener.
+  struct Region {
+    char* begin = nullptr;
+    size_t bytes = 0;
+    std::atomic<int64_t> refs{0};
+  };
+  Region* region_open(size_t bytes);      // nullptr when no block of that size is free or no slot is left
+  void region_adopt(Region* r, int64_t blocks);
+  void region_close(Region* r);
+
   static constexpr size_t kAlign = 256;
   static constexpr int kClasses = 16;                  // 256 B .. 8 MiB
   static constexpr size_t kSmallMax = kAlign << (kClasses - 1);
@@ -95,6 +111,15 @@ class Arena {
   std::unique_ptr<std::atomic<int8_t>[]> chunk_class_;
   size_t nchunks_ = 0;
   std::unique_ptr<Shard[]> shards_;
+
+  static constexpr int kRegions = 64;
+  Region regions_[kRegions];
+  // [lo, hi) of each open region (lo null: slot free), read by free() without a lock
+  std::atomic<char*> region_lo_[kRegions] = {};
+  std::atomic<char*> region_hi_[kRegions] = {};
+  std::atomic<int> nregions_{0};
+  std::mutex region_mu_;
+  void region_unref(int slot);
 
   void setup(char* base, size_t bytes, bool owned);
   size_t big_alloc(size_t bytes);                      // SIZE_MAX when it does not fit
