@@ -47,7 +47,9 @@ def parse():
                     help="batch: the 4096-query batch (default); plain: the same queries one at a "
                          "time; serve: Poisson arrivals on the hub graph; c3: the large snowflake "
                          "query on the 500M-triple hub graph")
-    ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (q/s)")
+    ap.add_argument("--rate", default="2000", help="serve: Poisson arrival rates (q/s), comma-separated")
+    ap.add_argument("--clients", type=int, default=4, help="serve: submitter threads")
+    ap.add_argument("--serve-pool", type=int, default=20000, help="serve: distinct queries drawn from")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: relation memory budget")
     ap.add_argument("--triples", type=int, default=None,
@@ -617,72 +619,106 @@ def bench_c3(args, rank, world, local, pg):
     ctx.close()
 
 
-def bench_serve(args, rank, world, local, pg):
-    """Serving: the hub graph resident in HBM, Poisson arrivals, continuous
-    batching with memory-budget admission; p50/p95/p99 latency and sustained
-    queries/s over all ranks (replicas)."""
-    import vedas_gb300 as vg
-    from vedas_gb300 import workloads
-    g = workloads.graph_hub(n=args.triples, n_entities=args.entities, seed=args.seed, dedup=False)
-    cs = workloads.ConstantSampler(g)
-    n_q = int(args.rate * args.duration)
-    qs = workloads.query_mix(g, n_q, seed=args.seed + 7 + 1000 * rank, cs=cs,
-                             mix={"S": 0.6, "C": 0.3, "F": 0.1})
-    rng = np.random.Generator(np.random.PCG64(args.seed + 99 + rank))
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n_q))
-    ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
-    ix = vg.Index(ctx, g.s, g.p, g.o)
-    srv = vg.Server(ix, budget_bytes=int(args.budget_gb * (1 << 30)))
-    for t in srv.submit_many(qs[:256]):     # warm-up: first waves, host mirrors
-        srv.wait(t)
-        srv.release(t)
-    barrier(pg)
-    # the client submits every query whose arrival time has come, in one call;
-    # a query's latency runs from its scheduled arrival to its completion
-    tickets, late = [], []
-    qb = [q.encode() for q in qs]
+def serve_point(srv, qb, rate, duration, clients, seed):
+    """One offered rate: Poisson arrivals over `duration` seconds, split over
+    `clients` submitter threads (arrival i goes to thread i % clients); each
+    thread submits its due queries in one call.  A query's latency runs from
+    its scheduled arrival to its completion."""
+    n_q = int(rate * duration)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_q))
+    picks = rng.integers(0, len(qb), size=n_q)
+    tickets = [None] * n_q
+    late = np.zeros(n_q)
     t0 = time.perf_counter()
-    i = 0
-    while i < n_q:
-        now = time.perf_counter() - t0
-        if arrivals[i] > now:
-            time.sleep(min(arrivals[i] - now, 0.0005))
-            continue
-        j = int(np.searchsorted(arrivals, now, side="right"))
-        sub = time.perf_counter() - t0
-        tickets.extend(srv.submit_many(qb[i:j]))
-        late.extend(sub - arrivals[i:j])
-        i = j
+
+    def client(c):
+        mine = np.arange(c, n_q, clients)
+        k = 0
+        while k < len(mine):
+            now = time.perf_counter() - t0
+            if arrivals[mine[k]] > now:
+                time.sleep(min(arrivals[mine[k]] - now, 0.0005))
+                continue
+            e = k + int(np.searchsorted(arrivals[mine[k:]], now, side="right"))
+            idx = mine[k:e]
+            sub = time.perf_counter() - t0
+            for i, t in zip(idx, srv.submit_many([qb[j] for j in picks[idx]])):
+                tickets[i] = t
+                late[i] = sub - arrivals[i]
+            k = e
+
+    th = [threading.Thread(target=client, args=(c,)) for c in range(clients)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
     lat, ok, rej = [], 0, 0
-    for t, lt in zip(tickets, late):
+    for i, t in enumerate(tickets):
         srv.wait(t)
         st = srv.status(t)
         _, tot = srv.latency(t)
         if st == 0:
             ok += 1
-            lat.append(tot + max(lt, 0.0))
+            lat.append(tot + max(late[i], 0.0))
         else:
             rej += 1
         srv.release(t)
     wall = time.perf_counter() - t0
+    return {"offered_rate": rate, "queries": n_q, "served_rate": ok / wall, "completed": ok,
+            "failed_or_rejected": rej, "wall_s": wall,
+            "latency_ms": {"p50": 1000 * float(np.percentile(lat, 50)), "p95": 1000 * float(np.percentile(lat, 95)),
+                           "p99": 1000 * float(np.percentile(lat, 99))}}
+
+
+def bench_serve(args, rank, world, local, pg):
+    """Serving: the hub graph resident in HBM, Poisson arrivals from several
+    client threads, continuous batching with memory-budget admission;
+    p50/p95/p99 latency and sustained queries/s over all ranks (replicas) at
+    each offered rate (--rate, comma-separated: the first is the headline)."""
+    import vedas_gb300 as vg
+    from vedas_gb300 import workloads
+    rates = [float(x) for x in str(args.rate).split(",")]
+    g = dedup_on_device(workloads.graph_hub(n=args.triples, n_entities=args.entities, seed=args.seed,
+                                            dedup=False), local)
+    note(f"hub graph: {g.n} triples")
+    cs = workloads.ConstantSampler(g)
+    # a pool of instantiated queries with the 60/30/10 star/chain/snowflake mix
+    pool = workloads.query_mix(g, args.serve_pool, seed=args.seed + 7 + 1000 * rank, cs=cs,
+                               mix={"S": 0.6, "C": 0.3, "F": 0.1})
+    qb = [q.encode() for q in pool]
+    note(f"{len(pool)} queries instantiated")
+    ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    del g, cs
+    srv = vg.Server(ix, budget_bytes=int(args.budget_gb * (1 << 30)))
+    for t in srv.submit_many(qb[:256]):     # warm-up: first waves, host mirrors
+        srv.wait(t)
+        srv.release(t)
+    points = []
+    for k, rate in enumerate(rates):
+        barrier(pg)
+        pt = serve_point(srv, qb, rate, args.duration, args.clients, args.seed + 99 + rank + 17 * k)
+        pt["served_rate"] = sum_over_ranks(pg, pt["served_rate"])
+        points.append(pt)
+        note(f"rate {rate:.0f}: served {pt['served_rate']:.0f} q/s, p50 {pt['latency_ms']['p50']:.2f} ms, "
+             f"p99 {pt['latency_ms']['p99']:.2f} ms")
     stats = srv.stats()
     srv.stop()
-    wall_max = max_over_ranks(pg, wall)
-    total_ok = sum_over_ranks(pg, float(ok))
     if rank == 0:
+        head = points[0]
         line = {
-            "metric": "serving queries/s", "value": total_ok / wall_max, "unit": UNIT, "n_gpus": world,
+            "metric": "serving queries/s", "value": head["served_rate"], "unit": UNIT, "n_gpus": world,
             "higher_is_better": True, "scaling": "weak", "dtype": "u32",
             "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": f"Poisson arrivals at {args.rate:.0f} q/s for {args.duration:.0f} s, "
-                                   f"60/30/10 star/chain/snowflake templates, on the "
-                                   f"{triples_label(args.triples)}-triple hub graph",
-                       "budget_gb": args.budget_gb, "queries": n_q, "failed_or_rejected": rej,
+            "config": {"workload": f"Poisson arrivals at {rates[0]:.0f} q/s for {args.duration:.0f} s from "
+                                   f"{args.clients} client threads, 60/30/10 star/chain/snowflake templates, on "
+                                   f"the {triples_label(args.triples)}-triple hub graph",
+                       "budget_gb": args.budget_gb, "query_pool": len(pool), "clients": args.clients,
                        "waves": stats["waves"], "peak_inflight": stats["peak_inflight"]},
-            "latency_ms": {"p50": 1000 * float(np.percentile(lat, 50)),
-                           "p95": 1000 * float(np.percentile(lat, 95)),
-                           "p99": 1000 * float(np.percentile(lat, 99))},
-            "offered_rate": args.rate,
+            "latency_ms": head["latency_ms"],
+            "offered_rate": rates[0],
+            "points": points,
         }
         print(json.dumps(line), flush=True)
     ix.close()
