@@ -196,10 +196,56 @@ struct JoinSeg {
 // and a segmented decoupled look-back over the join's earlier tiles give
 // every left key its output offset directly, and the join's last tile writes
 // its total.
+//
+// Joins with at most kSmallJoin left rows (most joins of a wave have a few)
+// take one warp each instead: the first small_blocks blocks hold
+// kJcBlock / 32 such joins, one per warp.  The warp finds the join's window
+// of right keys with two 32-ary searches, each lane counts the matches of
+// its kJcKeys keys with lockstep searches in that window, and a warp scan
+// gives the offsets and the total (no shared memory, no look-back).
+constexpr uint32_t kSmallJoin = 32 * kJcKeys;
+
+__device__ __forceinline__ void count_small_join(const JoinSeg& g, uint32_t* __restrict__ lo,
+                                                 uint64_t* __restrict__ offs, uint64_t* total) {
+  const uint32_t lane = lane_id();
+  const uint64_t nl = g.nl;
+  const uint64_t w0 = warp_bound<false, uint32_t>(g.rk, 0, g.nr, g.lk[0]);
+  const uint64_t w1 = warp_bound<true, uint32_t>(g.rk, w0, g.nr, g.lk[nl - 1]);
+  const uint64_t first = static_cast<uint64_t>(lane) * kJcKeys;
+  uint32_t key[kJcKeys];
+  uint64_t lb[kJcKeys], ub[kJcKeys];
+#pragma unroll
+  for (int q = 0; q < kJcKeys; ++q) key[q] = g.lk[first + q < nl ? first + q : nl - 1];
+  lockstep_bounds<kJcKeys>(g.rk, w0, w1, key, lb, ub);
+  uint64_t sum = 0;
+#pragma unroll
+  for (int q = 0; q < kJcKeys; ++q)
+    if (first + q < nl) sum += ub[q] - lb[q];
+  const uint64_t incl = warp_incl_scan64(sum);
+  uint64_t run = incl - sum;
+#pragma unroll
+  for (int q = 0; q < kJcKeys; ++q)
+    if (first + q < nl) {
+      lo[g.row0 + first + q] = static_cast<uint32_t>(lb[q]);
+      offs[g.row0 + first + q] = run;
+      run += ub[q] - lb[q];
+    }
+  if (lane == 31) *total = incl;
+}
+
 __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
     const JoinSeg* __restrict__ js, const uint64_t* __restrict__ bstart, const uint32_t* __restrict__ tile_join,
-    uint32_t* __restrict__ lo, uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket,
-    uint64_t* __restrict__ totals, DeviceErrors* err) {
+    const uint32_t* __restrict__ small, uint32_t nsmall, uint32_t small_blocks, uint32_t* __restrict__ lo,
+    uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket, uint64_t* __restrict__ totals,
+    DeviceErrors* err) {
+  if (blockIdx.x < small_blocks) {   // block-uniform: this block only counts small joins
+    const uint64_t sj = static_cast<uint64_t>(blockIdx.x) * (kJcBlock / 32) + (threadIdx.x >> 5);
+    if (sj < nsmall) {
+      const uint32_t j = small[sj];
+      count_small_join(js[j], lo, offs, &totals[j]);
+    }
+    return;
+  }
   __shared__ JoinCountSmem sm;
   __shared__ uint64_t s_scan[kJcBlock / 32 + 1];
   __shared__ uint64_t s_b;
@@ -256,15 +302,60 @@ struct JoinOut {
 // shared memory, and each thread walks its rows (k increasing, consecutive
 // threads on consecutive rows, so loads and stores coalesce) from the
 // previous one's left row.  Hub keys thus spread over many blocks.
+//
+// Small outputs (at most kSmallOut rows of a join with at most kSmallJoin
+// left rows; most outputs of a wave) are written one join per warp first,
+// before the tiles: the warp stages the join's offsets and lower bounds in
+// its own slice of the shared arrays and each lane writes every 32nd row.
+// Their list (small, nsmall of them; nsmall_dev when on the device) holds no
+// tiles.
+constexpr uint32_t kSmallOut = 1024;
+
+__device__ __forceinline__ void write_small_join(const JoinOut* __restrict__ jp, uint64_t* s_off, uint32_t* s_lo) {
+  const uint32_t lane = lane_id();
+  const uint64_t total = jp->total, nl = jp->nl;
+  const uint64_t* offs = jp->offs;
+  const uint32_t* lov = jp->lo;
+  for (uint32_t e = lane; e < nl; e += 32) {
+    s_off[e] = offs[e];
+    s_lo[e] = lov[e];
+  }
+  __syncwarp();
+  const uint32_t nlc = jp->nlc, nrc = jp->nrc;
+  for (uint64_t k = lane; k < total; k += 32) {
+    uint32_t a = 0, b = static_cast<uint32_t>(nl);   // last p with s_off[p] <= k
+    while (b - a > 1) {
+      const uint32_t mid = (a + b) >> 1;
+      if (s_off[mid] <= k) a = mid;
+      else b = mid;
+    }
+    const uint64_t jj = s_lo[a] + (k - s_off[a]);
+    uint32_t c = 0;
+    for (uint32_t x = 0; x < nlc; ++x) jp->oc[c++][k] = jp->lc[x][a];
+    for (uint32_t x = 0; x < nrc; ++x) jp->oc[c++][k] = jp->rc[x][jj];
+  }
+  __syncwarp();   // the slice is free for the warp's next join
+}
+
 __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __restrict__ jo,
                                                              const uint64_t* __restrict__ ostart,
                                                              const uint32_t* __restrict__ tile_join,
-                                                             uint64_t T_host, const uint64_t* ostart_end) {
+                                                             uint64_t T_host, const uint64_t* ostart_end,
+                                                             const uint32_t* __restrict__ small, uint32_t nsmall_host,
+                                                             const uint32_t* nsmall_dev) {
   constexpr int kStage = kTileRows + 1;
+  static_assert(kStage >= (kBlock / 32) * kSmallJoin, "a warp's slice holds a small join's left rows");
   __shared__ JoinOut s_o;
   __shared__ uint64_t s_off[kStage];
   __shared__ uint32_t s_lo[kStage];
   __shared__ uint64_t s_i[2];
+  {
+    const uint32_t nsm = nsmall_dev ? *nsmall_dev : nsmall_host;
+    const uint32_t warp = threadIdx.x >> 5, nwarps = kBlock / 32;
+    for (uint64_t w = static_cast<uint64_t>(blockIdx.x) * nwarps + warp; w < nsm;
+         w += static_cast<uint64_t>(gridDim.x) * nwarps)
+      write_small_join(&jo[small[w]], s_off + warp * kSmallJoin, s_lo + warp * kSmallJoin);
+  }
   const uint64_t T = ostart_end ? *ostart_end : T_host;
 #pragma unroll 1
   for (uint64_t tile = blockIdx.x; tile < T; tile += gridDim.x) {
@@ -341,7 +432,9 @@ struct JoinPlace {
   char* base;            // the region
   uint64_t cap;          // its bytes
   uint64_t* bump;        // bytes handed out before this wave (updated)
-  uint64_t* ostart;      // J + 1 output-tile starts (written)
+  uint64_t* ostart;      // J + 1 output-tile starts (written; small outputs have no tiles)
+  uint32_t* small;       // joins whose outputs are written one per warp (written)
+  uint32_t* nsmall;      // their number (written)
 };
 
 __global__ void __launch_bounds__(kPlaceBlock) join_place_kernel(JoinOut* __restrict__ jo,
@@ -349,7 +442,7 @@ __global__ void __launch_bounds__(kPlaceBlock) join_place_kernel(JoinOut* __rest
                                                                  JoinPlace pl) {
   __shared__ uint64_t s_scan[kPlaceBlock / 32 + 1];
   const uint64_t bump0 = *pl.bump;
-  uint64_t carry_b = 0, carry_t = 0, fit_b = 0;
+  uint64_t carry_b = 0, carry_t = 0, carry_s = 0, fit_b = 0;
   for (uint32_t c0 = 0; c0 < J; c0 += kPlaceBlock) {
     const uint32_t j = c0 + threadIdx.x;
     const uint64_t t = j < J ? totals[j] : 0;
@@ -360,22 +453,28 @@ __global__ void __launch_bounds__(kPlaceBlock) join_place_kernel(JoinOut* __rest
     const uint64_t eb = block_excl_scan64<kPlaceBlock>(bytes, tot_b, s_scan);
     const uint64_t off = bump0 + carry_b + eb;
     const bool fits = off + bytes <= pl.cap;
-    const uint64_t tiles = (fits && t) ? div_up(t, kTileRows) : 0;
+    const bool is_small = fits && t > 0 && t <= kSmallOut && j < J && jo[j].nl <= kSmallJoin;
+    const uint64_t tiles = (fits && t && !is_small) ? div_up(t, kTileRows) : 0;
     const uint64_t et = block_excl_scan64<kPlaceBlock>(tiles, tot_t, s_scan);
     (void)block_excl_scan64<kPlaceBlock>(fits ? bytes : 0, fb_sum, s_scan);
+    uint64_t tot_s;
+    const uint64_t es = block_excl_scan64<kPlaceBlock>(is_small ? 1 : 0, tot_s, s_scan);
     if (j < J) {
       JoinOut& o = jo[j];
       o.total = fits ? t : 0;
       for (uint32_t c = 0; c < VG_MAX_COLS; ++c)
         o.oc[c] = (fits && t && c < ncols) ? reinterpret_cast<uint32_t*>(pl.base + off + c * stride) : nullptr;
       pl.ostart[j] = carry_t + et;
+      if (is_small) pl.small[carry_s + es] = j;
     }
     carry_b += tot_b;
     carry_t += tot_t;
+    carry_s += tot_s;
     fit_b += fb_sum;
   }
   if (threadIdx.x == 0) {
     pl.ostart[J] = carry_t;
+    *pl.nsmall = static_cast<uint32_t>(carry_s);
     *pl.bump = bump0 + fit_b;
   }
 }
@@ -576,6 +675,7 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
   uint64_t rows = 0;
   double cbytes = 0;
   jb.row0.resize(J);
+  std::vector<uint32_t> small;   // joins counted by one warp each
   for (uint32_t j = 0; j < J; ++j) {
     if (l[j]->nrows == 0 || r[j]->nrows == 0) fail(VG_ERR_INVALID, "batched join of an empty relation");
     if (l[j]->nrows > 0xFFFFFFFFull || r[j]->nrows > 0xFFFFFFFFull)
@@ -584,9 +684,13 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
     js[j] = {l[j]->cols[0], r[j]->cols[0], l[j]->nrows, r[j]->nrows, rows};
     jb.row0[j] = rows;
     rows += l[j]->nrows;
-    bstart[j + 1] = bstart[j] + div_up(l[j]->nrows, kJcTile);
+    const bool is_small = l[j]->nrows <= kSmallJoin;
+    if (is_small) small.push_back(j);
+    bstart[j + 1] = bstart[j] + (is_small ? 0 : div_up(l[j]->nrows, kJcTile));
     cbytes += 4.0 * (l[j]->nrows + r[j]->nrows);
   }
+  const uint32_t nsmall = static_cast<uint32_t>(small.size());
+  const uint32_t small_blocks = static_cast<uint32_t>(div_up(nsmall, kJcBlock / 32));
   const uint64_t T = bstart[J];
   if (T > 0x7FFFFFFFull) fail(VG_ERR_OVERFLOW, "batched join count: too many tiles");
   std::vector<uint32_t> tile_join(T);
@@ -595,6 +699,7 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
   JoinSeg* djs = upload(ctx, js);
   uint64_t* dbs = upload(ctx, bstart);
   uint32_t* dtj = upload(ctx, tile_join);
+  uint32_t* dsm = upload(ctx, small);
   jb.lo = ctx.alloc<uint32_t>(rows);
   jb.offs = ctx.alloc<uint64_t>(rows);
   uint64_t* status = ctx.alloc<uint64_t>(T);
@@ -603,8 +708,8 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
   VG_CUDA(cudaMemsetAsync(status, 0, T * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), ctx.stream));
   ctx.launch("join_count_scan", cbytes + 12.0 * rows, [&] {
-    bjoin_count_scan_kernel<<<static_cast<unsigned>(T), kJcBlock, 0, ctx.stream>>>(
-        djs, dbs, dtj, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);
+    bjoin_count_scan_kernel<<<static_cast<unsigned>(small_blocks + T), kJcBlock, 0, ctx.stream>>>(
+        djs, dbs, dtj, dsm, nsmall, small_blocks, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaMemcpyAsync(totals_host, totals, J * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
@@ -615,6 +720,7 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
   ctx.free(djs);
   ctx.free(dbs);
   ctx.free(dtj);
+  ctx.free(dsm);
 }
 
 void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::vector<Rel>& out,
@@ -626,11 +732,16 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
   std::vector<uint64_t> ostart(J + 1, 0);
   double wbytes = 0;
   auto rows = [&](uint32_t j) -> uint64_t { return (skip && skip[j]) ? 0 : totals[j]; };
+  std::vector<uint32_t> small;   // outputs written one join per warp
   for (uint32_t j = 0; j < J; ++j) {
     if (rows(j) > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
-    ostart[j + 1] = ostart[j] + div_up(rows(j), kTileRows);
+    const bool is_small = rows(j) > 0 && rows(j) <= kSmallOut && jb.l[j]->nrows <= kSmallJoin;
+    if (is_small) small.push_back(j);
+    ostart[j + 1] = ostart[j] + (is_small ? 0 : div_up(rows(j), kTileRows));
     wbytes += 4.0 * rows(j) * (2.0 * (jb.l[j]->ncols + jb.r[j]->ncols - 1) - 1);
   }
+  const uint32_t nsmall = static_cast<uint32_t>(small.size());
+  const uint64_t small_blocks = div_up(nsmall, kBlock / 32);
   // the outputs of a wave's joins are allocated and described on the host pool
   parallel_for(J, [&](size_t j) {
     JoinOut& o = jo[j];
@@ -653,20 +764,22 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
   JoinOut* djo = upload(ctx, jo);
   uint32_t* dfl = ctx.alloc<uint32_t>(2 * J);
   VG_CUDA(cudaMemsetAsync(dfl, 0, 2 * J * sizeof(uint32_t), ctx.stream));
-  if (ostart[J] > 0) {
+  if (ostart[J] > 0 || nsmall > 0) {
     if (ostart[J] > 0x7FFFFFFFull) fail(VG_ERR_OVERFLOW, "batched join write: too many tiles");
     std::vector<uint32_t> tile_join(ostart[J]);
     for (uint32_t j = 0; j < J; ++j)
       for (uint64_t t = ostart[j]; t < ostart[j + 1]; ++t) tile_join[t] = j;
     uint64_t* dos = upload(ctx, ostart);
     uint32_t* dtj = upload(ctx, tile_join);
+    uint32_t* dsm = upload(ctx, small);
+    const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(ostart[J], small_blocks));
     ctx.launch("join_write", wbytes, [&] {
-      bjoin_write_kernel<<<static_cast<unsigned>(ostart[J]), kBlock, 0, ctx.stream>>>(djo, dos, dtj, ostart[J],
-                                                                                      nullptr);
+      bjoin_write_kernel<<<grid, kBlock, 0, ctx.stream>>>(djo, dos, dtj, ostart[J], nullptr, dsm, nsmall, nullptr);
     });
     VG_CUDA(cudaGetLastError());
     ctx.free(dos);
     ctx.free(dtj);
+    ctx.free(dsm);
   }
   ctx.launch("join_first_last", 8.0 * J, [&] {
     first_last_kernel<<<static_cast<unsigned>(div_up(J, 128)), 128, 0, ctx.stream>>>(djo, J, dfl);
@@ -728,13 +841,14 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
   JoinOut* djo = upload(ctx, jo);
   int32_t* dslot = upload(ctx, c0_slot);
   uint64_t* dos = ctx.alloc<uint64_t>(J + 1);
+  uint32_t* dsm = ctx.alloc<uint32_t>(J + 1);   // small list, then its length
   // every placed output tile covers kTileRows rows of at least one 4-byte column
   const uint64_t tile_cap = region->bytes / (4ull * kTileRows) + J + 1;
   uint32_t* dtj = ctx.alloc<uint32_t>(tile_cap);
   uint32_t* dfl = ctx.alloc<uint32_t>(2 * J);
   uint32_t* dstage = ctx.alloc<uint32_t>(static_cast<uint64_t>(nslots ? nslots : 1) * kSmallC0Words);
   VG_CUDA(cudaMemsetAsync(dfl, 0, 2 * J * sizeof(uint32_t), ctx.stream));
-  JoinPlace pl{region->begin, region->bytes, d_bump, dos};
+  JoinPlace pl{region->begin, region->bytes, d_bump, dos, dsm, dsm + J};
   ctx.launch("join_place", 16.0 * J, [&] {
     join_place_kernel<<<1, kPlaceBlock, 0, ctx.stream>>>(djo, jb.d_totals, J, pl);
   });
@@ -746,7 +860,7 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
   // algorithmic bytes are added when the host reads the totals)
   ctx.launch("join_write", 0.0, [&] {
     bjoin_write_kernel<<<static_cast<unsigned>(ctx.num_sms) * 8, kBlock, 0, ctx.stream>>>(djo, dos, dtj, 0,
-                                                                                           dos + J);
+                                                                                           dos + J, dsm, 0, dsm + J);
   });
   VG_CUDA(cudaGetLastError());
   ctx.launch("join_first_last", 8.0 * J, [&] {
@@ -766,6 +880,7 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
   ctx.free(djo);
   ctx.free(dslot);
   ctx.free(dos);
+  ctx.free(dsm);
   ctx.free(dtj);
   ctx.free(dfl);
   ctx.free(dstage);
