@@ -101,10 +101,53 @@ __global__ void __launch_bounds__(kBlock) bcopy_kernel(const CopyPiece* __restri
 }
 
 // ---------------------------------------------------------------------------
+// Adjacent-unique compaction of every segment.  Segments of at most
+// kSmallSeg rows (most final results) take one warp each in the first
+// small_blocks blocks: each lane flags its kRows consecutive rows, a warp
+// scan places the kept ones.  Larger segments take tiles of kTileRows rows
+// in ticket order (the tile's segment from a per-tile table), with a block
+// scan and a segmented look-back over the segment's earlier tiles.
+constexpr uint32_t kSmallSeg = 32 * kRows;
+
+__device__ __forceinline__ void unique_small_segment(const SegRows& g, uint64_t* count) {
+  const uint32_t lane = lane_id();
+  const uint64_t n = g.n, r0 = static_cast<uint64_t>(lane) * kRows;
+  uint32_t diff = (r0 == 0 && n > 0) ? 1u : 0u;
+  for (uint32_t c = 0; c < g.ncols; ++c) {
+    const uint32_t* col = g.in[c];
+    uint32_t prev = (r0 > 0 && r0 - 1 < n) ? col[r0 - 1] : 0u;
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+      const uint64_t r = r0 + i;
+      const uint32_t v = (r < n) ? col[r] : 0u;
+      if (r < n && r > 0 && v != prev) diff |= 1u << i;
+      prev = v;
+    }
+  }
+  if (r0 >= n) diff = 0;
+  else if (n - r0 < kRows) diff &= (1u << (n - r0)) - 1u;
+  const uint32_t cnt = __popc(diff);
+  const uint32_t incl = warp_incl_scan(cnt);
+  uint64_t o = incl - cnt;
+  for (int i = 0; i < kRows; ++i) {
+    if (!(diff >> i & 1u)) continue;
+    for (uint32_t c = 0; c < g.ncols; ++c) g.out[c][o] = g.in[c][r0 + i];
+    ++o;
+  }
+  if (lane == 31) *count = incl;
+}
+
 __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restrict__ segs,
-                                                         const uint64_t* __restrict__ tstart, uint32_t S,
-                                                         uint64_t* status, uint32_t* ticket,
+                                                         const uint64_t* __restrict__ tstart,
+                                                         const uint32_t* __restrict__ tile_seg,
+                                                         const uint32_t* __restrict__ small, uint32_t nsmall,
+                                                         uint32_t small_blocks, uint64_t* status, uint32_t* ticket,
                                                          uint64_t* counts, DeviceErrors* err) {
+  if (blockIdx.x < small_blocks) {   // block-uniform: this block only compacts small segments
+    const uint64_t w = static_cast<uint64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5);
+    if (w < nsmall) unique_small_segment(segs[small[w]], &counts[small[w]]);
+    return;
+  }
   __shared__ uint32_t s_scan[kBlock / 32 + 1];
   __shared__ uint64_t s_b;
   __shared__ uint32_t s_tile;
@@ -112,7 +155,7 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
   __shared__ uint32_t s_s;
   if (threadIdx.x == 0) {
     s_tile = atomicAdd(ticket, 1u);
-    s_s = seg_of(tstart, S, s_tile);
+    s_s = tile_seg[s_tile];
     s_seg = segs[s_s];
   }
   __syncthreads();
@@ -153,31 +196,66 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
 }
 
 // ---------------------------------------------------------------------------
+// Rows [r0, r0 + kBlock) of a grid-stride loop over segmented rows: the
+// block finds the segments of its first and last row once (two searches of
+// the segment starts), then each row searches only between those, which is
+// usually one or two segments.
+__device__ __forceinline__ uint32_t seg_of_row(const uint64_t* __restrict__ rstart, uint32_t k0, uint32_t k1,
+                                               uint64_t r) {
+  uint32_t lo = k0, hi = k1;   // last k in [k0, k1] with rstart[k] <= r
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (rstart[mid] <= r) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // (segment, key) composite sort keys: the segment sits above the key's
 // key_bits bits, so one sort orders rows by segment and, within it, by key.
 __global__ void __launch_bounds__(kBlock) composite_keys_kernel(const uint32_t* const* __restrict__ col0,
                                                                 const uint64_t* __restrict__ rstart, uint32_t S,
                                                                 uint32_t key_bits, uint64_t* __restrict__ keys) {
+  __shared__ uint32_t s_k[2];
   const uint64_t total = rstart[S];
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
-  for (uint64_t r = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; r < total; r += stride) {
-    const uint32_t s = seg_of(rstart, S, r);
-    keys[r] = (static_cast<uint64_t>(s) << key_bits) | col0[s][r - rstart[s]];
+  for (uint64_t b = static_cast<uint64_t>(blockIdx.x) * kBlock; b < total; b += stride) {
+    const uint64_t e = (b + kBlock < total) ? b + kBlock : total;
+    if (threadIdx.x == 0) s_k[0] = seg_of(rstart, S, b);
+    if (threadIdx.x == 32) s_k[1] = seg_of(rstart, S, e - 1);
+    __syncthreads();
+    const uint32_t k0 = s_k[0], k1 = s_k[1];
+    __syncthreads();
+    const uint64_t r = b + threadIdx.x;
+    if (r < e) {
+      const uint32_t s = seg_of_row(rstart, k0, k1, r);
+      keys[r] = (static_cast<uint64_t>(s) << key_bits) | col0[s][r - rstart[s]];
+    }
   }
 }
 
 __global__ void __launch_bounds__(kBlock) seg_gather_kernel(const SegRows* __restrict__ segs,
                                                             const uint64_t* __restrict__ rstart, uint32_t S,
                                                             const uint32_t* __restrict__ perm) {
+  __shared__ uint32_t s_k[2];
   const uint64_t total = rstart[S];
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
-  for (uint64_t r = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; r < total; r += stride) {
-    const uint32_t s = seg_of(rstart, S, r);
-    const uint64_t base = rstart[s];
-    const uint64_t src = perm[r] - base;
-    const uint64_t dst = r - base;
-    const SegRows& g = segs[s];
-    for (uint32_t c = 0; c < g.ncols; ++c) g.out[c][dst] = g.in[c][src];
+  for (uint64_t b = static_cast<uint64_t>(blockIdx.x) * kBlock; b < total; b += stride) {
+    const uint64_t e = (b + kBlock < total) ? b + kBlock : total;
+    if (threadIdx.x == 0) s_k[0] = seg_of(rstart, S, b);
+    if (threadIdx.x == 32) s_k[1] = seg_of(rstart, S, e - 1);
+    __syncthreads();
+    const uint32_t k0 = s_k[0], k1 = s_k[1];
+    __syncthreads();
+    const uint64_t r = b + threadIdx.x;
+    if (r < e) {
+      const uint32_t s = seg_of_row(rstart, k0, k1, r);
+      const uint64_t base = rstart[s];
+      const uint64_t src = perm[r] - base;
+      const uint64_t dst = r - base;
+      const SegRows& g = segs[s];
+      for (uint32_t c = 0; c < g.ncols; ++c) g.out[c][dst] = g.in[c][src];
+    }
   }
 }
 
@@ -557,31 +635,43 @@ void batched_unique_enqueue(Ctx& ctx, const std::vector<SegRows>& segs, uint64_t
   const uint32_t S = static_cast<uint32_t>(segs.size());
   if (S == 0) return;
   std::vector<uint64_t> tstart(S + 1, 0);
+  std::vector<uint32_t> small;
   double bytes = 0;
   for (uint32_t s = 0; s < S; ++s) {
-    tstart[s + 1] = tstart[s] + div_up(segs[s].n, kTileRows);
+    const bool is_small = segs[s].n > 0 && segs[s].n <= kSmallSeg;
+    if (is_small) small.push_back(s);
+    tstart[s + 1] = tstart[s] + (is_small ? 0 : div_up(segs[s].n, kTileRows));
     bytes += 4.0 * segs[s].n * segs[s].ncols;
   }
   const uint64_t tiles = tstart[S];
-  if (tiles == 0) {
+  const uint32_t nsmall = static_cast<uint32_t>(small.size());
+  const uint32_t small_blocks = static_cast<uint32_t>(div_up(nsmall, kBlock / 32));
+  if (tiles == 0 && nsmall == 0) {
     for (uint32_t s = 0; s < S; ++s) counts_host[s] = 0;
     return;
   }
+  std::vector<uint32_t> tile_seg(tiles);
+  for (uint32_t s = 0; s < S; ++s)
+    for (uint64_t t = tstart[s]; t < tstart[s + 1]; ++t) tile_seg[t] = s;
   SegRows* ds = upload(ctx, segs);
   uint64_t* dt = upload(ctx, tstart);
+  uint32_t* dts = upload(ctx, tile_seg);
+  uint32_t* dsm = upload(ctx, small);
   Scratch<uint64_t> status(ctx, tiles), dcount(ctx, S);
   Scratch<uint32_t> ticket(ctx, 1);
   VG_CUDA(cudaMemsetAsync(status.get(), 0, tiles * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(dcount.get(), 0, S * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(uint32_t), ctx.stream));
   ctx.launch("unique_compact", bytes, [&] {
-    bunique_kernel<<<static_cast<unsigned>(tiles), kBlock, 0, ctx.stream>>>(ds, dt, S, status.get(), ticket.get(),
-                                                                           dcount.get(), ctx.d_err);
+    bunique_kernel<<<static_cast<unsigned>(small_blocks + tiles), kBlock, 0, ctx.stream>>>(
+        ds, dt, dts, dsm, nsmall, small_blocks, status.get(), ticket.get(), dcount.get(), ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaMemcpyAsync(counts_host, dcount.get(), S * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.free(ds);
   ctx.free(dt);
+  ctx.free(dts);
+  ctx.free(dsm);
 }
 
 void note_unique_writes(Ctx& ctx, const std::vector<SegRows>& segs, const uint64_t* counts) {
