@@ -515,7 +515,7 @@ void WaveEngine::finish_wave() {
 }
 
 void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
-  Trace tr{'A', 0, 0, 0, 0, 0, 0, 0, 0};
+  Trace tr{'A', 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (tracing) tr.t0 = since(trace_origin);
   if (b_pending_) {
     auto t0 = Clock::now();
@@ -524,7 +524,11 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     prof.device_s += since(t0);
   }
   if (tracing) tr.t_wait = since(trace_origin);
-  if (!run_.empty()) finish_wave();
+  {
+    auto tf = Clock::now();
+    if (!run_.empty()) finish_wave();
+    tr.h_finish = since(tf);
+  }
 
   // queries with a next job run it; the others finish (or have failed)
   std::vector<PlannedQuery*> done;
@@ -563,6 +567,7 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     });
   }
   prof.prepare_s += since(t0);
+  tr.h_prepare = since(t0);
 
   // projection of the queries that finished; failed ones go back at once
   t0 = Clock::now();
@@ -597,6 +602,7 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     }
   }
   prof.final_s += since(t0);
+  tr.h_final = since(t0);
 
   // device half 1
   t0 = Clock::now();
@@ -645,18 +651,23 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
   const size_t c0a_words = placed_wave_ ? (static_cast<size_t>(nslots) * kSmallC0Words + 1) / 2 : 0;
   uint64_t* ha = h_a_.reserve(off_c0a_ + c0a_words + 1);
   bool any = false;
+  auto tp = Clock::now();
   if (!to_sort.empty()) {
     batched_sort_by_first(ctx_, to_sort, key_bits_);
     any = true;
   }
+  tr.h_sort = since(tp);
   if (!swap_rels.empty()) {
     batched_col0_enqueue(ctx_, swap_rels, reinterpret_cast<uint32_t*>(ha + off_c0_));
     any = true;
   }
+  tp = Clock::now();
   if (!pieces.empty()) {
     batched_copy(ctx_, pieces);
     any = true;
   }
+  tr.h_copy = since(tp);
+  tp = Clock::now();
   if (!jl.empty()) {
     batched_join_count(ctx_, jl, jr, jb_, ha + off_tot_);
     // the device error record comes back with the totals: a look-back that
@@ -669,10 +680,13 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
                                ha + off_bump_);
     any = true;
   }
+  tr.h_join = since(tp);
+  tp = Clock::now();
   if (!fin_seg_.empty()) {
     batched_unique_enqueue(ctx_, fin_seg_, ha + off_fin_);
     any = true;
   }
+  tr.h_unique = since(tp);
   if (any) {
     VG_CUDA(cudaEventRecord(ev_a_, ctx_.stream));
     a_pending_ = true;
@@ -690,7 +704,7 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
 
 void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   if (!a_pending_) return;
-  Trace tr{'B', 0, 0, 0, 0, 0, 0, 0, 0};
+  Trace tr{'B', 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (tracing) tr.t0 = since(trace_origin);
   auto t0 = Clock::now();
   wait_event(ev_a_);
@@ -983,14 +997,16 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
   }
   out.prof.plan_s = plan_s;
   if (trace_path) {
-    // one line per stage: engine stage t0 t_wait t_end items joins sorted_rels join_left_rows join_out_rows
+    // one line per stage: engine stage t0 t_wait t_end items joins sorted_rels join_left_rows
+    // join_out_rows, then host seconds: finish prepare final sort copy join unique
     if (FILE* f = std::fopen(trace_path, "a")) {
       std::fprintf(f, "# batch of %zu queries, planned in %.6f s\n", n, plan_s);
       for (size_t e = 0; e < eng.size(); ++e)
         for (const auto& t : eng[e]->trace)
-          std::fprintf(f, "%zu %c %.6f %.6f %.6f %u %u %u %llu %llu\n", e, t.stage, t.t0, t.t_wait, t.t_end, t.items,
-                       t.joins, t.sorted_rels, static_cast<unsigned long long>(t.join_left_rows),
-                       static_cast<unsigned long long>(t.join_out_rows));
+          std::fprintf(f, "%zu %c %.6f %.6f %.6f %u %u %u %llu %llu %.6f %.6f %.6f %.6f %.6f %.6f %.6f\n", e, t.stage,
+                       t.t0, t.t_wait, t.t_end, t.items, t.joins, t.sorted_rels,
+                       static_cast<unsigned long long>(t.join_left_rows), static_cast<unsigned long long>(t.join_out_rows),
+                       t.h_finish, t.h_prepare, t.h_final, t.h_sort, t.h_copy, t.h_join, t.h_unique);
       std::fclose(f);
     }
   }

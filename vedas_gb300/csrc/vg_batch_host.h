@@ -141,6 +141,10 @@ class WaveEngine {
     double t0, t_wait, t_end;
     uint32_t items, joins, sorted_rels;
     uint64_t join_left_rows, join_out_rows;
+    // host seconds of the stage's parts (stage A): finishing the previous
+    // wave, preparing the next jobs, projections, and enqueueing the sorts,
+    // the select copies, the joins and the final compaction
+    double h_finish, h_prepare, h_final, h_sort, h_copy, h_join, h_unique;
   };
   bool tracing = false;
   std::chrono::steady_clock::time_point trace_origin;
