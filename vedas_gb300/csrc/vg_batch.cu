@@ -101,6 +101,32 @@ __global__ void __launch_bounds__(kBlock) bcopy_kernel(const CopyPiece* __restri
 }
 
 // ---------------------------------------------------------------------------
+// Flags (bit i) of the rows r0 + i (i < kRows, r0 a multiple of kRows) that
+// differ from the previous row in column `col` (n rows; row 0 is left to the
+// caller).  A 16-byte aligned column is read with two 16-byte loads.
+__device__ __forceinline__ uint32_t diff_bits(const uint32_t* __restrict__ col, uint64_t n, uint64_t r0) {
+  static_assert(kRows == 8, "two 16-byte loads cover a thread's rows");
+  uint32_t v[kRows];
+  if ((reinterpret_cast<uintptr_t>(col) & 15u) == 0 && r0 + kRows <= n) {
+    const uint4 a = *reinterpret_cast<const uint4*>(col + r0);
+    const uint4 b = *reinterpret_cast<const uint4*>(col + r0 + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) v[i] = (r0 + i < n) ? col[r0 + i] : 0u;
+  }
+  uint32_t prev = (r0 > 0 && r0 - 1 < n) ? col[r0 - 1] : 0u;
+  uint32_t d = 0;
+#pragma unroll
+  for (int i = 0; i < kRows; ++i) {
+    const uint64_t r = r0 + i;
+    if (r < n && r > 0 && v[i] != prev) d |= 1u << i;
+    prev = v[i];
+  }
+  return d;
+}
+
 // Adjacent-unique compaction of every segment.  Segments of at most
 // kSmallSeg rows (most final results) take one warp each in the first
 // small_blocks blocks: each lane flags its kRows consecutive rows, a warp
@@ -113,17 +139,7 @@ __device__ __forceinline__ void unique_small_segment(const SegRows& g, uint64_t*
   const uint32_t lane = lane_id();
   const uint64_t n = g.n, r0 = static_cast<uint64_t>(lane) * kRows;
   uint32_t diff = (r0 == 0 && n > 0) ? 1u : 0u;
-  for (uint32_t c = 0; c < g.ncols; ++c) {
-    const uint32_t* col = g.in[c];
-    uint32_t prev = (r0 > 0 && r0 - 1 < n) ? col[r0 - 1] : 0u;
-#pragma unroll
-    for (int i = 0; i < kRows; ++i) {
-      const uint64_t r = r0 + i;
-      const uint32_t v = (r < n) ? col[r] : 0u;
-      if (r < n && r > 0 && v != prev) diff |= 1u << i;
-      prev = v;
-    }
-  }
+  for (uint32_t c = 0; c < g.ncols; ++c) diff |= diff_bits(g.in[c], n, r0);
   if (r0 >= n) diff = 0;
   else if (n - r0 < kRows) diff &= (1u << (n - r0)) - 1u;
   const uint32_t cnt = __popc(diff);
@@ -165,17 +181,7 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
   const uint32_t ncols = s_seg.ncols;
   const uint64_t r0 = (tile - tstart[s]) * kTileRows + threadIdx.x * kRows;
   uint32_t diff = (r0 == 0) ? 1u : 0u;
-  for (uint32_t c = 0; c < ncols; ++c) {
-    const uint32_t* col = s_seg.in[c];
-    uint32_t prev = (r0 > 0 && r0 - 1 < n) ? col[r0 - 1] : 0u;
-#pragma unroll
-    for (int i = 0; i < kRows; ++i) {
-      const uint64_t r = r0 + i;
-      const uint32_t v = (r < n) ? col[r] : 0u;
-      if (r < n && r > 0 && v != prev) diff |= 1u << i;
-      prev = v;
-    }
-  }
+  for (uint32_t c = 0; c < ncols; ++c) diff |= diff_bits(s_seg.in[c], n, r0);
   if (r0 >= n) diff = 0;
   else if (n - r0 < kRows) diff &= (1u << (n - r0)) - 1u;
   uint32_t tot;
@@ -389,8 +395,17 @@ struct JoinOut {
 // tiles.
 constexpr uint32_t kSmallOut = 1024;
 
-__device__ __forceinline__ void write_small_join(const JoinOut* __restrict__ jp, uint64_t* s_off, uint32_t* s_lo) {
+__device__ __forceinline__ void write_small_join(const JoinOut* __restrict__ src, JoinOut* jp, uint64_t* s_off,
+                                                 uint32_t* s_lo) {
   const uint32_t lane = lane_id();
+  // the join's description in the warp's shared slot: the row loop reads its
+  // column pointers from shared memory
+  {
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* b = reinterpret_cast<uint32_t*>(jp);
+    for (uint32_t w = lane; w < sizeof(JoinOut) / 4; w += 32) b[w] = a[w];
+    __syncwarp();
+  }
   const uint64_t total = jp->total, nl = jp->nl;
   const uint64_t* offs = jp->offs;
   const uint32_t* lov = jp->lo;
@@ -424,6 +439,7 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
   constexpr int kStage = kTileRows + 1;
   static_assert(kStage >= (kBlock / 32) * kSmallJoin, "a warp's slice holds a small join's left rows");
   __shared__ JoinOut s_o;
+  __shared__ JoinOut s_w[kBlock / 32];
   __shared__ uint64_t s_off[kStage];
   __shared__ uint32_t s_lo[kStage];
   __shared__ uint64_t s_i[2];
@@ -432,7 +448,7 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
     const uint32_t warp = threadIdx.x >> 5, nwarps = kBlock / 32;
     for (uint64_t w = static_cast<uint64_t>(blockIdx.x) * nwarps + warp; w < nsm;
          w += static_cast<uint64_t>(gridDim.x) * nwarps)
-      write_small_join(&jo[small[w]], s_off + warp * kSmallJoin, s_lo + warp * kSmallJoin);
+      write_small_join(&jo[small[w]], &s_w[warp], s_off + warp * kSmallJoin, s_lo + warp * kSmallJoin);
   }
   const uint64_t T = ostart_end ? *ostart_end : T_host;
 #pragma unroll 1
@@ -464,6 +480,28 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
         s_lo[e] = s_o.lo[ib + e];
       }
     __syncthreads();
+    // unstaged (a sparse tile: more than kStage left rows, most without
+    // matches): the left rows of the thread's kRows output rows come from
+    // kRows binary searches of the offsets advanced in lockstep, so each
+    // round has kRows independent loads in flight
+    uint64_t li[kRows];
+    if (!staged) {
+      uint64_t k8[kRows];
+#pragma unroll
+      for (int it = 0; it < kRows; ++it) {
+        const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
+        k8[it] = k < kend ? k : kend - 1;
+        li[it] = ib;
+      }
+      uint64_t n = ie - ib;                     // last i in [ib, ie) with offs[i] <= k
+      while (n > 1) {
+        const uint64_t half = n >> 1;
+#pragma unroll
+        for (int it = 0; it < kRows; ++it)
+          li[it] = (s_o.offs[li[it] + half] <= k8[it]) ? li[it] + half : li[it];
+        n -= half;
+      }
+    }
     uint32_t p = 0;   // staged: the current left row, relative to ib
     for (int it = 0; it < kRows; ++it) {
       const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
@@ -483,7 +521,7 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
         i = ib + p;
         jj = s_lo[p] + (k - s_off[p]);
       } else {
-        i = upper_bound_dev(s_o.offs, ib, ie, k) - 1;
+        i = li[it];
         jj = s_o.lo[i] + (k - s_o.offs[i]);
       }
       uint32_t c = 0;

@@ -65,7 +65,7 @@ __global__ void iota_kernel(uint32_t* out, uint64_t n) {
 }
 
 template <typename K, bool HAS_V, bool IOTA>
-__global__ void __launch_bounds__(kBlock) onesweep_kernel(
+__global__ void __launch_bounds__(kBlock, 3) onesweep_kernel(
     const K* __restrict__ kin, K* __restrict__ kout, const uint32_t* __restrict__ vin,
     uint32_t* __restrict__ vout, uint64_t n, uint32_t shift, const uint64_t* __restrict__ bucket_base,
     uint64_t* status, uint32_t* ticket, DeviceErrors* err) {
@@ -172,6 +172,10 @@ void launch_pass(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uint32_t*
   static const bool attr_set = [smem] {
     VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
+    // all of the unified L1/shared storage as shared memory: three or four
+    // blocks of a tile's keys (and values) per SM
+    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared));
     return true;
   }();
   (void)attr_set;
