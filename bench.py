@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ingest-triples", type=int, default=20_000_000,
                     help="triples of the N-Triples ingest measurement (0: skip)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default launch parameters (no autotuner trials)")
     ap.add_argument("--arena-gb", type=float, default=0.0,
                     help="HBM arena size (0: 90%% of free memory; profilers need room to replay)")
     a = ap.parse_args()
@@ -401,6 +403,11 @@ def bench_ours(args, rank, world, local, pg):
     run = run_batch if args.mode == "batch" else run_plain
     # the batch API takes UTF-8 query text; encode it once, as a client would
     batch_in = [q.encode() for q in kept] if args.mode == "batch" else kept
+    tuned = None
+    if not args.no_tune:
+        from vedas_gb300 import tune
+        tuned = tune.tune_batch(ix, [q.encode() for q in kept], reps=3, triples=g.n)
+        note(f"launch parameters: {tuned['params']} ({'cached' if tuned['from_cache'] else 'tuned'})")
     stream = torch.cuda.ExternalStream(ctx.stream, device=local)
 
     for _ in range(args.warmup):
@@ -492,6 +499,7 @@ def bench_ours(args, rank, world, local, pg):
             "batch_latency_ms": {"p50": step_ms_max, "p99": step_ms_max,
                                  "note": "every query of a batch completes with the batch"},
             "host_device_split_s_per_step": {k: round(v / args.steps, 4) for k, v in prof.items()},
+            "launch_parameters": tuned,
             "index_build": build,
             "chain_query": chain,
             "ingest": ingest,

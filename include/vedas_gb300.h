@@ -65,6 +65,24 @@ uint64_t vg_stats_launches(vg_ctx* ctx);
 vg_status vg_stats_get(vg_ctx* ctx, uint32_t i, const char** name, uint64_t* launches, double* bytes,
                        double* ms);
 
+/* Launch parameters of the context's kernels (no reference counterpart: the
+ * reference's tile and block sizes are ModernGPU's and Thrust's built-in
+ * ones).  Choices change speed only, never results:
+ *   sort_items           radix-sort keys per thread, 8 or 16 (tile 2048 / 4096)
+ *   join_small_rows      joins with at most this many left rows are counted
+ *                        one per warp (0..256)
+ *   write_small_rows     join outputs with at most this many rows (of joins
+ *                        with at most 256 left rows) are written one per warp
+ *                        (0..4096)
+ *   unique_small_rows    final compactions of at most this many rows run one
+ *                        per warp (0..256)
+ *   write_blocks_per_sm  blocks per SM of a batched join write whose size is
+ *                        only known on the device (1..8)
+ * vedas_gb300.tune picks them from timed trials per GPU and workload shape.
+ * VG_ERR_INVALID for an unknown name or a value out of range. */
+vg_status vg_tune_set(vg_ctx* ctx, const char* name, int64_t value);
+vg_status vg_tune_get(vg_ctx* ctx, const char* name, int64_t* value);
+
 /* ---- index build (hot path a) ----------------------------------------- */
 typedef struct vg_index vg_index;
 

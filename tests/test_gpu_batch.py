@@ -135,3 +135,41 @@ def test_batch_join_placement_regions(ctx, monkeypatch, region_mb):
         b.close()
     assert ctx.memory()[0] == used0         # every region went back with its last output
     ix.close()
+
+
+@pytest.mark.parametrize("params", [
+    {"sort_items": 8, "join_small_rows": 0, "write_small_rows": 0, "unique_small_rows": 0, "write_blocks_per_sm": 1},
+    {"sort_items": 16, "join_small_rows": 64, "write_small_rows": 4096, "unique_small_rows": 256,
+     "write_blocks_per_sm": 2},
+])
+def test_launch_parameters_change_speed_only(ctx, params):
+    """Every autotuner choice (sort tile, warp-per-join thresholds, write
+    grid) gives the oracle's results, logs included."""
+    import vedas_gb300 as vg
+    from vedas_gb300 import tune
+    g = workloads.graph_chain(n=300_000, n_entities=30_000, seed=31)
+    qs = workloads.query_mix(g, 300, seed=32)
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    ref = oracle_py.OracleIndex(g.s, g.p, g.o)
+    old = {k: ctx.tune_get(k) for k in params}
+    tune.apply(ctx, params)
+    try:
+        b = vg.Batch(ix, qs)
+        for i, q in enumerate(qs):
+            r = ref.query(q)
+            if r.status != 0:
+                assert b.status(i) != 0
+                continue
+            assert b.status(i) == 0, b.error(i)
+            for a, c in zip(b.columns(i), r.columns):
+                np.testing.assert_array_equal(a, c)
+            assert [x[:4] for x in b.log(i)] == [x[:4] for x in r.log]
+        b.close()
+        # the index build's sort with the same tile choice
+        ix2 = vg.Index(ctx, g.s, g.p, g.o)
+        for name in ("ps_data", "pso_data", "po_data", "pos_data", "ps_idx_offsets", "po_idx_offsets"):
+            np.testing.assert_array_equal(ix2.array(name), ref.array(name), err_msg=name)
+        ix2.close()
+    finally:
+        tune.apply(ctx, old)
+    ix.close()

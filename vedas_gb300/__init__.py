@@ -91,6 +91,8 @@ def lib():
             "vg_result_log": (None, [vp, u32, pu32, ctypes.POINTER(u64), ctypes.POINTER(u64),
                                      ctypes.POINTER(u64)]),
             "vg_result_free": (i32, [vp]),
+            "vg_tune_set": (i32, [vp, ctypes.c_char_p, ctypes.c_int64]),
+            "vg_tune_get": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]),
             "vg_query_loop": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(u64), ctypes.POINTER(i32)]),
             "vg_batch_run": (i32, [vp, vp, ctypes.POINTER(ctypes.c_char_p), u32, ctypes.POINTER(vp)]),
@@ -181,6 +183,15 @@ class Context:
 
     def __exit__(self, *a):
         self.close()
+
+    def tune_set(self, name: str, value: int) -> None:
+        """Sets one launch parameter (vg_tune_set)."""
+        check(lib().vg_tune_set(self.h, name.encode(), int(value)))
+
+    def tune_get(self, name: str) -> int:
+        v = ctypes.c_int64()
+        check(lib().vg_tune_get(self.h, name.encode(), ctypes.byref(v)))
+        return int(v.value)
 
     def memory(self):
         u, p, c = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()

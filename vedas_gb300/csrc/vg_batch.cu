@@ -387,13 +387,13 @@ struct JoinOut {
 // threads on consecutive rows, so loads and stores coalesce) from the
 // previous one's left row.  Hub keys thus spread over many blocks.
 //
-// Small outputs (at most kSmallOut rows of a join with at most kSmallJoin
+// Small outputs (at most Ctx::tune.write_small_rows rows of a join with at most kSmallJoin
 // left rows; most outputs of a wave) are written one join per warp first,
 // before the tiles: the warp stages the join's offsets and lower bounds in
 // its own slice of the shared arrays and each lane writes every 32nd row.
 // Their list (small, nsmall of them; nsmall_dev when on the device) holds no
 // tiles.
-constexpr uint32_t kSmallOut = 1024;
+constexpr uint32_t kSmallOutMax = 4096;   // largest write_small_rows a context may choose
 
 __device__ __forceinline__ void write_small_join(const JoinOut* __restrict__ src, JoinOut* jp, uint64_t* s_off,
                                                  uint32_t* s_lo) {
@@ -551,6 +551,7 @@ struct JoinPlace {
   uint64_t* ostart;      // J + 1 output-tile starts (written; small outputs have no tiles)
   uint32_t* small;       // joins whose outputs are written one per warp (written)
   uint32_t* nsmall;      // their number (written)
+  uint32_t small_rows;   // outputs of at most this many rows are small
 };
 
 __global__ void __launch_bounds__(kPlaceBlock) join_place_kernel(JoinOut* __restrict__ jo,
@@ -569,7 +570,7 @@ __global__ void __launch_bounds__(kPlaceBlock) join_place_kernel(JoinOut* __rest
     const uint64_t eb = block_excl_scan64<kPlaceBlock>(bytes, tot_b, s_scan);
     const uint64_t off = bump0 + carry_b + eb;
     const bool fits = off + bytes <= pl.cap;
-    const bool is_small = fits && t > 0 && t <= kSmallOut && j < J && jo[j].nl <= kSmallJoin;
+    const bool is_small = fits && t > 0 && t <= pl.small_rows && j < J && jo[j].nl <= kSmallJoin;
     const uint64_t tiles = (fits && t && !is_small) ? div_up(t, kTileRows) : 0;
     const uint64_t et = block_excl_scan64<kPlaceBlock>(tiles, tot_t, s_scan);
     (void)block_excl_scan64<kPlaceBlock>(fits ? bytes : 0, fb_sum, s_scan);
@@ -676,7 +677,7 @@ void batched_unique_enqueue(Ctx& ctx, const std::vector<SegRows>& segs, uint64_t
   std::vector<uint32_t> small;
   double bytes = 0;
   for (uint32_t s = 0; s < S; ++s) {
-    const bool is_small = segs[s].n > 0 && segs[s].n <= kSmallSeg;
+    const bool is_small = segs[s].n > 0 && segs[s].n <= std::min<uint32_t>(kSmallSeg, ctx.tune.unique_small_rows);
     if (is_small) small.push_back(s);
     tstart[s + 1] = tstart[s] + (is_small ? 0 : div_up(segs[s].n, kTileRows));
     bytes += 4.0 * segs[s].n * segs[s].ncols;
@@ -812,7 +813,7 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
     js[j] = {l[j]->cols[0], r[j]->cols[0], l[j]->nrows, r[j]->nrows, rows};
     jb.row0[j] = rows;
     rows += l[j]->nrows;
-    const bool is_small = l[j]->nrows <= kSmallJoin;
+    const bool is_small = l[j]->nrows <= std::min<uint32_t>(kSmallJoin, ctx.tune.join_small_rows);
     if (is_small) small.push_back(j);
     bstart[j + 1] = bstart[j] + (is_small ? 0 : div_up(l[j]->nrows, kJcTile));
     cbytes += 4.0 * (l[j]->nrows + r[j]->nrows);
@@ -863,7 +864,7 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
   std::vector<uint32_t> small;   // outputs written one join per warp
   for (uint32_t j = 0; j < J; ++j) {
     if (rows(j) > 0xFFFFFFFFull) fail(VG_ERR_OVERFLOW, "join output exceeds 2^32 rows");
-    const bool is_small = rows(j) > 0 && rows(j) <= kSmallOut && jb.l[j]->nrows <= kSmallJoin;
+    const bool is_small = rows(j) > 0 && rows(j) <= ctx.tune.write_small_rows && jb.l[j]->nrows <= kSmallJoin;
     if (is_small) small.push_back(j);
     ostart[j + 1] = ostart[j] + (is_small ? 0 : div_up(rows(j), kTileRows));
     wbytes += 4.0 * rows(j) * (2.0 * (jb.l[j]->ncols + jb.r[j]->ncols - 1) - 1);
@@ -976,7 +977,7 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
   uint32_t* dfl = ctx.alloc<uint32_t>(2 * J);
   uint32_t* dstage = ctx.alloc<uint32_t>(static_cast<uint64_t>(nslots ? nslots : 1) * kSmallC0Words);
   VG_CUDA(cudaMemsetAsync(dfl, 0, 2 * J * sizeof(uint32_t), ctx.stream));
-  JoinPlace pl{region->begin, region->bytes, d_bump, dos, dsm, dsm + J};
+  JoinPlace pl{region->begin, region->bytes, d_bump, dos, dsm, dsm + J, ctx.tune.write_small_rows};
   ctx.launch("join_place", 16.0 * J, [&] {
     join_place_kernel<<<1, kPlaceBlock, 0, ctx.stream>>>(djo, jb.d_totals, J, pl);
   });
@@ -987,8 +988,8 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
   // the tile count is on the device: a fixed grid loops over the tiles (the
   // algorithmic bytes are added when the host reads the totals)
   ctx.launch("join_write", 0.0, [&] {
-    bjoin_write_kernel<<<static_cast<unsigned>(ctx.num_sms) * 8, kBlock, 0, ctx.stream>>>(djo, dos, dtj, 0,
-                                                                                           dos + J, dsm, 0, dsm + J);
+    bjoin_write_kernel<<<static_cast<unsigned>(ctx.num_sms) * ctx.tune.write_blocks_per_sm, kBlock, 0,
+                         ctx.stream>>>(djo, dos, dtj, 0, dos + J, dsm, 0, dsm + J);
   });
   VG_CUDA(cudaGetLastError());
   ctx.launch("join_first_last", 8.0 * J, [&] {

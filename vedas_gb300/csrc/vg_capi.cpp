@@ -427,6 +427,43 @@ vg_status vg_result_free(vg_result* r) {
   return VG_OK;
 }
 
+namespace {
+// name -> (field, smallest value, largest value, value list: 0 for a range)
+struct TuneKnob {
+  const char* name;
+  uint32_t vg::TuneParams::*field;
+  uint32_t lo, hi;
+};
+const TuneKnob kKnobs[] = {
+    {"sort_items", &vg::TuneParams::sort_items, 8, 16},
+    {"join_small_rows", &vg::TuneParams::join_small_rows, 0, 256},
+    {"write_small_rows", &vg::TuneParams::write_small_rows, 0, 4096},
+    {"unique_small_rows", &vg::TuneParams::unique_small_rows, 0, 256},
+    {"write_blocks_per_sm", &vg::TuneParams::write_blocks_per_sm, 1, 8},
+};
+const TuneKnob* find_knob(const char* name) {
+  if (!name) return nullptr;
+  for (const TuneKnob& k : kKnobs)
+    if (std::strcmp(k.name, name) == 0) return &k;
+  return nullptr;
+}
+}  // namespace
+
+vg_status vg_tune_set(vg_ctx* ctx, const char* name, int64_t value) {
+  const TuneKnob* k = find_knob(name);
+  if (!ctx || !k || value < static_cast<int64_t>(k->lo) || value > static_cast<int64_t>(k->hi)) return VG_ERR_INVALID;
+  if (k->field == &vg::TuneParams::sort_items && value != 8 && value != 16) return VG_ERR_INVALID;
+  ctx->c.tune.*(k->field) = static_cast<uint32_t>(value);
+  return VG_OK;
+}
+
+vg_status vg_tune_get(vg_ctx* ctx, const char* name, int64_t* value) {
+  const TuneKnob* k = find_knob(name);
+  if (!ctx || !k || !value) return VG_ERR_INVALID;
+  *value = ctx->c.tune.*(k->field);
+  return VG_OK;
+}
+
 vg_status vg_query_loop(vg_ctx* ctx, vg_index* ix, const char* const* queries, uint32_t nq, double* seconds,
                         uint64_t* rows, vg_status* status) {
   if (!ctx || !ix || (nq && !queries)) return VG_ERR_INVALID;

@@ -143,8 +143,19 @@ struct KernelStat {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
 };
 
+// Launch parameters chosen per context (vg_tune_set; the autotuner picks
+// them from timed trials).  Each choice changes only speed, never results.
+struct TuneParams {
+  uint32_t sort_items = 16;          // onesweep keys per thread: 8 or 16
+  uint32_t join_small_rows = 256;    // joins with at most this many left rows: one warp each (0..256)
+  uint32_t write_small_rows = 1024;  // outputs with at most this many rows: one warp each (0..4096)
+  uint32_t unique_small_rows = 256;  // final compactions with at most this many rows: one warp each (0..256)
+  uint32_t write_blocks_per_sm = 8;  // blocks per SM of a join write whose size is on the device (1..8)
+};
+
 struct Ctx {
   int device = 0;
+  TuneParams tune;
   cudaStream_t stream = nullptr;
   Arena arena;
   DeviceErrors* d_err = nullptr;   // device error record

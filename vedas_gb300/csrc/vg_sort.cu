@@ -1,7 +1,7 @@
 // Stable LSD radix sort, onesweep style (one upfront histogram pass, then one
 // pass per 8-bit digit whose tile offsets come from a decoupled look-back).
 //
-// A tile is 256 threads x 16 keys.  Keys are ranked inside each warp with
+// A tile is 256 threads x 16 keys (or 8, a per-context tuning choice).  Keys are ranked inside each warp with
 // __match_any_sync in input order, so equal digits keep their order and the
 // sort is stable; tiles take their index from an atomic ticket in launch
 // order, which guarantees that every look-back predecessor is running.
@@ -19,8 +19,9 @@ namespace vg {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kItems = 16;
-constexpr int kTile = kBlock * kItems;
+// Keys per thread of a onesweep tile: 16 (tiles of 4096 keys) or 8 (2048),
+// chosen per context (Ctx::tune.sort_items).
+constexpr int kItemsMax = 16;
 constexpr int kRadix = 256;
 constexpr int kMaxPasses = 8;
 
@@ -64,11 +65,12 @@ __global__ void iota_kernel(uint32_t* out, uint64_t n) {
     out[i] = static_cast<uint32_t>(i);
 }
 
-template <typename K, bool HAS_V, bool IOTA>
-__global__ void __launch_bounds__(kBlock, 3) onesweep_kernel(
+template <typename K, bool HAS_V, bool IOTA, int kItems>
+__global__ void __launch_bounds__(kBlock, kItems <= 8 ? 4 : 3) onesweep_kernel(
     const K* __restrict__ kin, K* __restrict__ kout, const uint32_t* __restrict__ vin,
     uint32_t* __restrict__ vout, uint64_t n, uint32_t shift, const uint64_t* __restrict__ bucket_base,
     uint64_t* status, uint32_t* ticket, DeviceErrors* err) {
+  constexpr int kTile = kBlock * kItems;
   extern __shared__ __align__(16) unsigned char smem[];
   K* s_keys = reinterpret_cast<K*>(smem);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + kTile * sizeof(K));
@@ -164,28 +166,38 @@ __global__ void __launch_bounds__(kBlock, 3) onesweep_kernel(
   }
 }
 
-template <typename K, bool HAS_V, bool IOTA>
-void launch_pass(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint64_t n,
-                 uint32_t shift, const uint64_t* bases, uint64_t* status, uint32_t* ticket) {
+template <typename K, bool HAS_V, bool IOTA, int kItems>
+void launch_pass_items(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint64_t n,
+                       uint32_t shift, const uint64_t* bases, uint64_t* status, uint32_t* ticket) {
+  constexpr int kTile = kBlock * kItems;
   const size_t smem = kTile * sizeof(K) + (HAS_V ? kTile * sizeof(uint32_t) : 0);
   // once per instantiation (thread-safe static initialisation)
   static const bool attr_set = [smem] {
-    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem)));
-    // all of the unified L1/shared storage as shared memory: three or four
+    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA, kItems>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    // all of the unified L1/shared storage as shared memory: three or more
     // blocks of a tile's keys (and values) per SM
-    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared));
+    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA, kItems>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
     return true;
   }();
   (void)attr_set;
   const uint64_t tiles = div_up(n, kTile);
   const double bytes = static_cast<double>(n) * (2 * sizeof(K) + (HAS_V ? (IOTA ? 4 : 8) : 0));
   ctx.launch("radix_onesweep", bytes, [&] {
-    onesweep_kernel<K, HAS_V, IOTA><<<static_cast<unsigned>(tiles), kBlock, smem, ctx.stream>>>(
+    onesweep_kernel<K, HAS_V, IOTA, kItems><<<static_cast<unsigned>(tiles), kBlock, smem, ctx.stream>>>(
         kin, kout, vin, vout, n, shift, bases, status, ticket, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
+}
+
+template <typename K, bool HAS_V, bool IOTA>
+void launch_pass(Ctx& ctx, int items, const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint64_t n,
+                 uint32_t shift, const uint64_t* bases, uint64_t* status, uint32_t* ticket) {
+  if (items == 8)
+    launch_pass_items<K, HAS_V, IOTA, 8>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
+  else
+    launch_pass_items<K, HAS_V, IOTA, kItemsMax>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
 }
 
 template <typename K>
@@ -244,7 +256,8 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
     VG_CUDA(cudaGetLastError());
     for (int p = 0; p < passes; ++p) todo.push_back(p);
   }
-  const uint64_t tiles = div_up(n, kTile);
+  const int items = ctx.tune.sort_items == 8 ? 8 : kItemsMax;
+  const uint64_t tiles = div_up(n, static_cast<uint64_t>(kBlock) * items);
   Scratch<uint64_t> status(ctx, tiles * kRadix);
   Scratch<uint32_t> ticket(ctx, todo.size());
   VG_CUDA(cudaMemsetAsync(ticket.get(), 0, todo.size() * sizeof(uint32_t), ctx.stream));
@@ -259,13 +272,13 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
     const uint64_t* pb = d_bases.get() + p * kRadix;
     const uint32_t shift = static_cast<uint32_t>(8 * p);
     if (!has_v)
-      launch_pass<K, false, false>(ctx, kin, kout, nullptr, nullptr, n, shift, pb, status.get(),
+      launch_pass<K, false, false>(ctx, items, kin, kout, nullptr, nullptr, n, shift, pb, status.get(),
                                    ticket.get() + t);
     else if (t == 0 && vals_iota)
-      launch_pass<K, true, true>(ctx, kin, kout, nullptr, vout, n, shift, pb, status.get(),
+      launch_pass<K, true, true>(ctx, items, kin, kout, nullptr, vout, n, shift, pb, status.get(),
                                  ticket.get() + t);
     else
-      launch_pass<K, true, false>(ctx, kin, kout, vin, vout, n, shift, pb, status.get(),
+      launch_pass<K, true, false>(ctx, items, kin, kout, vin, vout, n, shift, pb, status.get(),
                                   ticket.get() + t);
     std::swap(kin, kout);
     std::swap(vin, vout);
