@@ -125,6 +125,18 @@ __global__ void __launch_bounds__(kBlock) unpack_rle_kernel(UnpackArgs a) {
   }
 }
 
+// (k0, k1, k2) keys packed at widths (b0, b1, b2) repacked as (k0, k2, k1).
+__global__ void repack_swap12_kernel(const uint64_t* __restrict__ in, uint64_t* __restrict__ out, uint64_t n,
+                                     uint32_t b1, uint32_t b2) {
+  const uint64_t m1 = (1ull << b1) - 1, m2 = (1ull << b2) - 1;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t k = in[i];
+    const uint64_t k2 = k & m2, k1 = (k >> b2) & m1, k0 = k >> (b1 + b2);
+    out[i] = (k0 << (b1 + b2)) | (k2 << b1) | k1;
+  }
+}
+
 int bits_for(uint32_t maxv) { return maxv == 0 ? 1 : 32 - __builtin_clz(maxv); }
 
 unsigned grid_for(const Ctx& ctx, uint64_t n, int per_thread) {
@@ -149,24 +161,13 @@ void column_max3(Ctx& ctx, const uint32_t* a, const uint32_t* b, const uint32_t*
   ctx.sync();
 }
 
-void build_permutation(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const uint32_t* k2,
-                       uint64_t n, const uint32_t maxes[3], PermOutputs& out) {
-  const int b0 = bits_for(maxes[0]), b1 = bits_for(maxes[1]), b2 = bits_for(maxes[2]);
-  if (b0 + b1 + b2 > 64)
-    fail(VG_ERR_UNSUPPORTED, "triple ids need more than 64 key bits for the packed index sort");
-  out.col1.clear();
-  out.col2.clear();
-  if (n == 0) return;
-  const uint32_t sh1 = static_cast<uint32_t>(b2), sh0 = static_cast<uint32_t>(b1 + b2);
-  uint64_t* keys = ctx.alloc<uint64_t>(n);
-  uint64_t* keys_alt = ctx.alloc<uint64_t>(n);
-  ctx.launch("index_pack", 20.0 * n,
-             [&] { pack_kernel<<<grid_for(ctx, n, 8), kBlock, 0, ctx.stream>>>(k0, k1, k2, n, sh0, sh1, keys); });
-  VG_CUDA(cudaGetLastError());
-  const bool alt = radix_sort_u64(ctx, keys, keys_alt, nullptr, nullptr, n, b0 + b1 + b2, false);
-  uint64_t* sorted = alt ? keys_alt : keys;
-  ctx.free(alt ? keys : keys_alt);
+namespace {
 
+// Run-length encodes and unpacks sorted packed keys (widths b0, b1, b2) into
+// the requested outputs.
+void unpack_outputs(Ctx& ctx, const uint64_t* sorted, uint64_t n, int b0, int b1, int b2, PermOutputs& out) {
+  (void)b0;
+  const uint32_t sh1 = static_cast<uint32_t>(b2), sh0 = static_cast<uint32_t>(b1 + b2);
   UnpackArgs a{};
   a.keys = sorted;
   a.n = n;
@@ -200,7 +201,6 @@ void build_permutation(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const u
   VG_CUDA(cudaMemcpyAsync(hc, counts.get(), sizeof(hc), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.sync();
   ctx.check_device_errors();
-  ctx.free(sorted);
   out.col1 = DevArray(a.col1, a.col1 ? n : 0);
   out.col2 = DevArray(a.col2, a.col2 ? n : 0);
   if (a.l1_vals) {
@@ -215,6 +215,65 @@ void build_permutation(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const u
     out.l2_vals = DevArray(a.l2_vals, hc[1]);
     out.l2_offs = DevArray(a.l2_offs, hc[1]);
   }
+}
+
+// Packs (k0, k1, k2) at widths (b0, b1, b2) and sorts the keys; returns the
+// sorted array (the caller frees it).
+uint64_t* sort_packed(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const uint32_t* k2, uint64_t n, int b0,
+                      int b1, int b2) {
+  const uint32_t sh1 = static_cast<uint32_t>(b2), sh0 = static_cast<uint32_t>(b1 + b2);
+  uint64_t* keys = ctx.alloc<uint64_t>(n);
+  uint64_t* keys_alt = ctx.alloc<uint64_t>(n);
+  ctx.launch("index_pack", 20.0 * n,
+             [&] { pack_kernel<<<grid_for(ctx, n, 8), kBlock, 0, ctx.stream>>>(k0, k1, k2, n, sh0, sh1, keys); });
+  VG_CUDA(cudaGetLastError());
+  const bool alt = radix_sort_u64(ctx, keys, keys_alt, nullptr, nullptr, n, b0 + b1 + b2, false);
+  ctx.free(alt ? keys : keys_alt);
+  return alt ? keys_alt : keys;
+}
+
+}  // namespace
+
+void build_permutation(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const uint32_t* k2,
+                       uint64_t n, const uint32_t maxes[3], PermOutputs& out) {
+  const int b0 = bits_for(maxes[0]), b1 = bits_for(maxes[1]), b2 = bits_for(maxes[2]);
+  if (b0 + b1 + b2 > 64)
+    fail(VG_ERR_UNSUPPORTED, "triple ids need more than 64 key bits for the packed index sort");
+  out.col1.clear();
+  out.col2.clear();
+  if (n == 0) return;
+  uint64_t* sorted = sort_packed(ctx, k0, k1, k2, n, b0, b1, b2);
+  unpack_outputs(ctx, sorted, n, b0, b1, b2, out);
+  ctx.free(sorted);
+}
+
+void build_permutation_pair(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const uint32_t* k2, uint64_t n,
+                            const uint32_t maxes[3], PermOutputs& first, PermOutputs& second) {
+  const int b0 = bits_for(maxes[0]), b1 = bits_for(maxes[1]), b2 = bits_for(maxes[2]);
+  if (b0 + b1 + b2 > 64)
+    fail(VG_ERR_UNSUPPORTED, "triple ids need more than 64 key bits for the packed index sort");
+  first.col1.clear();
+  first.col2.clear();
+  second.col1.clear();
+  second.col2.clear();
+  if (n == 0) return;
+  uint64_t* sorted = sort_packed(ctx, k0, k1, k2, n, b0, b1, b2);
+  unpack_outputs(ctx, sorted, n, b0, b1, b2, first);
+  // (k0, k2, k1) order from (k0, k1, k2) order: a stable sort by (k0, k2)
+  // alone keeps equal (k0, k2) keys in (k0, k1, k2) order, i.e. by k1
+  uint64_t* re = ctx.alloc<uint64_t>(n);
+  uint64_t* re_alt = ctx.alloc<uint64_t>(n);
+  ctx.launch("index_repack", 16.0 * n, [&] {
+    repack_swap12_kernel<<<grid_for(ctx, n, 8), kBlock, 0, ctx.stream>>>(sorted, re, n, static_cast<uint32_t>(b1),
+                                                                         static_cast<uint32_t>(b2));
+  });
+  VG_CUDA(cudaGetLastError());
+  ctx.free(sorted);
+  const bool alt = radix_sort_u64_bits(ctx, re, re_alt, n, b1, b0 + b1 + b2);
+  uint64_t* s2 = alt ? re_alt : re;
+  ctx.free(alt ? re : re_alt);
+  unpack_outputs(ctx, s2, n, b0, b2, b1, second);
+  ctx.free(s2);
 }
 
 }  // namespace vg

@@ -34,6 +34,11 @@ void column_max3(Ctx& ctx, const uint32_t* a, const uint32_t* b, const uint32_t*
 // row), level-2 = (k1 of each (k0,k1) run, first row).
 void build_permutation(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const uint32_t* k2,
                        uint64_t n, const uint32_t maxes[3], PermOutputs& out);
+// Two permutations sharing their leading column: (k0, k1, k2) into `first`
+// and (k0, k2, k1) into `second`, the second re-sorted from the first's
+// sorted keys by (k0, k2) bits only (fewer radix passes than a full sort).
+void build_permutation_pair(Ctx& ctx, const uint32_t* k0, const uint32_t* k1, const uint32_t* k2, uint64_t n,
+                            const uint32_t maxes[3], PermOutputs& first, PermOutputs& second);
 
 // The resident permutation indexes in the reference's VedasStorage layout.
 struct Index {

@@ -27,7 +27,7 @@ constexpr int kMaxPasses = 8;
 
 template <typename K>
 __global__ void __launch_bounds__(kBlock) radix_hist_kernel(const K* __restrict__ keys, uint64_t n,
-                                                            uint32_t passes,
+                                                            uint32_t passes, uint32_t begin_bit,
                                                             unsigned long long* __restrict__ hist) {
   __shared__ uint32_t sh[kMaxPasses * kRadix];
   for (uint32_t i = threadIdx.x; i < kMaxPasses * kRadix; i += kBlock) sh[i] = 0;
@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kBlock) radix_hist_kernel(const K* __restrict_
   for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; i < n; i += stride) {
     K k = keys[i];
     for (uint32_t p = 0; p < passes; ++p)
-      atomicAdd(&sh[p * kRadix + (static_cast<uint32_t>(k >> (8 * p)) & 0xFFu)], 1u);
+      atomicAdd(&sh[p * kRadix + (static_cast<uint32_t>(k >> (begin_bit + 8 * p)) & 0xFFu)], 1u);
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < passes * kRadix; i += kBlock)
@@ -202,13 +202,15 @@ void launch_pass(Ctx& ctx, int items, const K* kin, K* kout, const uint32_t* vin
 
 template <typename K>
 bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* vals_alt, uint64_t n,
-                     int end_bit, bool vals_iota, bool host_skip) {
+                     int begin_bit, int end_bit, bool vals_iota, bool host_skip) {
   const bool has_v = vals != nullptr;
   if (n == 0) return false;
   if (n > 0xFFFFFFFFull && has_v) fail(VG_ERR_OVERFLOW, "radix sort values are 32-bit row ids");
-  int passes = (end_bit + 7) / 8;
+  if (begin_bit < 0 || begin_bit >= end_bit) begin_bit = 0;
+  int passes = (end_bit - begin_bit + 7) / 8;
   if (passes < 1) passes = 1;
-  if (passes > static_cast<int>(sizeof(K))) passes = static_cast<int>(sizeof(K));
+  // the last pass may read bits above end_bit; it must not shift past the key
+  while (passes > 1 && begin_bit + 8 * (passes - 1) >= static_cast<int>(8 * sizeof(K))) --passes;
 
   Scratch<unsigned long long> hist(ctx, passes * kRadix);
   VG_CUDA(cudaMemsetAsync(hist.get(), 0, passes * kRadix * sizeof(unsigned long long), ctx.stream));
@@ -217,7 +219,8 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
   if (grid > gmax) grid = gmax;
   if (grid < 1) grid = 1;
   ctx.launch("radix_histogram", static_cast<double>(n) * sizeof(K), [&] {
-    radix_hist_kernel<K><<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(keys, n, passes, hist.get());
+    radix_hist_kernel<K><<<static_cast<unsigned>(grid), kBlock, 0, ctx.stream>>>(keys, n, passes, begin_bit,
+                                                                                hist.get());
   });
   VG_CUDA(cudaGetLastError());
   Scratch<uint64_t> d_bases(ctx, passes * kRadix);
@@ -270,7 +273,7 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
     const int p = todo[t];
     VG_CUDA(cudaMemsetAsync(status.get(), 0, tiles * kRadix * sizeof(uint64_t), ctx.stream));
     const uint64_t* pb = d_bases.get() + p * kRadix;
-    const uint32_t shift = static_cast<uint32_t>(8 * p);
+    const uint32_t shift = static_cast<uint32_t>(begin_bit + 8 * p);
     if (!has_v)
       launch_pass<K, false, false>(ctx, items, kin, kout, nullptr, nullptr, n, shift, pb, status.get(),
                                    ticket.get() + t);
@@ -290,12 +293,16 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
 
 bool radix_sort_u32(Ctx& ctx, uint32_t* keys, uint32_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
                     uint64_t n, int end_bit, bool vals_iota, bool host_skip) {
-  return radix_sort_impl<uint32_t>(ctx, keys, keys_alt, vals, vals_alt, n, end_bit, vals_iota, host_skip);
+  return radix_sort_impl<uint32_t>(ctx, keys, keys_alt, vals, vals_alt, n, 0, end_bit, vals_iota, host_skip);
 }
 
 bool radix_sort_u64(Ctx& ctx, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
                     uint64_t n, int end_bit, bool vals_iota, bool host_skip) {
-  return radix_sort_impl<uint64_t>(ctx, keys, keys_alt, vals, vals_alt, n, end_bit, vals_iota, host_skip);
+  return radix_sort_impl<uint64_t>(ctx, keys, keys_alt, vals, vals_alt, n, 0, end_bit, vals_iota, host_skip);
+}
+
+bool radix_sort_u64_bits(Ctx& ctx, uint64_t* keys, uint64_t* keys_alt, uint64_t n, int begin_bit, int end_bit) {
+  return radix_sort_impl<uint64_t>(ctx, keys, keys_alt, nullptr, nullptr, n, begin_bit, end_bit, false, true);
 }
 
 void fill_iota(Ctx& ctx, uint32_t* out, uint64_t n) {

@@ -15,6 +15,9 @@ bool radix_sort_u32(Ctx& ctx, uint32_t* keys, uint32_t* keys_alt, uint32_t* vals
                     uint64_t n, int end_bit, bool vals_iota, bool host_skip = true);
 bool radix_sort_u64(Ctx& ctx, uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt,
                     uint64_t n, int end_bit, bool vals_iota, bool host_skip = true);
+// Keys only, ordered by bits [begin_bit, end_bit): a stable sort, so keys
+// equal in those bits keep their input order (their lower bits included).
+bool radix_sort_u64_bits(Ctx& ctx, uint64_t* keys, uint64_t* keys_alt, uint64_t n, int begin_bit, int end_bit);
 void fill_iota(Ctx& ctx, uint32_t* out, uint64_t n);
 
 }  // namespace vg

@@ -50,22 +50,18 @@ void build_index(Ctx& ctx, const uint32_t* s, const uint32_t* p, const uint32_t*
   ix.max_id = std::max(ms, std::max(mp, mo));
   auto put = [&](const char* name, const DevArray& a) { ix.dev[name] = a; };
   {
-    PermOutputs pso;
+    // PSO by a full sort; POS from PSO's sorted keys by a sort of (p, o) only
+    PermOutputs pso, pos;
     pso.want_col1 = pso.want_col2 = pso.want_l1 = pso.want_l2 = true;
+    pos.want_col1 = pos.want_col2 = pos.want_l2 = true;
     const uint32_t m[3] = {mp, ms, mo};
-    build_permutation(ctx, p, s, o, n, m, pso);
+    build_permutation_pair(ctx, p, s, o, n, m, pso, pos);
     put("p_idx_values", pso.l1_vals);
     put("p_idx_offsets", pso.l1_offs);
     put("ps_data", pso.col1);
     put("pso_data", pso.col2);
     put("ps_s_idx_values", pso.l2_vals);
     put("ps_idx_offsets", pso.l2_offs);
-  }
-  {
-    PermOutputs pos;
-    pos.want_col1 = pos.want_col2 = pos.want_l2 = true;
-    const uint32_t m[3] = {mp, mo, ms};
-    build_permutation(ctx, p, o, s, n, m, pos);
     put("po_data", pos.col1);
     put("pos_data", pos.col2);
     put("po_o_idx_values", pos.l2_vals);
