@@ -107,14 +107,18 @@ def test_batch_host_copies_equal_device_results(ctx):
     ix.close()
 
 
+@pytest.mark.parametrize("streams", ["1", "0"])
 @pytest.mark.parametrize("region_mb", ["0", "1", "64"])
-def test_batch_join_placement_regions(ctx, monkeypatch, region_mb):
+def test_batch_join_placement_regions(ctx, monkeypatch, region_mb, streams):
     """Join outputs placed on the device in a per-engine region (the default),
     in a region so small that most outputs overflow it and are written after a
-    host round trip instead, and with no region at all: the same results and
-    logs, and the arena holds no more than before once the batches are freed."""
+    host round trip instead, and with no region at all; the wave engines on
+    streams of their own (the default) or all on the context's stream: the
+    same results and logs, and the arena holds no more than before once the
+    batches are freed."""
     import vedas_gb300 as vg
     monkeypatch.setenv("VG_JOIN_REGION_MB", region_mb)
+    monkeypatch.setenv("VG_ENGINE_STREAMS", streams)
     g = workloads.graph_chain(n=400_000, n_entities=40_000, seed=21)
     qs = workloads.query_mix(g, 400, seed=22)
     ix = vg.Index(ctx, g.s, g.p, g.o)

@@ -90,11 +90,19 @@ class WorkerPool {
   WorkerPool(const WorkerPool&) = delete;
   WorkerPool& operator=(const WorkerPool&) = delete;
 
-  void run(size_t n, const std::function<void(size_t)>& f) {
+  void run(size_t n, const std::function<void(size_t)>& f0) {
     if (n < 64 || workers_.empty()) {   // small loops run on the caller alone
-      for (size_t i = 0; i < n; ++i) f(i);
+      for (size_t i = 0; i < n; ++i) f0(i);
       return;
     }
+    // the items run with the caller's stream and deferred frees
+    const ThreadExec ex = tl_exec;
+    const bool carry = ex.stream != nullptr || ex.defer != nullptr;
+    const std::function<void(size_t)> wrapped = [&](size_t i) {
+      ThreadExecScope sc(ex);
+      f0(i);
+    };
+    const std::function<void(size_t)>& f = carry ? wrapped : f0;
     std::lock_guard<std::mutex> serial(run_mu_);  // one parallel loop at a time
     // No worker is inside a loop here (the last one closed with active_ at 0),
     // so the loop's state can be written before it is opened.
@@ -390,6 +398,25 @@ WaveEngine::WaveEngine(Ctx& ctx, int key_bits) : ctx_(ctx), key_bits_(key_bits) 
   VG_CUDA(cudaEventCreateWithFlags(&ev_b_, cudaEventDisableTiming | cudaEventBlockingSync));
 }
 
+void WaveEngine::use_own_stream() {
+  if (own_stream_) return;
+  VG_CUDA(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
+  // the engine's work starts after everything already on the context's stream
+  cudaEvent_t ev;
+  VG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  VG_CUDA(cudaEventRecord(ev, ctx_.stream.main));
+  VG_CUDA(cudaStreamWaitEvent(own_stream_, ev, 0));
+  cudaEventDestroy(ev);
+}
+
+ThreadExec WaveEngine::exec() { return ThreadExec{own_stream_, own_stream_ ? &defer_ : nullptr}; }
+
+void WaveEngine::finish_stream() {
+  if (!own_stream_) return;
+  VG_CUDA(cudaStreamSynchronize(own_stream_));
+  ctx_.flush(defer_);
+}
+
 namespace {
 // Waits for a stage's event: polls briefly (most stages are nearly done
 // when asked), then sleeps in the CUDA driver so that a waiting engine thread
@@ -406,12 +433,18 @@ void wait_event(cudaEvent_t ev) {
 
 WaveEngine::~WaveEngine() {
   bury();
-  if (a_pending_ || b_pending_) cudaStreamSynchronize(ctx_.stream);
-  for (auto& r : jouts_) rel_free(ctx_, r);
-  if (jb_.lo || jb_.offs || jb_.d_totals) jb_.release(ctx_);
-  if (d_bump_) ctx_.free(d_bump_);
+  if (own_stream_) cudaStreamSynchronize(own_stream_);
+  else if (a_pending_ || b_pending_) cudaStreamSynchronize(ctx_.stream.main);
+  {
+    ThreadExecScope sc(exec());
+    for (auto& r : jouts_) rel_free(ctx_, r);
+    if (jb_.lo || jb_.offs || jb_.d_totals) jb_.release(ctx_);
+    if (d_bump_) ctx_.free(d_bump_);
+  }
+  ctx_.flush(defer_);   // the stream is idle: every held-back free is safe now
   // the region goes back to the arena when its last output is freed
   if (region_) ctx_.arena.region_close(region_);
+  if (own_stream_) cudaStreamDestroy(own_stream_);
   if (ev_a_) cudaEventDestroy(ev_a_);
   if (ev_b_) cudaEventDestroy(ev_b_);
 }
@@ -449,6 +482,7 @@ void WaveEngine::reset() {
 }
 
 void WaveEngine::step(std::vector<PlannedQuery*>& completed) {
+  ThreadExecScope sc(exec());
   if (next_is_a_) stage_a(completed);
   else stage_b(completed);
   next_is_a_ = !next_is_a_;
@@ -523,6 +557,9 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     b_pending_ = false;
     prof.device_s += since(t0);
   }
+  // everything enqueued on the engine's stream so far is done (waited for
+  // now, or in stage B, with nothing enqueued since): held-back frees are safe
+  if (own_stream_) ctx_.flush(defer_);
   if (tracing) tr.t_wait = since(trace_origin);
   {
     auto tf = Clock::now();
@@ -710,6 +747,7 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   wait_event(ev_a_);
   a_pending_ = false;
   prof.device_s += since(t0);
+  if (own_stream_) ctx_.flush(defer_);
   if (tracing) tr.t_wait = since(trace_origin);
   const uint64_t* ha = h_a_.data();
 
@@ -957,9 +995,15 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
     out.host = std::make_unique<HostResults>(ctx);
     for (auto& e : eng) e->set_host_results(out.host.get());
   }
-  // each engine places its join outputs on the device, in a region of its own
+  // each engine places its join outputs on the device, in a region of its
+  // own, and (VG_ENGINE_STREAMS, default on) issues its work on a stream of
+  // its own, so that the engines' kernels overlap on the device
   const size_t region_bytes = join_region_bytes(ctx, ne);
-  for (auto& e : eng) e->use_region(region_bytes);
+  const bool own_streams = engine_streams();
+  for (auto& e : eng) {
+    e->use_region(region_bytes);
+    if (own_streams) e->use_own_stream();
+  }
   const char* trace_path = std::getenv("VG_WAVE_TRACE");
   for (auto& e : eng) {
     e->tracing = trace_path != nullptr;
@@ -984,6 +1028,8 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
   for (size_t e = 1; e < ne; ++e) th.emplace_back(drive, e);
   drive(0);
   for (auto& t : th) t.join();
+  // the results are read on the context's stream: the engines' streams finish first
+  for (auto& e : eng) e->finish_stream();
   for (auto& e : err)
     if (e) std::rethrow_exception(e);
   out.waves = 0;
@@ -1032,6 +1078,11 @@ size_t join_region_bytes(const Ctx& ctx, size_t engines) {
   return std::min(want, cap);
 }
 
+bool engine_streams() {
+  const char* e = std::getenv("VG_ENGINE_STREAMS");
+  return !(e && std::strtol(e, nullptr, 10) == 0);
+}
+
 size_t batch_engines() {
   static const size_t n = [] {
     long v = 4;
@@ -1044,6 +1095,8 @@ size_t batch_engines() {
 void post_background(void (*fn)(void*), void* arg) { WorkerPool::get().post(fn, arg); }
 
 void drain_background() {
+  // the queued releases free blocks whose last use is done: to the arena at once
+  ThreadExecScope sc(ThreadExec{tl_exec.stream, nullptr});
   WorkerPool::global().drain();
   if (g_engine_pools_made.load())
     for (auto& p : engine_pools()) p->drain();

@@ -87,6 +87,9 @@ size_t batch_engines();
 // Bytes of the region in which each of `engines` wave engines places its join
 // outputs on the device (0: no region).
 size_t join_region_bytes(const Ctx& ctx, size_t engines);
+// Whether the wave engines of a batch run on streams of their own
+// (VG_ENGINE_STREAMS=0 puts them all on the context's stream).
+bool engine_streams();
 void prepare_mirrors(vedas::VedasStorage* storage);
 
 // Advances every added query by one job per wave; the device work of a wave
@@ -127,6 +130,11 @@ class WaveEngine {
   // follows its count without a host round trip; outputs that do not fit
   // are written after one, as without a region.
   void use_region(size_t bytes);
+  // Issues the engine's work on a stream of its own (after everything on the
+  // context's stream), with its frees held back until its stream has passed
+  // the blocks' last use.  finish_stream waits for that stream.
+  void use_own_stream();
+  void finish_stream();
   // Destroys the plans of handed-back queries that are still pending.
   void bury();
   uint32_t waves() const { return waves_; }
@@ -193,6 +201,10 @@ class WaveEngine {
   size_t off_tot_ = 0, off_fin_ = 0, off_c0_ = 0, off_err_ = 0;   // words into h_a_
   size_t off_fla_ = 0, off_bump_ = 0, off_c0a_ = 0;               // words into h_a_ (placed joins)
   size_t off_fl_ = 0, off_jc0_ = 0;                               // words into h_b_
+  // the engine's own stream and its held-back frees (use_own_stream)
+  cudaStream_t own_stream_ = nullptr;
+  DeferredFrees defer_;
+  ThreadExec exec();
   // device-side placement of join outputs (use_region)
   Arena::Region* region_ = nullptr;
   uint64_t* d_bump_ = nullptr;     // device: region bytes handed out

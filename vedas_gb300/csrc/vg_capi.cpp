@@ -116,7 +116,7 @@ vg_status vg_ctx_create(int device, size_t arena_bytes, vg_ctx** out) {
     vg::Ctx& c = h->c;
     c.device = device;
     VG_CUDA(cudaSetDevice(device));
-    VG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    VG_CUDA(cudaStreamCreateWithFlags(&c.stream.main, cudaStreamNonBlocking));
     VG_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
     if (arena_bytes == 0) {
       size_t fr = 0, tot = 0;
@@ -141,14 +141,14 @@ vg_status vg_ctx_destroy(vg_ctx* ctx) {
   vg::Ctx& c = ctx->c;
   // queued releases of finished queries free into this context's arena
   guard([] { vg::drain_background(); });
-  if (c.stream) cudaStreamSynchronize(c.stream);
+  if (c.stream.main) cudaStreamSynchronize(c.stream.main);
   c.release_dl_stream();
   c.release_pinned();
   c.release_upload_ring();
   c.arena.release();
   if (c.d_err) cudaFree(c.d_err);
   if (c.h_small) cudaFreeHost(c.h_small);
-  if (c.stream) cudaStreamDestroy(c.stream);
+  if (c.stream.main) cudaStreamDestroy(c.stream.main);
   delete ctx;
   return VG_OK;
 }
@@ -168,7 +168,7 @@ vg_status vg_ctx_sync(vg_ctx* ctx) {
   return guard([&] { ctx->c.sync(); });
 }
 
-void* vg_ctx_stream(vg_ctx* ctx) { return ctx ? static_cast<void*>(ctx->c.stream) : nullptr; }
+void* vg_ctx_stream(vg_ctx* ctx) { return ctx ? static_cast<void*>(ctx->c.stream.main) : nullptr; }
 
 vg_status vg_stats_reset(vg_ctx* ctx, int timing) {
   if (!ctx) return VG_ERR_INVALID;

@@ -143,6 +143,47 @@ struct KernelStat {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
 };
 
+// Frees held back until the work that may still read the blocks is known to
+// be done: a wave engine with a stream of its own collects its frees here
+// while its stage runs and hands them to the arena after its next wait on
+// that stream (flush), so that no other engine's stream reuses a block that
+// a kernel still in flight reads.
+struct DeferredFrees {
+  std::mutex mu;
+  std::vector<void*> blocks;
+  void push(void* p) {
+    std::lock_guard<std::mutex> lk(mu);
+    blocks.push_back(p);
+  }
+};
+
+// Per host thread: the stream its work goes to (null: the context's own) and
+// where its frees go (null: to the arena at once).  A wave engine sets both
+// on its thread; the worker pools carry them into the items of a parallel
+// loop.
+struct ThreadExec {
+  cudaStream_t stream = nullptr;
+  DeferredFrees* defer = nullptr;
+};
+inline thread_local ThreadExec tl_exec;
+
+// Sets the calling thread's ThreadExec for a scope.
+struct ThreadExecScope {
+  ThreadExec saved;
+  explicit ThreadExecScope(const ThreadExec& e) : saved(tl_exec) { tl_exec = e; }
+  ~ThreadExecScope() { tl_exec = saved; }
+  ThreadExecScope(const ThreadExecScope&) = delete;
+  ThreadExecScope& operator=(const ThreadExecScope&) = delete;
+};
+
+// The context's stream as seen by the calling thread: the thread's own
+// stream when it has one (a wave engine's), else the context's.  Converts to
+// cudaStream_t wherever a stream is passed.
+struct StreamRef {
+  cudaStream_t main = nullptr;
+  operator cudaStream_t() const { return tl_exec.stream ? tl_exec.stream : main; }
+};
+
 // Launch parameters chosen per context (vg_tune_set; the autotuner picks
 // them from timed trials).  Each choice changes only speed, never results.
 struct TuneParams {
@@ -156,7 +197,7 @@ struct TuneParams {
 struct Ctx {
   int device = 0;
   TuneParams tune;
-  cudaStream_t stream = nullptr;
+  StreamRef stream;   // the context's stream (stream.main), or the calling thread's own
   Arena arena;
   DeviceErrors* d_err = nullptr;   // device error record
   int num_sms = 0;
@@ -233,7 +274,20 @@ struct Ctx {
   T* alloc(uint64_t n) {
     return static_cast<T*>(arena.alloc((n ? n : 1) * sizeof(T)));
   }
-  void free(void* p) { arena.free(p); }
+  void free(void* p) {
+    if (!p) return;
+    if (tl_exec.defer) tl_exec.defer->push(p);
+    else arena.free(p);
+  }
+  // Hands a collection of held-back frees to the arena (their work is done).
+  void flush(DeferredFrees& d) {
+    std::vector<void*> v;
+    {
+      std::lock_guard<std::mutex> lk(d.mu);
+      v.swap(d.blocks);
+    }
+    for (void* p : v) arena.free(p);
+  }
   void sync() { VG_CUDA(cudaStreamSynchronize(stream)); }
   // Raises VG_ERR_TIMEOUT / VG_ERR_OVERFLOW if a kernel recorded one (syncs).
   void check_device_errors();
