@@ -409,7 +409,13 @@ void WaveEngine::use_own_stream() {
   cudaEventDestroy(ev);
 }
 
-ThreadExec WaveEngine::exec() { return ThreadExec{own_stream_, own_stream_ ? &defer_ : nullptr}; }
+ThreadExec WaveEngine::exec() { return ThreadExec{own_stream_, nullptr}; }
+
+// While a stage enqueues device work, the blocks it frees (scratch of the
+// launches just enqueued) may still be read on the engine's stream: those
+// frees are held back.  Elsewhere in a stage every block freed was last used
+// by work the stage has already waited for, and goes back at once.
+ThreadExec WaveEngine::enqueue_exec() { return ThreadExec{own_stream_, own_stream_ ? &defer_ : nullptr}; }
 
 void WaveEngine::finish_stream() {
   if (!own_stream_) return;
@@ -436,7 +442,7 @@ WaveEngine::~WaveEngine() {
   if (own_stream_) cudaStreamSynchronize(own_stream_);
   else if (a_pending_ || b_pending_) cudaStreamSynchronize(ctx_.stream.main);
   {
-    ThreadExecScope sc(exec());
+    ThreadExecScope sc(exec());   // the stream is idle: frees go back at once
     for (auto& r : jouts_) rel_free(ctx_, r);
     if (jb_.lo || jb_.offs || jb_.d_totals) jb_.release(ctx_);
     if (d_bump_) ctx_.free(d_bump_);
@@ -642,6 +648,7 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
   tr.h_final = since(t0);
 
   // device half 1
+  ThreadExecScope enqueue_scope(enqueue_exec());
   t0 = Clock::now();
   std::vector<Rel*> to_sort;
   std::vector<const Rel*> swap_rels;
@@ -794,6 +801,7 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
     if (host_) {
       std::vector<BatchQuery*> outs;
       for (PlannedQuery* q : final_) outs.push_back(q->out);
+      ThreadExecScope es(enqueue_exec());
       host_->add(outs);
     }
     final_.clear();
@@ -803,6 +811,7 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   prof.final_s += since(t0);
 
   // device half 2: join outputs
+  ThreadExecScope enqueue_scope(enqueue_exec());
   t0 = Clock::now();
   if (!joins_.empty() && placed_wave_) {
     DeviceErrors he;

@@ -204,7 +204,8 @@ class WaveEngine {
   // the engine's own stream and its held-back frees (use_own_stream)
   cudaStream_t own_stream_ = nullptr;
   DeferredFrees defer_;
-  ThreadExec exec();
+  ThreadExec exec();           // the engine's stream, frees at once
+  ThreadExec enqueue_exec();   // the engine's stream, frees held back
   // device-side placement of join outputs (use_region)
   Arena::Region* region_ = nullptr;
   uint64_t* d_bump_ = nullptr;     // device: region bytes handed out
