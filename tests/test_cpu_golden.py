@@ -285,9 +285,10 @@ def test_query_texts_packed_for_the_c_abi(built):
 
 def test_level2_lookup_table_matches_reference_searches(built):
     """The select lookups through the per-predicate level-2 range table (and
-    the upper bound searched forward from the lower one) give the reference's
-    std::lower_bound / std::upper_bound results on random index arrays, the
-    out-of-bounds cases included.  No device is used."""
+    the upper bound searched forward from the lower one), and the fenced
+    searches of the select bounds and empty-interval pieces, give the
+    reference's std::lower_bound / std::upper_bound results on random index
+    arrays, the out-of-bounds cases included.  No device is used."""
     import vedas_gb300 as vg
     L = vg.lib()
     bad = ctypes.c_uint64(1)

@@ -53,8 +53,11 @@ const char* const VedasStorage::kMirrorName[VedasStorage::kMirrors] = {
 void VedasStorage::prepareMirrors() {
   std::call_once(mirrors_once_, [this] {
     for (int m = 0; m < kMirrors; ++m) h(static_cast<Mirror>(m));
-    for (int po = 0; po < 2; ++po)
+    for (int po = 0; po < 2; ++po) {
       l2r_[po] = QueryExecutor::l2RangesOfL1(*mirror_[kPIdxO], *mirror_[po ? kPOIdxO : kPSIdxO], ix_.n);
+      const TYPEID_HOST_VEC& d = *mirror_[po ? kPO : kPS];
+      fence_[po] = make_fences(d.data(), d.size());
+    }
   });
 }
 
@@ -211,18 +214,21 @@ void EmptyIntervalDict::updateBound(const std::string& var, size_t lb1, size_t u
 void EmptyIntervalDict::getUploadRelationData(const std::string& var, const TYPEID* data, size_t start,
                                               size_t end, size_t& relationSize,
                                               std::vector<std::pair<size_t, size_t>>& up,
-                                              std::vector<size_t>& offsets) {
+                                              std::vector<size_t>& offsets, const std::vector<uint32_t>* fences) {
   up.clear();
   offsets.clear();
   VAR_BOUND& t = dict[var];
   const size_t lb1 = std::get<0>(t), ub1 = std::get<1>(t), lb2 = std::get<2>(t), ub2 = std::get<3>(t);
   if (!(lb1 == 0 || ub1 == 0 || lb1 != ub1) || !(lb2 == 0 || ub2 == 0 || lb2 != ub2))
     throw ReferenceUB("EmptyIntervalDict assert: degenerate interval for " + var);
+  // bounds of 64-bit values over 32-bit keys, searched through the fences when given
   auto lb = [&](size_t v) {
+    if (fences) return fenced_bound(data, *fences, start, end, v, false);
     return static_cast<size_t>(
         std::lower_bound(data + start, data + end, v, [](TYPEID a, size_t b) { return a < b; }) - data);
   };
   auto ub = [&](size_t v) {
+    if (fences) return fenced_bound(data, *fences, start, end, v, true);
     return static_cast<size_t>(
         std::upper_bound(data + start, data + end, v, [](size_t a, TYPEID b) { return a < b; }) - data);
   };
@@ -716,10 +722,9 @@ void SelectQueryJob::prepare(SelectWork& w) {
   size_t first = b0, second = e0;
   if (ex->variables_bound.count(variables[0]) > 0) {
     auto bd = ex->variables_bound[variables[0]];
-    if (bd.first > cur_min)
-      first = std::lower_bound(l2d->begin() + b0, l2d->begin() + e0, bd.first) - l2d->begin();
-    if (bd.second < cur_max)
-      second = std::upper_bound(l2d->begin() + b0, l2d->begin() + e0, bd.second) - l2d->begin();
+    const std::vector<uint32_t>& fences = st->l2Fences(pos_index);
+    if (bd.first > cur_min) first = fenced_bound(l2d->data(), fences, b0, e0, bd.first, false);
+    if (bd.second < cur_max) second = fenced_bound(l2d->data(), fences, b0, e0, bd.second, true);
   }
   size_t ds = first, de = second;
   if (ds > de) de = ds;
@@ -760,7 +765,8 @@ void SelectQueryJob::prepare(SelectWork& w) {
   size_t total = 0;
   std::vector<std::pair<size_t, size_t>> up;
   std::vector<size_t> offs;
-  ex->empty_interval_dict.getUploadRelationData(variables[0], l2d->data(), ds, de, total, up, offs);
+  ex->empty_interval_dict.getUploadRelationData(variables[0], l2d->data(), ds, de, total, up, offs,
+                                                &st->l2Fences(pos_index));
   // one whole interval: the relation views the two index slices
   if (up.size() == 1 && offs[0] == 0 && up[0].second >= up[0].first && up[0].second - up[0].first == total &&
       total > 0) {
@@ -1271,7 +1277,7 @@ uint64_t selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups) {
       pid += 1 + static_cast<TYPEID>(rnd(3));
       l1v.push_back(pid);
       l1o.push_back(static_cast<TYPEID>(data.size()));
-      const size_t nk = 1 + rnd(60);
+      const size_t nk = 1 + rnd(gi % 2 ? 3000 : 60);   // long predicates exercise the fenced searches
       TYPEID key = static_cast<TYPEID>(rnd(5));
       for (size_t k = 0; k < nk; ++k) {
         key += (dups && rnd(4) == 0) ? 0 : 1 + static_cast<TYPEID>(rnd(4));
@@ -1283,6 +1289,7 @@ uint64_t selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups) {
     }
     const size_t n = data.size();
     const std::vector<size_t> l2r = QueryExecutor::l2RangesOfL1(l1o, l2o, n);
+    const std::vector<uint32_t> fences = make_fences(data.data(), data.size());
     for (uint32_t li = 0; li < lookups; ++li) {
       const TYPEID id1 = static_cast<TYPEID>(rnd(pid + 3));
       const TYPEID id2 = static_cast<TYPEID>(rnd(l2v.empty() ? 8 : l2v.back() + 3));
@@ -1301,6 +1308,9 @@ uint64_t selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups) {
         const size_t ws = std::lower_bound(data.begin() + lo, data.begin() + hi, id2) - data.begin();
         const size_t we = std::upper_bound(data.begin() + lo, data.begin() + hi, id2) - data.begin();
         if (d.first != ws || d.second != we) ++bad;
+        // the fenced searches of the select bounds and empty-interval pieces
+        if (fenced_bound(data.data(), fences, lo, hi, id2, false) != ws) ++bad;
+        if (fenced_bound(data.data(), fences, lo, hi, id2, true) != we) ++bad;
       }
     }
   }

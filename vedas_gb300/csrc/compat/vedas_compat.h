@@ -17,6 +17,8 @@
 // for the host-side binary searches the reference performs.
 #pragma once
 
+#include "vg_fence.h"
+
 #include <cstdint>
 #include <array>
 #include <map>
@@ -99,6 +101,9 @@ class VedasStorage {
   // uses the triple count), i.e. findDataOffsetFromL2's two searches of the
   // level-2 offsets done once per predicate.  Empty before prepareMirrors().
   const std::vector<size_t>& l2RangeOfL1(bool po) const { return l2r_[po ? 1 : 0]; }
+  // Every 64th key of the level-2 data (ps_data for po = false, po_data for
+  // po = true), for fenced_bound; empty before prepareMirrors().
+  const std::vector<uint32_t>& l2Fences(bool po) const { return fence_[po ? 1 : 0]; }
   // Device copies (resident).
   const TYPEID* dev(const char* name) const { return ix_.get(name).ptr; }
   const TYPEID* devPSdata() const { return d_[kPS]; }
@@ -123,6 +128,7 @@ class VedasStorage {
   TYPEID_HOST_VEC* mirror_[kMirrors] = {};
   const TYPEID* d_[kMirrors] = {};
   std::vector<size_t> l2r_[2];
+  std::vector<uint32_t> fence_[2];
   std::once_flag mirrors_once_;
   void cacheDevice();   // the device arrays' addresses (set at construction)
   TYPEID_HOST_VEC* h(Mirror m) {
@@ -196,7 +202,8 @@ class EmptyIntervalDict {
   // (offsets relative to the start of `data`).
   void getUploadRelationData(const std::string& var, const TYPEID* data, size_t start, size_t end,
                              size_t& relationSize, std::vector<std::pair<size_t, size_t>>& uploadIntervals,
-                             std::vector<size_t>& offsets);
+                             std::vector<size_t>& offsets,
+                             const std::vector<uint32_t>* fences = nullptr);
   size_t emptySize(const std::string& var);
   bool hasBoundFor(const std::string& var) const { return dict.count(var) > 0; }
 
