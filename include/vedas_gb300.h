@@ -364,7 +364,7 @@ vg_status vg_selfcheck_pools(uint32_t pools, uint32_t threads, uint32_t loops, u
  * index arrays, `lookups` random (predicate, key) lookups through the
  * per-predicate level-2 range table, and searches of level-2 data ranges
  * through their sampled fences, give what the reference's searches give
- * (src/QueryExecutor.cu:596-646, src/QueryExecutor.cu:720-722,
+ * (src/QueryExecutor.cu:596-646, src/SelectQueryJob.cu:74-86,
  * src/EmptyIntervalDict.cu:108-170), out-of-bounds cases included.
  * *mismatches = lookups that differ. */
 vg_status vg_selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookups, uint64_t* mismatches);
