@@ -662,6 +662,7 @@ def serve_point(srv, qb, rate, duration, clients, seed):
     for t in th:
         t.join()
     lat, ok, rej = [], 0, 0
+    statuses = {}
     for i, t in enumerate(tickets):
         srv.wait(t)
         st = srv.status(t)
@@ -671,10 +672,12 @@ def serve_point(srv, qb, rate, duration, clients, seed):
             lat.append(tot + max(late[i], 0.0))
         else:
             rej += 1
+            statuses[st] = statuses.get(st, 0) + 1
         srv.release(t)
     wall = time.perf_counter() - t0
     return {"offered_rate": rate, "queries": n_q, "served_rate": ok / wall, "completed": ok,
-            "failed_or_rejected": rej, "wall_s": wall,
+            "failed_or_rejected": rej, "failure_statuses": {str(k): v for k, v in sorted(statuses.items())},
+            "wall_s": wall,
             "latency_ms": {"p50": 1000 * float(np.percentile(lat, 50)), "p95": 1000 * float(np.percentile(lat, 95)),
                            "p99": 1000 * float(np.percentile(lat, 99))}}
 

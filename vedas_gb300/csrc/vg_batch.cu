@@ -101,32 +101,6 @@ __global__ void __launch_bounds__(kBlock) bcopy_kernel(const CopyPiece* __restri
 }
 
 // ---------------------------------------------------------------------------
-// Flags (bit i) of the rows r0 + i (i < kRows, r0 a multiple of kRows) that
-// differ from the previous row in column `col` (n rows; row 0 is left to the
-// caller).  A 16-byte aligned column is read with two 16-byte loads.
-__device__ __forceinline__ uint32_t diff_bits(const uint32_t* __restrict__ col, uint64_t n, uint64_t r0) {
-  static_assert(kRows == 8, "two 16-byte loads cover a thread's rows");
-  uint32_t v[kRows];
-  if ((reinterpret_cast<uintptr_t>(col) & 15u) == 0 && r0 + kRows <= n) {
-    const uint4 a = *reinterpret_cast<const uint4*>(col + r0);
-    const uint4 b = *reinterpret_cast<const uint4*>(col + r0 + 4);
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-  } else {
-#pragma unroll
-    for (int i = 0; i < kRows; ++i) v[i] = (r0 + i < n) ? col[r0 + i] : 0u;
-  }
-  uint32_t prev = (r0 > 0 && r0 - 1 < n) ? col[r0 - 1] : 0u;
-  uint32_t d = 0;
-#pragma unroll
-  for (int i = 0; i < kRows; ++i) {
-    const uint64_t r = r0 + i;
-    if (r < n && r > 0 && v[i] != prev) d |= 1u << i;
-    prev = v[i];
-  }
-  return d;
-}
-
 // Adjacent-unique compaction of every segment.  Segments of at most
 // kSmallSeg rows (most final results) take one warp each in the first
 // small_blocks blocks: each lane flags its kRows consecutive rows, a warp
@@ -139,7 +113,7 @@ __device__ __forceinline__ void unique_small_segment(const SegRows& g, uint64_t*
   const uint32_t lane = lane_id();
   const uint64_t n = g.n, r0 = static_cast<uint64_t>(lane) * kRows;
   uint32_t diff = (r0 == 0 && n > 0) ? 1u : 0u;
-  for (uint32_t c = 0; c < g.ncols; ++c) diff |= diff_bits(g.in[c], n, r0);
+  for (uint32_t c = 0; c < g.ncols; ++c) diff |= unique_diff_bits(g.in[c], n, r0);
   if (r0 >= n) diff = 0;
   else if (n - r0 < kRows) diff &= (1u << (n - r0)) - 1u;
   const uint32_t cnt = __popc(diff);
@@ -169,6 +143,7 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
   __shared__ uint32_t s_tile;
   __shared__ SegRows s_seg;
   __shared__ uint32_t s_s;
+  __shared__ uint32_t s_keep[kTileRows];
   if (threadIdx.x == 0) {
     s_tile = atomicAdd(ticket, 1u);
     s_s = tile_seg[s_tile];
@@ -181,7 +156,7 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
   const uint32_t ncols = s_seg.ncols;
   const uint64_t r0 = (tile - tstart[s]) * kTileRows + threadIdx.x * kRows;
   uint32_t diff = (r0 == 0) ? 1u : 0u;
-  for (uint32_t c = 0; c < ncols; ++c) diff |= diff_bits(s_seg.in[c], n, r0);
+  for (uint32_t c = 0; c < ncols; ++c) diff |= unique_diff_bits(s_seg.in[c], n, r0);
   if (r0 >= n) diff = 0;
   else if (n - r0 < kRows) diff &= (1u << (n - r0)) - 1u;
   uint32_t tot;
@@ -193,12 +168,7 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
   __syncthreads();
   const uint64_t g = s_b;
   if (tile == tstart[s + 1] - 1 && threadIdx.x == 0) counts[s] = g + tot;
-  uint64_t o = g + e;
-  for (int i = 0; i < kRows; ++i) {
-    if (!(diff >> i & 1u)) continue;
-    for (uint32_t c = 0; c < ncols; ++c) s_seg.out[c][o] = s_seg.in[c][r0 + i];
-    ++o;
-  }
+  compact_store<kBlock>(s_seg.in, s_seg.out, ncols, n, r0, diff, e, tot, g, s_keep);
 }
 
 // ---------------------------------------------------------------------------

@@ -220,6 +220,54 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Adjacent-unique building blocks (a thread owns 8 consecutive rows r0..r0+7,
+// r0 a multiple of 8).  unique_diff_bits: bit i set when row r0 + i (< n)
+// differs from the row before it in column `col` (row 0 is left to the
+// caller); a 16-byte aligned column is read with two 16-byte loads.
+__device__ __forceinline__ uint32_t unique_diff_bits(const uint32_t* __restrict__ col, uint64_t n, uint64_t r0) {
+  uint32_t v[8];
+  if ((reinterpret_cast<uintptr_t>(col) & 15u) == 0 && r0 + 8 <= n) {
+    const uint4 a = *reinterpret_cast<const uint4*>(col + r0);
+    const uint4 b = *reinterpret_cast<const uint4*>(col + r0 + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = (r0 + i < n) ? col[r0 + i] : 0u;
+  }
+  uint32_t prev = (r0 > 0 && r0 - 1 < n) ? col[r0 - 1] : 0u;
+  uint32_t d = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint64_t r = r0 + i;
+    if (r < n && r > 0 && v[i] != prev) d |= 1u << i;
+    prev = v[i];
+  }
+  return d;
+}
+
+// compact_store: the kept rows of a tile (bit i of `keep` for row r0 + i,
+// the thread's first kept row at tile position e, `tot` kept in the tile,
+// the tile's first at output row g) written column by column through shared
+// memory (s_buf: BLOCK * 8 words), so that every store of a column is
+// coalesced.  Every thread of the block calls it.
+template <int BLOCK>
+__device__ __forceinline__ void compact_store(const uint32_t* const* in, uint32_t* const* out, uint32_t ncols,
+                                              uint64_t n, uint64_t r0, uint32_t keep, uint32_t e, uint32_t tot,
+                                              uint64_t g, uint32_t* s_buf) {
+  for (uint32_t c = 0; c < ncols; ++c) {
+    const uint32_t* col = in[c];
+    uint32_t o = e;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if ((keep >> i & 1u) && r0 + i < n) s_buf[o++] = col[r0 + i];
+    __syncthreads();
+    uint32_t* dst = out[c] + g;
+    for (uint32_t k = threadIdx.x; k < tot; k += BLOCK) dst[k] = s_buf[k];
+    __syncthreads();
+  }
+}
+
 // Branch-free lower/upper bound over a sorted device array.
 template <typename T, typename V>
 __device__ __forceinline__ uint64_t lower_bound_dev(const T* a, uint64_t lo, uint64_t hi, V key) {

@@ -82,38 +82,29 @@ struct UniqueArgs {
   DeviceErrors* err;
 };
 
+// Adjacent-unique compaction: each thread flags its kRows rows (16-byte
+// loads of aligned columns), a block scan and a look-back place the tile's
+// kept rows, which are stored column by column through shared memory so
+// that every store is coalesced.
 __global__ void __launch_bounds__(kBlock) unique_kernel(UniqueArgs a) {
+  static_assert(kRows == 8, "unique_diff_bits and compact_store take 8 rows per thread");
   __shared__ uint32_t s_scan[kBlock / 32 + 1];
   __shared__ uint64_t s_b;
   __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_keep[kTileRows];
   if (threadIdx.x == 0) s_tile = atomicAdd(a.ticket, 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint64_t r0 = static_cast<uint64_t>(tile) * kTileRows + threadIdx.x * kRows;
   uint32_t diff = (r0 == 0) ? 1u : 0u;
-  for (uint32_t c = 0; c < a.ncols; ++c) {
-    const uint32_t* col = a.in[c];
-    uint32_t prev = (r0 > 0 && r0 - 1 < a.n) ? col[r0 - 1] : 0u;
-#pragma unroll
-    for (int i = 0; i < kRows; ++i) {
-      const uint64_t r = r0 + i;
-      const uint32_t v = (r < a.n) ? col[r] : 0u;
-      if (r < a.n && r > 0 && v != prev) diff |= 1u << i;
-      prev = v;
-    }
-  }
+  for (uint32_t c = 0; c < a.ncols; ++c) diff |= unique_diff_bits(a.in[c], a.n, r0);
   if (r0 >= a.n) diff = 0;
   else if (a.n - r0 < kRows) diff &= (1u << (a.n - r0)) - 1u;
   uint32_t tot;
   const uint32_t e = block_excl_scan<kBlock>(__popc(diff), tot, s_scan);
   const uint64_t g = block_lookback(a.status, tile, tot, a.err, &s_b);
   if (tile == a.tiles - 1 && threadIdx.x == 0) *a.count = g + tot;
-  uint64_t o = g + e;
-  for (int i = 0; i < kRows; ++i) {
-    if (!(diff >> i & 1u)) continue;
-    for (uint32_t c = 0; c < a.ncols; ++c) a.out[c][o] = a.in[c][r0 + i];
-    ++o;
-  }
+  compact_store<kBlock>(a.in, a.out, a.ncols, a.n, r0, diff, e, tot, g, s_keep);
 }
 
 // ---------------------------------------------------------------------------
