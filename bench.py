@@ -630,14 +630,20 @@ def bench_c3(args, rank, world, local, pg):
 def serve_point(srv, qb, rate, duration, clients, seed):
     """One offered rate: Poisson arrivals over `duration` seconds, split over
     `clients` submitter threads (arrival i goes to thread i % clients); each
-    thread submits its due queries in one call.  A query's latency runs from
+    thread submits its due queries in one call and hands the tickets to a
+    collector of its own, which waits for each result and releases it (the
+    server counts unreleased results against its memory budget, as a client
+    that reads its results and lets go of them).  A query's latency runs from
     its scheduled arrival to its completion."""
+    import queue as _queue
     n_q = int(rate * duration)
     rng = np.random.Generator(np.random.PCG64(seed))
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_q))
     picks = rng.integers(0, len(qb), size=n_q)
-    tickets = [None] * n_q
     late = np.zeros(n_q)
+    status = np.zeros(n_q, dtype=np.int64)
+    total = np.zeros(n_q)
+    inbox = [_queue.SimpleQueue() for _ in range(clients)]
     t0 = time.perf_counter()
 
     def client(c):
@@ -651,32 +657,38 @@ def serve_point(srv, qb, rate, duration, clients, seed):
             e = k + int(np.searchsorted(arrivals[mine[k:]], now, side="right"))
             idx = mine[k:e]
             sub = time.perf_counter() - t0
-            for i, t in zip(idx, srv.submit_many([qb[j] for j in picks[idx]])):
-                tickets[i] = t
-                late[i] = sub - arrivals[i]
+            ts = srv.submit_many([qb[j] for j in picks[idx]])
+            late[idx] = sub - arrivals[idx]
+            inbox[c].put((idx, ts))
             k = e
+        inbox[c].put(None)
+
+    def collector(c):
+        while True:
+            item = inbox[c].get()
+            if item is None:
+                return
+            for i, t in zip(*item):
+                srv.wait(t)
+                status[i] = srv.status(t)
+                total[i] = srv.latency(t)[1]
+                srv.release(t)
 
     th = [threading.Thread(target=client, args=(c,)) for c in range(clients)]
+    th += [threading.Thread(target=collector, args=(c,)) for c in range(clients)]
     for t in th:
         t.start()
     for t in th:
         t.join()
-    lat, ok, rej = [], 0, 0
-    statuses = {}
-    for i, t in enumerate(tickets):
-        srv.wait(t)
-        st = srv.status(t)
-        _, tot = srv.latency(t)
-        if st == 0:
-            ok += 1
-            lat.append(tot + max(late[i], 0.0))
-        else:
-            rej += 1
-            statuses[st] = statuses.get(st, 0) + 1
-        srv.release(t)
     wall = time.perf_counter() - t0
+    okm = status == 0
+    lat = total[okm] + np.maximum(late[okm], 0.0)
+    ok = int(okm.sum())
+    statuses = {}
+    for st in status[~okm]:
+        statuses[int(st)] = statuses.get(int(st), 0) + 1
     return {"offered_rate": rate, "queries": n_q, "served_rate": ok / wall, "completed": ok,
-            "failed_or_rejected": rej, "failure_statuses": {str(k): v for k, v in sorted(statuses.items())},
+            "failed_or_rejected": n_q - ok, "failure_statuses": {str(k): v for k, v in sorted(statuses.items())},
             "wall_s": wall,
             "latency_ms": {"p50": 1000 * float(np.percentile(lat, 50)), "p95": 1000 * float(np.percentile(lat, 95)),
                            "p99": 1000 * float(np.percentile(lat, 99))}}

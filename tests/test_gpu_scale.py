@@ -102,6 +102,29 @@ def test_c2_100m_whole_bench_batch_matches_oracle(c2):
     assert min(nonempty) >= per // 2, nonempty       # every template mostly returns rows
 
 
+def test_c2_100m_batches_to_host_repeated(c2):
+    """Back-to-back batches with host copies (engines on their own streams,
+    join outputs placed on the device, the packing's scratch freed only after
+    the engine waited for it): every batch's host copies equal its device
+    results and the first batch's rows."""
+    import vedas_gb300 as vg
+    g, ix, ox, cs = c2
+    qs = workloads.query_mix(g, 4096, seed=1, cs=cs)
+    first = None
+    for rep in range(4):
+        b = vg.Batch(ix, qs, to_host=True)
+        rows = b.rows()
+        if first is None:
+            first = rows
+        assert np.array_equal(rows, first), rep
+        for i in range(0, len(qs), 7):
+            if b.status(i) != 0:
+                continue
+            for x, y in zip(b.host_columns(i), b.columns(i)):
+                np.testing.assert_array_equal(x, y, err_msg=qs[i])
+        b.close()
+
+
 def _gpu_dedup(g):
     """Sorted set of the triples, deduplicated on the device (test input prep)."""
     import torch

@@ -85,3 +85,33 @@ def test_admission_rejects_over_budget_and_matches_oracle(ctx):
     srv.release(t)
     srv.stop()
     ix.close()
+
+
+def test_unreleased_results_hold_back_admission_without_stalling(ctx):
+    """Finished results count against the budget until released: with a
+    budget smaller than the results a client keeps, every query still
+    finishes (the queue head is admitted whenever nothing is in flight), and
+    releasing them lets the next ones in."""
+    import vedas_gb300 as vg
+    g = workloads.graph_chain(n=400_000, n_entities=40_000, seed=8)
+    qs = workloads.query_mix(g, 64, seed=11, mix={"S": 0.6, "C": 0.3, "F": 0.1})
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    ref = oracle_py.OracleIndex(g.s, g.p, g.o)
+    srv = vg.Server(ix, budget_bytes=1 << 20)        # 1 MiB: a few results fill it
+    tickets = srv.submit_many([q.encode() for q in qs])
+    for t in tickets:                                # nothing released while waiting
+        assert srv.wait(t, 60.0)
+    for q, t in zip(qs, tickets):
+        r = ref.query(q)
+        if r.status != 0 or srv.status(t) == 8:      # refused, or over the budget on its own
+            continue
+        assert srv.status(t) == 0, q
+        for a, b in zip(srv.columns(t), r.columns):
+            np.testing.assert_array_equal(a, b, err_msg=q)
+    for t in tickets:
+        srv.release(t)
+    t = srv.submit(qs[0])
+    assert srv.wait(t, 60.0)
+    srv.release(t)
+    srv.stop()
+    ix.close()

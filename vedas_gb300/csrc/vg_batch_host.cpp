@@ -564,7 +564,8 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     prof.device_s += since(t0);
   }
   // everything enqueued on the engine's stream so far is done (waited for
-  // now, or in stage B, with nothing enqueued since): held-back frees are safe
+  // now, or in stage B, which records ev_b_ whenever it enqueues work):
+  // held-back frees are safe
   if (own_stream_) ctx_.flush(defer_);
   if (tracing) tr.t_wait = since(trace_origin);
   {
@@ -757,6 +758,7 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   if (own_stream_) ctx_.flush(defer_);
   if (tracing) tr.t_wait = since(trace_origin);
   const uint64_t* ha = h_a_.data();
+  bool enqueued_b = false;   // device work enqueued by this stage (ev_b_ must cover it)
 
   // staged columns of the wave in flight
   {
@@ -802,7 +804,7 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
       std::vector<BatchQuery*> outs;
       for (PlannedQuery* q : final_) outs.push_back(q->out);
       ThreadExecScope es(enqueue_exec());
-      host_->add(outs);
+      enqueued_b = host_->add(outs);
     }
     final_.clear();
     fin_seg_.clear();
@@ -904,6 +906,12 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   } else {
     jsmall_.clear();
   }
+  // the result packing above was enqueued with its scratch held back: the
+  // next stage A waits for it before the held-back blocks are freed
+  if (enqueued_b && !b_pending_) {
+    VG_CUDA(cudaEventRecord(ev_b_, ctx_.stream));
+    b_pending_ = true;
+  }
   prof.device_s += since(t0);
   if (tracing) {
     tr.t_end = since(trace_origin);
@@ -913,8 +921,17 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
 }
 
 HostResults::~HostResults() {
-  finish();
-  for (Chunk& c : chunks_) ctx_.give_pinned(c.p, c.cap);
+  // a destructor reports nothing: an error of the copies (a context already
+  // failed) has been raised by the batch itself; the chunks are kept out of
+  // the pool then, since a copy into them may not have ended
+  bool ok = true;
+  try {
+    finish();
+  } catch (const std::exception&) {
+    ok = false;
+  }
+  if (ok)
+    for (Chunk& c : chunks_) ctx_.give_pinned(c.p, c.cap);
 }
 
 void HostResults::retire_stages(bool all) {
@@ -933,12 +950,12 @@ void HostResults::retire_stages(bool all) {
   pending_.swap(keep);
 }
 
-void HostResults::add(const std::vector<BatchQuery*>& qs) {
+bool HostResults::add(const std::vector<BatchQuery*>& qs) {
   std::lock_guard<std::mutex> lk(mu_);
   retire_stages(false);
   uint64_t words = 0;
   for (const BatchQuery* q : qs) words += q->rel.nrows * q->rel.ncols;
-  if (words == 0) return;
+  if (words == 0) return false;
   const size_t bytes = words * sizeof(uint32_t);
   const size_t span = (bytes + 255) / 256 * 256;   // what the chunk gives up (the next start stays aligned)
   if (chunks_.empty() || chunks_.back().used + span > chunks_.back().cap) {
@@ -970,6 +987,7 @@ void HostResults::add(const std::vector<BatchQuery*>& qs) {
   pending_.push_back({stage, done});
   ch.used += span;
   bytes_ += bytes;
+  return true;
 }
 
 void HostResults::finish() {

@@ -34,8 +34,10 @@ class HostResults {
   ~HostResults();
   HostResults(const HostResults&) = delete;
   HostResults& operator=(const HostResults&) = delete;
-  // Enqueues the copies of these queries' result columns.
-  void add(const std::vector<BatchQuery*>& qs);
+  // Enqueues the copies of these queries' result columns on the calling
+  // thread's stream (scratch freed through the thread's held-back frees);
+  // false when there was nothing to copy.
+  bool add(const std::vector<BatchQuery*>& qs);
   // Waits for every copy.
   void finish();
   uint64_t bytes() const { return bytes_; }

@@ -3,8 +3,11 @@
 // Clients submit query text from any thread; the query is planned on the
 // caller's thread (host work only) and queued.  One worker thread owns the
 // device: before every wave it admits queued queries, first come first
-// served, while the sum of their estimated relation bytes stays within the
-// budget; then it runs one wave for everything in flight, so queries that
+// served, while the sum of their estimated relation bytes and the bytes of
+// finished results not yet released stays within the budget (with nothing in
+// flight the head of the queue is admitted whenever its own estimate fits, so
+// a client holding results cannot stall the queue for good); then it runs one
+// wave for everything in flight, so queries that
 // arrived while others were on the GPU join them at the next wave boundary
 // and their work shares the same batched launches.  Finished queries release
 // their reservation and wake their waiters.  Results are read on a separate
@@ -31,6 +34,7 @@ struct ServeItem {
   PlannedQuery pq;
   BatchQuery q;
   Clock::time_point t_submit, t_admit, t_done;
+  uint64_t held = 0;   // device bytes of the finished result until release
   bool done = false;
 };
 
@@ -127,8 +131,10 @@ class Server {
       if (!f->second->done) fail(VG_ERR_INVALID, "query still running");
       it = std::move(f->second);
       items_.erase(f);
+      held_ -= it->held;
     }
     rel_free(ctx_, it->q.rel);
+    cv_work_.notify_all();   // admission may have waited for these bytes
   }
 
   void stats(uint64_t out[6]) {
@@ -159,6 +165,7 @@ class Server {
   std::unordered_map<uint64_t, std::unique_ptr<ServeItem>> items_;
   std::unordered_map<PlannedQuery*, ServeItem*> inflight_;
   uint64_t next_ticket_ = 0, submitted_ = 0, completed_ = 0, rejected_ = 0, reserved_ = 0, peak_inflight_ = 0;
+  uint64_t held_ = 0;   // bytes of finished results not yet released
   bool stop_ = false;
   vg_status worker_status_ = VG_OK;
 
@@ -167,6 +174,8 @@ class Server {
     if (f == items_.end()) fail(VG_ERR_INVALID, "unknown ticket");
     return f->second.get();
   }
+
+  static uint64_t result_bytes(const Rel& r) { return 4ull * r.nrows * r.ncols; }
 
   void finish_locked(ServeItem* it) {
     it->done = true;
@@ -181,7 +190,8 @@ class Server {
         cv_work_.wait(lk, [&] { return stop_ || !queue_.empty() || eng_.active() > 0; });
         if (stop_ && eng_.active() == 0) return;
         // admission at the wave boundary, first come first served
-        while (!queue_.empty() && reserved_ + queue_.front()->pq.est_bytes <= budget_) {
+        while (!queue_.empty() && (reserved_ + held_ + queue_.front()->pq.est_bytes <= budget_ ||
+                                   (eng_.active() == 0 && reserved_ == 0))) {
           ServeItem* it = queue_.front();
           queue_.pop_front();
           reserved_ += it->pq.est_bytes;
@@ -217,6 +227,8 @@ class Server {
         ServeItem* it = f->second;
         inflight_.erase(f);
         reserved_ -= it->pq.est_bytes;
+        it->held = it->q.status == VG_OK ? result_bytes(it->q.rel) : 0;
+        held_ += it->held;
         ++completed_;
         finish_locked(it);
       }
