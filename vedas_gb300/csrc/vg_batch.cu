@@ -246,7 +246,8 @@ struct JoinSeg {
 // One block per tile of kJcTile left keys of one join, tiles taken in ticket
 // order (the tile's join from a per-tile table, one load instead of a search
 // of the join starts).  The tile's match counts stay in registers (the
-// right-key window is staged by a bulk copy when it fits); their block scan
+// right-key window, found beforehand by jc_window_kernel, is staged by a bulk
+// copy when it fits); their block scan
 // and a segmented decoupled look-back over the join's earlier tiles give
 // every left key its output offset directly, and the join's last tile writes
 // its total.
@@ -287,11 +288,31 @@ __device__ __forceinline__ void count_small_join(const JoinSeg& g, uint32_t* __r
   if (lane == 31) *total = incl;
 }
 
+// Every tile's right-key window [win.x, win.y) (one warp per tile, both ends
+// at once), so that the counting blocks start their bulk copies at once
+// instead of each searching the right keys first.
+__global__ void __launch_bounds__(kJcBlock) jc_window_kernel(const JoinSeg* __restrict__ js,
+                                                             const uint64_t* __restrict__ bstart,
+                                                             const uint32_t* __restrict__ tile_join, uint64_t T,
+                                                             uint2* __restrict__ win) {
+  const uint64_t nw = static_cast<uint64_t>(gridDim.x) * (kJcBlock / 32);
+  for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * (kJcBlock / 32) + (threadIdx.x >> 5); t < T; t += nw) {
+    const uint32_t j = tile_join[t];
+    const uint64_t nl = js[j].nl;
+    const uint32_t* lk = js[j].lk;
+    const uint64_t i0 = (t - bstart[j]) * static_cast<uint64_t>(kJcTile);
+    const uint64_t i1 = (i0 + kJcTile < nl ? i0 + kJcTile : nl) - 1;
+    uint64_t w0, w1;
+    warp_window(js[j].rk, js[j].nr, lk[i0], lk[i1], w0, w1);
+    if ((threadIdx.x & 31) == 0) win[t] = make_uint2(static_cast<uint32_t>(w0), static_cast<uint32_t>(w1));
+  }
+}
+
 __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
     const JoinSeg* __restrict__ js, const uint64_t* __restrict__ bstart, const uint32_t* __restrict__ tile_join,
-    const uint32_t* __restrict__ small, uint32_t nsmall, uint32_t small_blocks, uint32_t* __restrict__ lo,
-    uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket, uint64_t* __restrict__ totals,
-    DeviceErrors* err) {
+    const uint2* __restrict__ win, const uint32_t* __restrict__ small, uint32_t nsmall, uint32_t small_blocks,
+    uint32_t* __restrict__ lo, uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket,
+    uint64_t* __restrict__ totals, DeviceErrors* err) {
   if (blockIdx.x < small_blocks) {   // block-uniform: this block only counts small joins
     const uint64_t sj = static_cast<uint64_t>(blockIdx.x) * (kJcBlock / 32) + (threadIdx.x >> 5);
     if (sj < nsmall) {
@@ -305,8 +326,13 @@ __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
   __shared__ uint64_t s_b;
   __shared__ uint32_t s_tile, s_j;
   if (threadIdx.x == 0) {
-    s_tile = atomicAdd(ticket, 1u);
-    s_j = tile_join[s_tile];
+    // the window is known: its bulk copy starts before the block's first barrier
+    const uint32_t t = atomicAdd(ticket, 1u);
+    const uint32_t jj = tile_join[t];
+    const uint2 w = win[t];
+    s_tile = t;
+    s_j = jj;
+    jc_issue_window(js[jj].rk, w.x, w.y, sm);
   }
   __syncthreads();
   const uint64_t tile = s_tile;
@@ -314,7 +340,7 @@ __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
   const JoinSeg g = js[j];
   const uint64_t i0 = (tile - bstart[j]) * static_cast<uint64_t>(kJcTile);
   uint32_t cnt[kJcKeys];
-  join_count_tile_regs(g.lk, g.nl, g.rk, g.nr, i0, lo + g.row0, cnt, sm, err);
+  jc_count_staged(g.lk, g.nl, g.rk, i0, lo + g.row0, cnt, sm, err);
   uint64_t sum = 0;
 #pragma unroll
   for (int k = 0; k < kJcKeys; ++k) sum += cnt[k];
@@ -804,11 +830,19 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
   uint64_t* status = ctx.alloc<uint64_t>(T);
   uint64_t* totals = ctx.alloc<uint64_t>(J);
   uint32_t* ticket = ctx.alloc<uint32_t>(1);
+  uint2* dwin = ctx.alloc<uint2>(T ? T : 1);
   VG_CUDA(cudaMemsetAsync(status, 0, T * sizeof(uint64_t), ctx.stream));
   VG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), ctx.stream));
+  if (T) {
+    const uint64_t wblocks = std::min<uint64_t>(div_up(T, kJcBlock / 32), static_cast<uint64_t>(ctx.num_sms) * 8);
+    ctx.launch("join_windows", 8.0 * T, [&] {
+      jc_window_kernel<<<static_cast<unsigned>(wblocks), kJcBlock, 0, ctx.stream>>>(djs, dbs, dtj, T, dwin);
+    });
+    VG_CUDA(cudaGetLastError());
+  }
   ctx.launch("join_count_scan", cbytes + 12.0 * rows, [&] {
     bjoin_count_scan_kernel<<<static_cast<unsigned>(small_blocks + T), kJcBlock, 0, ctx.stream>>>(
-        djs, dbs, dtj, dsm, nsmall, small_blocks, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);
+        djs, dbs, dtj, dwin, dsm, nsmall, small_blocks, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
   VG_CUDA(cudaMemcpyAsync(totals_host, totals, J * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
@@ -816,6 +850,7 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
   // the stream orders every later use of these blocks after the kernel above
   ctx.free(status);
   ctx.free(ticket);
+  ctx.free(dwin);
   ctx.free(djs);
   ctx.free(dbs);
   ctx.free(dtj);

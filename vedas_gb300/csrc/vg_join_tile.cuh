@@ -95,6 +95,49 @@ __device__ __forceinline__ uint64_t warp_bound(const T* __restrict__ R, uint64_t
   return lo + __popc(__ballot_sync(0xffffffffu, below));
 }
 
+// A tile's right-key window by one warp: the lower bound of klo (lanes 0-15)
+// and the upper bound of khi (lanes 16-31) in R[0, nr), both at once.  Each
+// round every half-warp probes 15 evenly spaced keys of its range and the
+// ballot of its comparisons narrows the range 16-fold.  Every lane of the
+// warp must call it with the same arguments; every lane gets both bounds.
+__device__ __forceinline__ void warp_window(const uint32_t* __restrict__ R, uint64_t nr, uint32_t klo,
+                                            uint32_t khi, uint64_t& w0, uint64_t& w1) {
+  const uint32_t lane = threadIdx.x & 31, sl = lane & 15;
+  const bool upper = lane >= 16;
+  const uint32_t half = upper ? 0xffff0000u : 0x0000ffffu;
+  const uint32_t key = upper ? khi : klo;
+  uint64_t lo = 0, hi = nr;
+  while (true) {
+    const bool wide = hi - lo > 16;
+    if (__ballot_sync(0xffffffffu, wide) == 0) break;
+    uint64_t step = 0;
+    bool below = false;
+    if (wide) {
+      step = (hi - lo + 15) >> 4;
+      const uint64_t p = lo + static_cast<uint64_t>(sl + 1) * step;
+      if (sl < 15 && p < hi) {
+        const uint32_t a = __ldg(R + p);
+        below = upper ? (a <= key) : (a < key);
+      }
+    }
+    const uint32_t c = __popc(__ballot_sync(0xffffffffu, below) & half);
+    if (wide) {
+      const uint64_t nlo = c ? lo + static_cast<uint64_t>(c) * step + 1 : lo;
+      const uint64_t cap = lo + static_cast<uint64_t>(c + 1) * step;
+      hi = cap < hi ? cap : hi;
+      lo = nlo;
+    }
+  }
+  bool below = false;
+  if (lo + sl < hi) {
+    const uint32_t a = __ldg(R + lo + sl);
+    below = upper ? (a <= key) : (a < key);
+  }
+  const uint64_t res = lo + __popc(__ballot_sync(0xffffffffu, below) & half);
+  w0 = __shfl_sync(0xffffffffu, res, 0);
+  w1 = __shfl_sync(0xffffffffu, res, 16);
+}
+
 // Lower and upper bounds of K keys in R[w0, w1) at once: branchless binary
 // searches advanced in lockstep, so each round has 2K independent loads in
 // flight instead of one dependent chain per key.
@@ -178,6 +221,16 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
   const uint64_t w0 = sm.w0, w1 = sm.w1 > sm.w0 ? sm.w1 : sm.w0;
   const uint32_t staged = sm.staged;
   const uint64_t base = ((w0 + mis) & ~3ull) - mis;
+  // the thread's left keys are loaded while the window's bulk copy is in flight
+  const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
+  uint32_t key[kJcKeys];
+  if (first < i_end) {
+#pragma unroll
+    for (int j = 0; j < kJcKeys; ++j) {
+      const uint64_t i = first + j;
+      key[j] = L[i < i_end ? i : i_end - 1];
+    }
+  }
   if (staged) {
     const uint64_t a0 = (staged == 2) ? ((w0 + mis + 3) & ~3ull) - mis : w1;
     const uint64_t a1 = (staged == 2) ? ((w1 + mis) & ~3ull) - mis : w1;
@@ -193,17 +246,10 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
   }
   __syncthreads();
   const bool use_smem = staged != 0 && sm.failed == 0;
-  const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
   if (first >= i_end) return;   // counts stay zero
 
   if (!use_smem) {
-    uint32_t key[kJcKeys];
     uint64_t lo[kJcKeys], hi[kJcKeys];
-#pragma unroll
-    for (int j = 0; j < kJcKeys; ++j) {
-      const uint64_t i = first + j;
-      key[j] = L[i < i_end ? i : i_end - 1];
-    }
     lockstep_bounds<kJcKeys>(R, w0, w1, key, lo, hi);
 #pragma unroll
     for (int j = 0; j < kJcKeys; ++j) {
@@ -224,20 +270,20 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
   for (int j = 0; j < kJcKeys; ++j) {
     const uint64_t i = first + j;
     if (i < i_end) {
-      const uint32_t key = L[i];
+      const uint32_t k = key[j];
       uint32_t lo, hi;
-      if (j > 0 && key == pkey) {
+      if (j > 0 && k == pkey) {
         lo = plo;
         hi = phi;
       } else {
-        lo = (j == 0) ? smem_search<false>(win, 0, n, key) : smem_gallop<false>(win, phi, n, key);
-        hi = smem_gallop<true>(win, lo, n, key);
+        lo = (j == 0) ? smem_search<false>(win, 0, n, k) : smem_gallop<false>(win, phi, n, k);
+        hi = smem_gallop<true>(win, lo, n, k);
       }
       lo_out[i] = static_cast<uint32_t>(w0 + lo);
       cnt[j] = hi - lo;
       plo = lo;
       phi = hi;
-      pkey = key;
+      pkey = k;
     }
   }
 }
