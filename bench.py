@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--serve-pool", type=int, default=20000, help="serve: distinct queries drawn from")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: relation memory budget")
+    ap.add_argument("--queue-limit-ms", type=float, default=0.0,
+                    help="serve: refuse queries that waited longer in the queue (0: no limit)")
     ap.add_argument("--triples", type=int, default=None,
                     help="graph size (default: 100M; 500M for --mode c3 and serve)")
     ap.add_argument("--entities", type=int, default=None,
@@ -739,7 +741,7 @@ def bench_serve(args, rank, world, local, pg):
     ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
     ix = vg.Index(ctx, g.s, g.p, g.o)
     del g, cs
-    srv = vg.Server(ix, budget_bytes=int(args.budget_gb * (1 << 30)))
+    srv = vg.Server(ix, budget_bytes=int(args.budget_gb * (1 << 30)), queue_limit_s=args.queue_limit_ms / 1000.0)
     for t in srv.submit_many(qb[:256]):     # warm-up: first waves, host mirrors
         srv.wait(t)
         srv.release(t)
@@ -763,6 +765,7 @@ def bench_serve(args, rank, world, local, pg):
                                    f"{args.clients} client threads, 60/30/10 star/chain/snowflake templates, on "
                                    f"the {triples_label(args.triples)}-triple hub graph",
                        "budget_gb": args.budget_gb, "query_pool": len(pool), "clients": args.clients,
+                       "queue_limit_ms": args.queue_limit_ms or None,
                        "waves": stats["waves"], "peak_inflight": stats["peak_inflight"]},
             "latency_ms": head["latency_ms"],
             "offered_rate": rates[0],

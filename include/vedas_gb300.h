@@ -372,13 +372,15 @@ vg_status vg_selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookup
 /* ---- serving (continuous batching) -------------------------------------- */
 typedef struct vg_server vg_server;
 
-/* Starts a serving loop on the context: one worker thread owns the device.
+/* Starts a serving loop on the context: VG_BATCH_ENGINES wave engines
+ * (default 4), each with a worker thread and a stream of its own.
  * Submitted queries are planned on the caller's thread, then admitted first
- * come first served at wave boundaries while the sum of their estimated
- * relation bytes stays within `budget_bytes`; admitted queries share the
- * batched launches of every wave until they finish.  Replaces vdQuery's REPL
- * loop (src/VedasQuery.cu:136-205), which runs one query at a time.
- * Only vg_serve_* calls may use the context while the server runs. */
+ * come first served at the engines' wave boundaries while the estimated
+ * relation bytes of the queries in flight plus the bytes of finished results
+ * not yet released stay within `budget_bytes`; admitted queries share the
+ * batched launches of their engine's waves until they finish.  Replaces
+ * vdQuery's REPL loop (src/VedasQuery.cu:136-205), which runs one query at a
+ * time.  Only vg_serve_* calls may use the context while the server runs. */
 vg_status vg_serve_start(vg_ctx* ctx, vg_index* ix, size_t budget_bytes, vg_server** out);
 /* Queues one query; `ticket` identifies it.  A query whose estimate alone
  * exceeds the budget finishes at once with VG_ERR_REJECTED. */
@@ -398,6 +400,10 @@ vg_status vg_serve_download(vg_server* s, uint64_t ticket, uint32_t c, uint32_t*
 vg_status vg_serve_latency(vg_server* s, uint64_t ticket, double* queued_s, double* total_s);
 /* Frees a finished query's result. */
 vg_status vg_serve_release(vg_server* s, uint64_t ticket);
+/* Load shedding (no reference counterpart): queries that waited more than
+ * `seconds` in the queue finish with VG_ERR_REJECTED instead of being
+ * admitted; 0 (the default) admits every query however long it waited. */
+vg_status vg_serve_set_queue_limit(vg_server* s, double seconds);
 /* out6 = {submitted, completed, rejected, waves, reserved bytes, peak queries in flight}. */
 vg_status vg_serve_stats(vg_server* s, uint64_t out6[6]);
 /* Lets the queries in flight finish, then stops the worker. */

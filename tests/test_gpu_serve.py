@@ -115,3 +115,31 @@ def test_unreleased_results_hold_back_admission_without_stalling(ctx):
     srv.release(t)
     srv.stop()
     ix.close()
+
+
+def test_queue_limit_refuses_queries_that_waited_too_long(ctx):
+    """Load shedding: with a small budget only a few queries run at a time,
+    and those that waited in the queue longer than the limit are refused
+    (VG_ERR_REJECTED); the admitted ones still match the oracle."""
+    import vedas_gb300 as vg
+    g = workloads.graph_chain(n=400_000, n_entities=40_000, seed=8)
+    qs = workloads.query_mix(g, 400, seed=12, mix={"S": 0.6, "C": 0.3, "F": 0.1})
+    ix = vg.Index(ctx, g.s, g.p, g.o)
+    ref = oracle_py.OracleIndex(g.s, g.p, g.o)
+    srv = vg.Server(ix, budget_bytes=1 << 20, queue_limit_s=0.002)
+    tickets = srv.submit_many([q.encode() for q in qs])
+    ok = shed = 0
+    for q, t in zip(qs, tickets):
+        assert srv.wait(t, 60.0)
+        st = srv.status(t)
+        if st == 0:
+            ok += 1
+            r = ref.query(q)
+            for a, b in zip(srv.columns(t), r.columns):
+                np.testing.assert_array_equal(a, b, err_msg=q)
+        elif st == 8:
+            shed += 1
+        srv.release(t)
+    assert ok > 0 and shed > 0, (ok, shed)
+    srv.stop()
+    ix.close()

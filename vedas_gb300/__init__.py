@@ -145,6 +145,7 @@ def lib():
             "vg_serve_latency": (i32, [vp, u64, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double)]),
             "vg_serve_release": (i32, [vp, u64]),
+            "vg_serve_set_queue_limit": (i32, [vp, ctypes.c_double]),
             "vg_serve_stats": (i32, [vp, ctypes.POINTER(u64)]),
             "vg_serve_stop": (i32, [vp]),
         }
@@ -471,10 +472,17 @@ class Batch:
 class Server:
     """Continuous-batching serving loop (vg_serve_*)."""
 
-    def __init__(self, ix: "Index", budget_bytes: int):
+    def __init__(self, ix: "Index", budget_bytes: int, queue_limit_s: float = 0.0):
         h = ctypes.c_void_p()
         check(lib().vg_serve_start(ix.ctx.h, ix.h, budget_bytes, ctypes.byref(h)))
         self.h = h
+        if queue_limit_s:
+            self.set_queue_limit(queue_limit_s)
+
+    def set_queue_limit(self, seconds: float) -> None:
+        """Queries that waited more than `seconds` in the queue are refused
+        (status VG_ERR_REJECTED); 0 admits every query."""
+        check(lib().vg_serve_set_queue_limit(self.h, ctypes.c_double(seconds)))
 
     def submit(self, sparql: str) -> int:
         t = ctypes.c_uint64()

@@ -339,13 +339,13 @@ __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
   const uint32_t j = s_j;
   const JoinSeg g = js[j];
   const uint64_t i0 = (tile - bstart[j]) * static_cast<uint64_t>(kJcTile);
-  uint32_t cnt[kJcKeys];
-  jc_count_staged(g.lk, g.nl, g.rk, i0, lo + g.row0, cnt, sm, err);
+  uint32_t cnt[kJcKeys], lov[kJcKeys];
+  jc_count_staged(g.lk, g.nl, g.rk, i0, lov, cnt, sm, err);
   uint64_t sum = 0;
 #pragma unroll
   for (int k = 0; k < kJcKeys; ++k) sum += cnt[k];
   uint64_t tot;
-  const uint64_t e = block_excl_scan64<kJcBlock>(sum, tot, s_scan);
+  const uint64_t e = block_excl_scan64<kJcBlock>(sum, tot, s_scan);   // every thread is past its search
   if (threadIdx.x < 32) {
     const uint64_t p = warp_lookback_seg(status, tile, bstart[j], tot, err);
     if (threadIdx.x == 0) s_b = p;
@@ -353,13 +353,38 @@ __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
   __syncthreads();
   if (tile == bstart[j + 1] - 1 && threadIdx.x == 0) totals[j] = s_b + tot;
   uint64_t run = s_b + e;
-  const uint64_t first = i0 + static_cast<uint64_t>(threadIdx.x) * kJcKeys;
+  const uint32_t tid = threadIdx.x;
+  const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
+  const uint32_t tile_n = static_cast<uint32_t>(g.nl - i0 < kJcTile ? g.nl - i0 : kJcTile);
+  if (sm.staged == 2 && sm.failed) {
+    // a bulk copy that gave up may still land in the window: no staging there
+#pragma unroll
+    for (int k = 0; k < kJcKeys; ++k) {
+      if (first + k < g.nl) {
+        offs[g.row0 + first + k] = run;
+        lo[g.row0 + first + k] = lov[k];
+      }
+      run += cnt[k];
+    }
+    if (tid == 0) jc_drain_window(sm, err);
+    return;
+  }
+  uint32_t* s_lo = jc_stage_lo(sm);
+  uint64_t* s_off = jc_stage_off(sm);
 #pragma unroll
   for (int k = 0; k < kJcKeys; ++k) {
-    if (first + k < g.nl) offs[g.row0 + first + k] = run;
+    const uint32_t q = tid * kJcKeys + k;
+    s_lo[q + q / 32] = lov[k];
+    s_off[q + q / 16] = run;
     run += cnt[k];
   }
-  if (threadIdx.x == 0) jc_drain_window(sm, err);
+  __syncthreads();
+  uint32_t* lo_t = lo + g.row0 + i0;
+  uint64_t* off_t = offs + g.row0 + i0;
+  for (uint32_t q = tid; q < tile_n; q += kJcBlock) {
+    lo_t[q] = s_lo[q + q / 32];
+    off_t[q] = s_off[q + q / 16];
+  }
 }
 
 struct JoinOut {
@@ -426,9 +451,31 @@ __device__ __forceinline__ void write_small_join(const JoinOut* __restrict__ src
   __syncwarp();   // the slice is free for the warp's next join
 }
 
+// Every output tile's left rows [x, y): x the last row whose output starts
+// at or before the tile's first row, y the first row whose output starts
+// after its last (one warp per tile, both searches at once), so that the
+// writing blocks start staging at once.  T as for bjoin_write_kernel.
+__global__ void __launch_bounds__(kBlock) jw_range_kernel(const JoinOut* __restrict__ jo,
+                                                          const uint64_t* __restrict__ ostart,
+                                                          const uint32_t* __restrict__ tile_join, uint64_t T_host,
+                                                          const uint64_t* ostart_end, uint2* __restrict__ ranges) {
+  const uint64_t T = ostart_end ? *ostart_end : T_host;
+  const uint64_t nw = static_cast<uint64_t>(gridDim.x) * (kBlock / 32);
+  for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5); t < T; t += nw) {
+    const uint32_t jn = tile_join[t];
+    const uint64_t total = jo[jn].total, nl = jo[jn].nl;
+    const uint64_t kb = (t - ostart[jn]) * static_cast<uint64_t>(kTileRows);
+    const uint64_t kend = (kb + kTileRows < total) ? kb + kTileRows : total;
+    uint64_t a, b;
+    warp_bound_pair<true, true, uint64_t>(jo[jn].offs, nl, kb, kend - 1, a, b);
+    if ((threadIdx.x & 31) == 0) ranges[t] = make_uint2(static_cast<uint32_t>(a - 1), static_cast<uint32_t>(b));
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __restrict__ jo,
                                                              const uint64_t* __restrict__ ostart,
                                                              const uint32_t* __restrict__ tile_join,
+                                                             const uint2* __restrict__ ranges,
                                                              uint64_t T_host, const uint64_t* ostart_end,
                                                              const uint32_t* __restrict__ small, uint32_t nsmall_host,
                                                              const uint32_t* nsmall_dev) {
@@ -438,7 +485,6 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
   __shared__ JoinOut s_w[kBlock / 32];
   __shared__ uint64_t s_off[kStage];
   __shared__ uint32_t s_lo[kStage];
-  __shared__ uint64_t s_i[2];
   {
     const uint32_t nsm = nsmall_dev ? *nsmall_dev : nsmall_host;
     const uint32_t warp = threadIdx.x >> 5, nwarps = kBlock / 32;
@@ -451,23 +497,17 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
   for (uint64_t tile = blockIdx.x; tile < T; tile += gridDim.x) {
     __syncthreads();   // the previous tile's readers of the shared arrays are done
     const uint32_t jn = tile_join[tile];
+    const uint2 rg = ranges[tile];
+    const uint64_t tile0 = ostart[jn];
     {
       const uint32_t* src = reinterpret_cast<const uint32_t*>(&jo[jn]);
       uint32_t* dst = reinterpret_cast<uint32_t*>(&s_o);
       for (uint32_t w = threadIdx.x; w < sizeof(JoinOut) / 4; w += kBlock) dst[w] = src[w];
     }
     __syncthreads();
-    const uint64_t kb = (tile - ostart[jn]) * static_cast<uint64_t>(kTileRows);
+    const uint64_t kb = (tile - tile0) * static_cast<uint64_t>(kTileRows);
     const uint64_t kend = (kb + kTileRows < s_o.total) ? kb + kTileRows : s_o.total;
-    if (threadIdx.x < 32) {
-      const uint64_t f = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kb) - 1;
-      if (threadIdx.x == 0) s_i[0] = f;
-    } else if (threadIdx.x < 64) {
-      const uint64_t e = warp_bound<true, uint64_t>(s_o.offs, 0, s_o.nl, kend - 1);
-      if (threadIdx.x == 32) s_i[1] = e;
-    }
-    __syncthreads();
-    const uint64_t ib = s_i[0], ie = s_i[1];
+    const uint64_t ib = rg.x, ie = rg.y;
     const uint64_t m = ie - ib;
     const bool staged = m <= static_cast<uint64_t>(kStage);
     if (staged)
@@ -906,11 +946,23 @@ void batched_join_write(Ctx& ctx, JoinBatch& jb, const uint64_t* totals, std::ve
     uint64_t* dos = upload(ctx, ostart);
     uint32_t* dtj = upload(ctx, tile_join);
     uint32_t* dsm = upload(ctx, small);
+    uint2* drg = ctx.alloc<uint2>(ostart[J] ? ostart[J] : 1);
+    if (ostart[J]) {
+      const uint64_t rblocks =
+          std::min<uint64_t>(div_up(ostart[J], kBlock / 32), static_cast<uint64_t>(ctx.num_sms) * 8);
+      ctx.launch("join_write_ranges", 8.0 * ostart[J], [&] {
+        jw_range_kernel<<<static_cast<unsigned>(rblocks), kBlock, 0, ctx.stream>>>(djo, dos, dtj, ostart[J], nullptr,
+                                                                                   drg);
+      });
+      VG_CUDA(cudaGetLastError());
+    }
     const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(ostart[J], small_blocks));
     ctx.launch("join_write", wbytes, [&] {
-      bjoin_write_kernel<<<grid, kBlock, 0, ctx.stream>>>(djo, dos, dtj, ostart[J], nullptr, dsm, nsmall, nullptr);
+      bjoin_write_kernel<<<grid, kBlock, 0, ctx.stream>>>(djo, dos, dtj, drg, ostart[J], nullptr, dsm, nsmall,
+                                                          nullptr);
     });
     VG_CUDA(cudaGetLastError());
+    ctx.free(drg);
     ctx.free(dos);
     ctx.free(dtj);
     ctx.free(dsm);
@@ -990,11 +1042,17 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
   const unsigned jgrid = static_cast<unsigned>(std::min<uint64_t>(J, static_cast<uint64_t>(ctx.num_sms) * 8));
   ctx.launch("join_tile_map", 0.0, [&] { tile_join_fill_kernel<<<jgrid, 128, 0, ctx.stream>>>(dos, J, dtj); });
   VG_CUDA(cudaGetLastError());
-  // the tile count is on the device: a fixed grid loops over the tiles (the
+  // the tile count is on the device: fixed grids loop over the tiles (the
   // algorithmic bytes are added when the host reads the totals)
+  uint2* drg = ctx.alloc<uint2>(tile_cap);
+  ctx.launch("join_write_ranges", 0.0, [&] {
+    jw_range_kernel<<<static_cast<unsigned>(ctx.num_sms) * 8, kBlock, 0, ctx.stream>>>(djo, dos, dtj, 0, dos + J,
+                                                                                       drg);
+  });
+  VG_CUDA(cudaGetLastError());
   ctx.launch("join_write", 0.0, [&] {
     bjoin_write_kernel<<<static_cast<unsigned>(ctx.num_sms) * ctx.tune.write_blocks_per_sm, kBlock, 0,
-                         ctx.stream>>>(djo, dos, dtj, 0, dos + J, dsm, 0, dsm + J);
+                         ctx.stream>>>(djo, dos, dtj, drg, 0, dos + J, dsm, 0, dsm + J);
   });
   VG_CUDA(cudaGetLastError());
   ctx.launch("join_first_last", 8.0 * J, [&] {
@@ -1016,6 +1074,7 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
   ctx.free(dos);
   ctx.free(dsm);
   ctx.free(dtj);
+  ctx.free(drg);
   ctx.free(dfl);
   ctx.free(dstage);
 }

@@ -1094,6 +1094,11 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
 
 void parallel_for(size_t n, const std::function<void(size_t)>& f) { WorkerPool::get().run(n, f); }
 
+void run_on_engine_pool(size_t e, const std::function<void()>& f) {
+  UseEnginePool use(e);
+  f();
+}
+
 size_t join_region_bytes(const Ctx& ctx, size_t engines) {
   // VG_JOIN_REGION_MB per engine (default 4096; 0 turns device-side placement
   // off), at most an eighth of the arena shared by the engines

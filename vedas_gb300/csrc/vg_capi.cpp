@@ -436,6 +436,8 @@ struct TuneKnob {
 };
 const TuneKnob kKnobs[] = {
     {"sort_items", &vg::TuneParams::sort_items, 8, 16},
+    {"sort_ballot", &vg::TuneParams::sort_ballot, 0, 1},
+    {"sort_lookback", &vg::TuneParams::sort_lookback, 1, 4},
     {"join_small_rows", &vg::TuneParams::join_small_rows, 0, 256},
     {"write_small_rows", &vg::TuneParams::write_small_rows, 0, 4096},
     {"unique_small_rows", &vg::TuneParams::unique_small_rows, 0, 256},
@@ -883,6 +885,11 @@ vg_status vg_serve_latency(vg_server* s, uint64_t ticket, double* queued_s, doub
 vg_status vg_serve_release(vg_server* s, uint64_t ticket) {
   if (!s) return VG_ERR_INVALID;
   return guard([&] { s->srv->release(ticket); });
+}
+
+vg_status vg_serve_set_queue_limit(vg_server* s, double seconds) {
+  if (!s || !(seconds >= 0)) return VG_ERR_INVALID;
+  return guard([&] { s->srv->set_queue_limit(seconds); });
 }
 
 vg_status vg_serve_stats(vg_server* s, uint64_t out6[6]) {

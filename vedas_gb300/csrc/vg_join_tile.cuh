@@ -95,18 +95,21 @@ __device__ __forceinline__ uint64_t warp_bound(const T* __restrict__ R, uint64_t
   return lo + __popc(__ballot_sync(0xffffffffu, below));
 }
 
-// A tile's right-key window by one warp: the lower bound of klo (lanes 0-15)
-// and the upper bound of khi (lanes 16-31) in R[0, nr), both at once.  Each
-// round every half-warp probes 15 evenly spaced keys of its range and the
-// ballot of its comparisons narrows the range 16-fold.  Every lane of the
-// warp must call it with the same arguments; every lane gets both bounds.
-__device__ __forceinline__ void warp_window(const uint32_t* __restrict__ R, uint64_t nr, uint32_t klo,
-                                            uint32_t khi, uint64_t& w0, uint64_t& w1) {
+// Two bounds in R[0, n) by one warp at once: lanes 0-15 find the first
+// index whose key is above ka (kUpperA) or not below it, lanes 16-31 the
+// same for kb (kUpperB).  Each round every half-warp probes 15 evenly spaced
+// keys of its range and the ballot of its comparisons narrows the range
+// 16-fold.  Every lane of the warp must call it with the same arguments;
+// every lane gets both bounds.
+template <bool kUpperA, bool kUpperB, typename T>
+__device__ __forceinline__ void warp_bound_pair(const T* __restrict__ R, uint64_t n, T ka, T kb, uint64_t& ra,
+                                                uint64_t& rb) {
   const uint32_t lane = threadIdx.x & 31, sl = lane & 15;
-  const bool upper = lane >= 16;
-  const uint32_t half = upper ? 0xffff0000u : 0x0000ffffu;
-  const uint32_t key = upper ? khi : klo;
-  uint64_t lo = 0, hi = nr;
+  const bool second = lane >= 16;
+  const bool upper = second ? kUpperB : kUpperA;
+  const uint32_t half = second ? 0xffff0000u : 0x0000ffffu;
+  const T key = second ? kb : ka;
+  uint64_t lo = 0, hi = n;
   while (true) {
     const bool wide = hi - lo > 16;
     if (__ballot_sync(0xffffffffu, wide) == 0) break;
@@ -116,7 +119,7 @@ __device__ __forceinline__ void warp_window(const uint32_t* __restrict__ R, uint
       step = (hi - lo + 15) >> 4;
       const uint64_t p = lo + static_cast<uint64_t>(sl + 1) * step;
       if (sl < 15 && p < hi) {
-        const uint32_t a = __ldg(R + p);
+        const T a = __ldg(R + p);
         below = upper ? (a <= key) : (a < key);
       }
     }
@@ -130,12 +133,19 @@ __device__ __forceinline__ void warp_window(const uint32_t* __restrict__ R, uint
   }
   bool below = false;
   if (lo + sl < hi) {
-    const uint32_t a = __ldg(R + lo + sl);
+    const T a = __ldg(R + lo + sl);
     below = upper ? (a <= key) : (a < key);
   }
   const uint64_t res = lo + __popc(__ballot_sync(0xffffffffu, below) & half);
-  w0 = __shfl_sync(0xffffffffu, res, 0);
-  w1 = __shfl_sync(0xffffffffu, res, 16);
+  ra = __shfl_sync(0xffffffffu, res, 0);
+  rb = __shfl_sync(0xffffffffu, res, 16);
+}
+
+// A tile's right-key window: the lower bound of klo and the upper bound of
+// khi in R[0, nr), by one warp.
+__device__ __forceinline__ void warp_window(const uint32_t* __restrict__ R, uint64_t nr, uint32_t klo,
+                                            uint32_t khi, uint64_t& w0, uint64_t& w1) {
+  warp_bound_pair<false, true, uint32_t>(R, nr, klo, khi, w0, w1);
 }
 
 // Lower and upper bounds of K keys in R[w0, w1) at once: branchless binary
@@ -207,14 +217,14 @@ __device__ __forceinline__ void jc_issue_window(const uint32_t* __restrict__ R, 
 // fit (a heavy key, or a right side much longer than the left) is searched in
 // global memory with lockstep bounds instead.
 // The tile's counts stay in registers: thread t holds the counts of left
-// keys i0 + 8t .. i0 + 8t + 7 in cnt[] (zero past the end); lower bounds go
-// to lo_out.  Every thread of the block must call it.
+// keys i0 + 8t .. i0 + 8t + 7 in cnt[] and their lower bounds in lov[] (zero
+// past the end).  Every thread of the block must call it.
 __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, uint64_t nl,
                                                 const uint32_t* __restrict__ R, uint64_t i0,
-                                                uint32_t* __restrict__ lo_out, uint32_t (&cnt)[kJcKeys],
+                                                uint32_t (&lov)[kJcKeys], uint32_t (&cnt)[kJcKeys],
                                                 JoinCountSmem& sm, DeviceErrors* err) {
 #pragma unroll
-  for (int j = 0; j < kJcKeys; ++j) cnt[j] = 0;
+  for (int j = 0; j < kJcKeys; ++j) cnt[j] = lov[j] = 0;
   const uint32_t tid = threadIdx.x;
   const uint64_t i_end = (i0 + kJcTile < nl) ? i0 + kJcTile : nl;
   const uint64_t mis = (reinterpret_cast<uintptr_t>(R) >> 2) & 3u;
@@ -224,13 +234,20 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
   // the thread's left keys are loaded while the window's bulk copy is in flight
   const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
   uint32_t key[kJcKeys];
-  if (first < i_end) {
+  if (first + kJcKeys <= i_end && (reinterpret_cast<uintptr_t>(L + first) & 15u) == 0) {
+    // two 16-byte loads (the thread's keys are consecutive)
+    const uint4 a = *reinterpret_cast<const uint4*>(L + first);
+    const uint4 b = *reinterpret_cast<const uint4*>(L + first + 4);
+    key[0] = a.x, key[1] = a.y, key[2] = a.z, key[3] = a.w;
+    key[4] = b.x, key[5] = b.y, key[6] = b.z, key[7] = b.w;
+  } else if (first < i_end) {
 #pragma unroll
     for (int j = 0; j < kJcKeys; ++j) {
       const uint64_t i = first + j;
       key[j] = L[i < i_end ? i : i_end - 1];
     }
   }
+  static_assert(kJcKeys == 8, "the vector loads above take 8 keys");
   if (staged) {
     const uint64_t a0 = (staged == 2) ? ((w0 + mis + 3) & ~3ull) - mis : w1;
     const uint64_t a1 = (staged == 2) ? ((w1 + mis) & ~3ull) - mis : w1;
@@ -255,7 +272,7 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
     for (int j = 0; j < kJcKeys; ++j) {
       const uint64_t i = first + j;
       if (i < i_end) {
-        lo_out[i] = static_cast<uint32_t>(lo[j]);
+        lov[j] = static_cast<uint32_t>(lo[j]);
         cnt[j] = static_cast<uint32_t>(hi[j] - lo[j]);
       }
     }
@@ -279,7 +296,7 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
         lo = (j == 0) ? smem_search<false>(win, 0, n, k) : smem_gallop<false>(win, phi, n, k);
         hi = smem_gallop<true>(win, lo, n, k);
       }
-      lo_out[i] = static_cast<uint32_t>(w0 + lo);
+      lov[j] = static_cast<uint32_t>(w0 + lo);
       cnt[j] = hi - lo;
       plo = lo;
       phi = hi;
@@ -287,6 +304,19 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
     }
   }
 }
+
+// A tile's lower bounds and output offsets, staged in the window's shared
+// memory after the search so that they leave in coalesced stores: element e
+// of the tile (thread e / 8's key e % 8) sits at e + e / 32 (lower bounds,
+// 32-bit) and at e + e / 16 of the 64-bit area (offsets), which keeps both
+// the per-thread writes and the row-order reads free of bank conflicts.
+constexpr uint32_t kJcStageLoWords = kJcTile + kJcTile / 32;
+__device__ __forceinline__ uint32_t* jc_stage_lo(JoinCountSmem& sm) { return sm.keys; }
+__device__ __forceinline__ uint64_t* jc_stage_off(JoinCountSmem& sm) {
+  return reinterpret_cast<uint64_t*>(sm.keys + kJcStageLoWords);
+}
+static_assert(kJcStageLoWords % 2 == 0, "the 64-bit staging area starts 8-byte aligned");
+static_assert(kJcStageLoWords + 2 * (kJcTile + kJcTile / 16) <= kJcWindow, "staging fits in the window");
 
 // Called by one thread after the block's last use of the window: a bulk copy
 // whose wait gave up may still be in flight into this block's shared memory,
@@ -320,7 +350,12 @@ __device__ __forceinline__ void join_count_tile_regs(const uint32_t* __restrict_
   __syncthreads();
   if (tid == 0) jc_issue_window(R, sm.w0, sm.w1, sm);
   __syncthreads();
-  jc_count_staged(L, nl, R, i0, lo_out, cnt, sm, err);
+  uint32_t lov[kJcKeys];
+  jc_count_staged(L, nl, R, i0, lov, cnt, sm, err);
+  const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
+#pragma unroll
+  for (int j = 0; j < kJcKeys; ++j)
+    if (first + j < nl) lo_out[first + j] = lov[j];
 }
 
 // Lower bound and match count of every left key of the tile, to lo_out and

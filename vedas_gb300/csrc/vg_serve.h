@@ -1,17 +1,22 @@
-// Serving loop: continuous batching over the wave engine.
+// Serving loop: continuous batching over wave engines.
 //
 // Clients submit query text from any thread; the query is planned on the
-// caller's thread (host work only) and queued.  One worker thread owns the
-// device: before every wave it admits queued queries, first come first
-// served, while the sum of their estimated relation bytes and the bytes of
-// finished results not yet released stays within the budget (with nothing in
-// flight the head of the queue is admitted whenever its own estimate fits, so
-// a client holding results cannot stall the queue for good); then it runs one
-// wave for everything in flight, so queries that
-// arrived while others were on the GPU join them at the next wave boundary
-// and their work shares the same batched launches.  Finished queries release
+// caller's thread (host work only) and queued.  Each of the server's wave
+// engines (VG_BATCH_ENGINES, default 4) has a worker thread, a stream and a
+// join-output region of its own.  Before each of its waves a worker admits
+// queued queries into its engine, first come first served, while the sum of
+// the estimated relation bytes of every query in flight and the bytes of
+// finished results not yet released stays within the budget (with nothing
+// in flight anywhere the head of the queue is admitted whenever its own
+// estimate fits, so a client holding results cannot stall the queue for
+// good); then it runs one wave for everything its engine holds, so queries
+// that arrived while others were on the GPU join them at the next wave
+// boundary and share its batched launches.  The engines' waves overlap on
+// the device as in a batch.  A queue limit, when set, refuses the queries
+// that waited longer than it before admission (load shedding: under
+// overload the admitted ones keep their latency).  Finished queries release
 // their reservation and wake their waiters.  Results are read on a separate
-// stream, so a download does not wait for the worker's next wave.
+// stream, so a download does not wait for any engine's next wave.
 #pragma once
 
 #include <chrono>
@@ -35,16 +40,24 @@ struct ServeItem {
   BatchQuery q;
   Clock::time_point t_submit, t_admit, t_done;
   uint64_t held = 0;   // device bytes of the finished result until release
+  size_t engine = 0;   // the engine that runs it
   bool done = false;
 };
 
 class Server {
  public:
-  Server(Ctx& ctx, vedas::VedasStorage* st, uint64_t budget)
-      : ctx_(ctx), st_(st), budget_(budget), eng_(ctx, key_bits_for(st)) {
+  Server(Ctx& ctx, vedas::VedasStorage* st, uint64_t budget) : ctx_(ctx), st_(st), budget_(budget) {
     prepare_mirrors(st_);
     VG_CUDA(cudaStreamCreateWithFlags(&dl_stream_, cudaStreamNonBlocking));
-    worker_ = std::thread([this] { loop(); });
+    const size_t ne = batch_engines();
+    const size_t region = join_region_bytes(ctx_, ne);
+    const bool streams = engine_streams();
+    for (size_t e = 0; e < ne; ++e) {
+      eng_.push_back(std::make_unique<WaveEngine>(ctx_, key_bits_for(st_)));
+      if (region) eng_.back()->use_region(region);
+      if (streams) eng_.back()->use_own_stream();
+    }
+    for (size_t e = 0; e < ne; ++e) workers_.emplace_back([this, e] { run_on_engine_pool(e, [&] { loop(e); }); });
   }
 
   ~Server() {
@@ -53,7 +66,10 @@ class Server {
       stop_ = true;
     }
     cv_work_.notify_all();
-    if (worker_.joinable()) worker_.join();
+    for (auto& w : workers_)
+      if (w.joinable()) w.join();
+    for (auto& e : eng_) e->finish_stream();
+    eng_.clear();
     for (auto& kv : items_) rel_free(ctx_, kv.second->q.rel);
     if (dl_stream_) cudaStreamDestroy(dl_stream_);
   }
@@ -137,12 +153,21 @@ class Server {
     cv_work_.notify_all();   // admission may have waited for these bytes
   }
 
+  // Queries that waited longer than `seconds` in the queue are refused
+  // (VG_ERR_REJECTED) instead of admitted; 0 turns the limit off.
+  void set_queue_limit(double seconds) {
+    std::lock_guard<std::mutex> lk(mu_);
+    queue_limit_s_ = seconds > 0 ? seconds : 0.0;
+  }
+
   void stats(uint64_t out[6]) {
     std::lock_guard<std::mutex> lk(mu_);
     out[0] = submitted_;
     out[1] = completed_;
     out[2] = rejected_;
-    out[3] = eng_.waves();
+    uint64_t w = 0;
+    for (auto& e : eng_) w += e->waves();
+    out[3] = w;
     out[4] = reserved_;
     out[5] = peak_inflight_;
   }
@@ -156,9 +181,9 @@ class Server {
   Ctx& ctx_;
   vedas::VedasStorage* st_;
   uint64_t budget_;
-  WaveEngine eng_;
+  std::vector<std::unique_ptr<WaveEngine>> eng_;
   cudaStream_t dl_stream_ = nullptr;
-  std::thread worker_;
+  std::vector<std::thread> workers_;
   std::mutex mu_;
   std::condition_variable cv_work_, cv_done_;
   std::deque<ServeItem*> queue_;
@@ -166,8 +191,11 @@ class Server {
   std::unordered_map<PlannedQuery*, ServeItem*> inflight_;
   uint64_t next_ticket_ = 0, submitted_ = 0, completed_ = 0, rejected_ = 0, reserved_ = 0, peak_inflight_ = 0;
   uint64_t held_ = 0;   // bytes of finished results not yet released
+  double queue_limit_s_ = 0.0;
   bool stop_ = false;
   vg_status worker_status_ = VG_OK;
+
+  static uint64_t result_bytes(const Rel& r) { return 4ull * r.nrows * r.ncols; }
 
   ServeItem* find_locked(uint64_t ticket) {
     auto f = items_.find(ticket);
@@ -175,50 +203,77 @@ class Server {
     return f->second.get();
   }
 
-  static uint64_t result_bytes(const Rel& r) { return 4ull * r.nrows * r.ncols; }
-
   void finish_locked(ServeItem* it) {
     it->done = true;
     it->t_done = Clock::now();
     cv_done_.notify_all();
   }
 
-  void loop() {
+  // Refuses queued queries past the queue limit (from the head: the queue
+  // is in arrival order).
+  void shed_locked(Clock::time_point now) {
+    if (queue_limit_s_ <= 0) return;
+    while (!queue_.empty() &&
+           std::chrono::duration<double>(now - queue_.front()->t_submit).count() > queue_limit_s_) {
+      ServeItem* it = queue_.front();
+      queue_.pop_front();
+      it->q.status = VG_ERR_REJECTED;
+      it->q.error = "waited longer than the serving queue limit";
+      ++rejected_;
+      finish_locked(it);
+    }
+  }
+
+  bool head_fits_locked() const {
+    if (queue_.empty()) return false;
+    return reserved_ + held_ + queue_.front()->pq.est_bytes <= budget_ || reserved_ == 0;
+  }
+
+  void loop(size_t e) {
+    WaveEngine& eng = *eng_[e];
     while (true) {
       {
         std::unique_lock<std::mutex> lk(mu_);
-        cv_work_.wait(lk, [&] { return stop_ || !queue_.empty() || eng_.active() > 0; });
-        if (stop_ && eng_.active() == 0) return;
-        // admission at the wave boundary, first come first served
-        while (!queue_.empty() && (reserved_ + held_ + queue_.front()->pq.est_bytes <= budget_ ||
-                                   (eng_.active() == 0 && reserved_ == 0))) {
+        cv_work_.wait(lk, [&] {
+          shed_locked(Clock::now());
+          return stop_ || eng.active() > 0 || head_fits_locked();
+        });
+        if (stop_ && eng.active() == 0) return;
+        // admission at the engine's wave boundary, first come first served
+        while (head_fits_locked()) {
           ServeItem* it = queue_.front();
           queue_.pop_front();
           reserved_ += it->pq.est_bytes;
           it->t_admit = Clock::now();
+          it->engine = e;
           inflight_[&it->pq] = it;
-          eng_.add(&it->pq);
+          eng.add(&it->pq);
         }
-        if (eng_.active() > peak_inflight_) peak_inflight_ = eng_.active();
+        if (inflight_.size() > peak_inflight_) peak_inflight_ = inflight_.size();
       }
-      if (eng_.active() == 0) continue;
+      if (eng.active() == 0) continue;
       std::vector<PlannedQuery*> completed;
       try {
-        eng_.wave(completed);
-        if (eng_.active() == 0) eng_.bury();   // idle: free finished queries' intermediates now
-      } catch (const Error& e) {
-        // a device-level failure ends every query in flight with its status
-        std::lock_guard<std::mutex> lk(mu_);
-        worker_status_ = e.status;
-        for (auto& kv : inflight_) {
-          kv.second->q.status = e.status;
-          kv.second->q.error = e.what();
+        eng.wave(completed);
+        if (eng.active() == 0) eng.bury();   // idle: free finished queries' intermediates now
+      } catch (const Error& err) {
+        // a device-level failure ends every query in flight on this engine with its status
+        try {
+          eng.finish_stream();
+        } catch (const Error&) {
+          // the context itself failed: the status below says so
         }
-        std::vector<PlannedQuery*> all;
-        for (auto& kv : inflight_) all.push_back(kv.first);
-        completed = all;
-        for (PlannedQuery* pq : all) pq->plan.reset();
-        eng_.reset();
+        std::lock_guard<std::mutex> lk(mu_);
+        worker_status_ = err.status;
+        completed.clear();
+        for (auto& kv : inflight_)
+          if (kv.second->engine == e) {
+            kv.second->q.status = err.status;
+            kv.second->q.error = err.what();
+            completed.push_back(kv.first);
+          }
+        for (PlannedQuery* pq : completed) pq->plan.reset();
+        eng.reset();
       }
       std::lock_guard<std::mutex> lk(mu_);
       for (PlannedQuery* pq : completed) {
@@ -232,6 +287,7 @@ class Server {
         ++completed_;
         finish_locked(it);
       }
+      if (!completed.empty()) cv_work_.notify_all();   // reservations went back
     }
   }
 };
