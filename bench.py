@@ -43,10 +43,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="batch", choices=["batch", "plain", "serve", "c3"],
+    ap.add_argument("--mode", default="batch", choices=["batch", "plain", "serve", "c3", "profile"],
                     help="batch: the 4096-query batch (default); plain: the same queries one at a "
                          "time; serve: Poisson arrivals on the hub graph; c3: the large snowflake "
-                         "query on the 500M-triple hub graph")
+                         "query on the 500M-triple hub graph; profile: index build and batches only, "
+                         "for profilers")
     ap.add_argument("--rate", default="2000", help="serve: Poisson arrival rates (q/s), comma-separated")
     ap.add_argument("--clients", type=int, default=4, help="serve: submitter threads")
     ap.add_argument("--serve-pool", type=int, default=20000, help="serve: distinct queries drawn from")
@@ -329,6 +330,35 @@ def bench_ingest(args, ctx, g):
         out["cpu_oracle_triples_per_s"] = k / (time.perf_counter() - t1)
         out["cpu_oracle_sample"] = f"{k} triples, one thread (the loader's sequential hash-map rule)"
     return out
+
+
+def bench_profile(args, local):
+    """For profilers: the index build (from device columns) and then only
+    --warmup + --steps batches of the workload, the batches inside an NVTX
+    range named timed_batch (ncu --nvtx --nvtx-include "timed_batch/").  Prints
+    the step time, which is not a reported number."""
+    import torch
+    import vedas_gb300 as vg
+    g, queries, _ = make_workload(args, 0)
+    ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
+    dcols = [torch.from_numpy(x.astype(np.int32)).cuda(local) for x in (g.s, g.p, g.o)]
+    torch.cuda.synchronize(local)
+    ix = vg.Index(ctx, device_ptrs=[c.data_ptr() for c in dcols], n=g.n)
+    del dcols
+    batch_in = [q.encode() for q in queries]
+    for _ in range(args.warmup):
+        run_batch(ix, batch_in)
+    ctx.sync()
+    torch.cuda.nvtx.range_push("timed_batch")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run_batch(ix, batch_in)
+    ctx.sync()
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    torch.cuda.nvtx.range_pop()
+    print(json.dumps({"mode": "profile", "triples": g.n, "queries": len(queries), "s_per_step": dt}), flush=True)
+    ix.close()
+    ctx.close()
 
 
 def bench_ours(args, rank, world, local, pg):
@@ -785,6 +815,8 @@ def main():
         bench_serve(args, rank, world, local, pg)
     elif args.mode == "c3":
         bench_c3(args, rank, world, local, pg)
+    elif args.mode == "profile":
+        bench_profile(args, local)
     else:
         bench_ours(args, rank, world, local, pg)
     if pg is not None:

@@ -372,8 +372,8 @@ vg_status vg_selfcheck_l2_lookup(uint32_t seed, uint32_t graphs, uint32_t lookup
 /* ---- serving (continuous batching) -------------------------------------- */
 typedef struct vg_server vg_server;
 
-/* Starts a serving loop on the context: VG_BATCH_ENGINES wave engines
- * (default 4), each with a worker thread and a stream of its own.
+/* Starts a serving loop on the context: VG_SERVE_ENGINES wave engines
+ * (default 1), each with a worker thread and a stream of its own.
  * Submitted queries are planned on the caller's thread, then admitted first
  * come first served at the engines' wave boundaries while the estimated
  * relation bytes of the queries in flight plus the bytes of finished results
@@ -402,7 +402,9 @@ vg_status vg_serve_latency(vg_server* s, uint64_t ticket, double* queued_s, doub
 vg_status vg_serve_release(vg_server* s, uint64_t ticket);
 /* Load shedding (no reference counterpart): queries that waited more than
  * `seconds` in the queue finish with VG_ERR_REJECTED instead of being
- * admitted; 0 (the default) admits every query however long it waited. */
+ * admitted, and queries submitted while the head of the queue has waited
+ * half of it are refused at once, unplanned; 0 (the default) admits every
+ * query however long it waited. */
 vg_status vg_serve_set_queue_limit(vg_server* s, double seconds);
 /* out6 = {submitted, completed, rejected, waves, reserved bytes, peak queries in flight}. */
 vg_status vg_serve_stats(vg_server* s, uint64_t out6[6]);

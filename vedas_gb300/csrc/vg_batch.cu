@@ -121,7 +121,7 @@ __device__ __forceinline__ void unique_small_segment(const SegRows& g, uint64_t*
   uint64_t o = incl - cnt;
   for (int i = 0; i < kRows; ++i) {
     if (!(diff >> i & 1u)) continue;
-    for (uint32_t c = 0; c < g.ncols; ++c) g.out[c][o] = g.in[c][r0 + i];
+    copy_row(g.out, g.in, g.ncols, r0 + i, o);
     ++o;
   }
   if (lane == 31) *count = incl;
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(kBlock) seg_gather_kernel(const SegRows* __res
       const uint64_t src = perm[r] - base;
       const uint64_t dst = r - base;
       const SegRows& g = segs[s];
-      for (uint32_t c = 0; c < g.ncols; ++c) g.out[c][dst] = g.in[c][src];
+      copy_row(g.out, g.in, g.ncols, src, dst);
     }
   }
 }
@@ -414,7 +414,6 @@ struct JoinOut {
 // its own slice of the shared arrays and each lane writes every 32nd row.
 // Their list (small, nsmall of them; nsmall_dev when on the device) holds no
 // tiles.
-constexpr uint32_t kSmallOutMax = 4096;   // largest write_small_rows a context may choose
 
 __device__ __forceinline__ void write_small_join(const JoinOut* __restrict__ src, JoinOut* jp, uint64_t* s_off,
                                                  uint32_t* s_lo) {
@@ -444,9 +443,7 @@ __device__ __forceinline__ void write_small_join(const JoinOut* __restrict__ src
       else b = mid;
     }
     const uint64_t jj = s_lo[a] + (k - s_off[a]);
-    uint32_t c = 0;
-    for (uint32_t x = 0; x < nlc; ++x) jp->oc[c++][k] = jp->lc[x][a];
-    for (uint32_t x = 0; x < nrc; ++x) jp->oc[c++][k] = jp->rc[x][jj];
+    copy_join_row(jp->oc, jp->lc, nlc, jp->rc, nrc, a, jj, k);
   }
   __syncwarp();   // the slice is free for the warp's next join
 }
@@ -560,9 +557,7 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
         i = li[it];
         jj = s_o.lo[i] + (k - s_o.offs[i]);
       }
-      uint32_t c = 0;
-      for (uint32_t x = 0; x < s_o.nlc; ++x) s_o.oc[c++][k] = s_o.lc[x][i];
-      for (uint32_t x = 0; x < s_o.nrc; ++x) s_o.oc[c++][k] = s_o.rc[x][jj];
+      copy_join_row(s_o.oc, s_o.lc, s_o.nlc, s_o.rc, s_o.nrc, i, jj, k);
     }
   }
 }

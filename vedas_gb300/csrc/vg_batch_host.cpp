@@ -1124,6 +1124,15 @@ size_t batch_engines() {
   return n;
 }
 
+size_t serve_engines() {
+  static const size_t n = [] {
+    long v = 1;
+    if (const char* e = std::getenv("VG_SERVE_ENGINES")) v = std::strtol(e, nullptr, 10);
+    return static_cast<size_t>(std::min(8L, std::max(1L, v)));
+  }();
+  return n;
+}
+
 void post_background(void (*fn)(void*), void* arg) { WorkerPool::get().post(fn, arg); }
 
 void drain_background() {

@@ -86,6 +86,8 @@ void release_later(std::vector<PlannedQuery>& pq);
 // Wave engines of one run_batch, each on its own host thread with its own
 // share of the host worker threads (VG_BATCH_ENGINES, 1..8; default 4).
 size_t batch_engines();
+// Wave engines of a server (VG_SERVE_ENGINES, 1-8, default 1).
+size_t serve_engines();
 // Runs f on the calling thread with engine e's share of the host threads as
 // the pool of its parallel loops (as a batch's engine thread e does).
 void run_on_engine_pool(size_t e, const std::function<void()>& f);

@@ -436,7 +436,6 @@ struct TuneKnob {
 };
 const TuneKnob kKnobs[] = {
     {"sort_items", &vg::TuneParams::sort_items, 8, 16},
-    {"sort_ballot", &vg::TuneParams::sort_ballot, 0, 1},
     {"sort_lookback", &vg::TuneParams::sort_lookback, 1, 4},
     {"join_small_rows", &vg::TuneParams::join_small_rows, 0, 256},
     {"write_small_rows", &vg::TuneParams::write_small_rows, 0, 4096},
@@ -455,6 +454,7 @@ vg_status vg_tune_set(vg_ctx* ctx, const char* name, int64_t value) {
   const TuneKnob* k = find_knob(name);
   if (!ctx || !k || value < static_cast<int64_t>(k->lo) || value > static_cast<int64_t>(k->hi)) return VG_ERR_INVALID;
   if (k->field == &vg::TuneParams::sort_items && value != 8 && value != 16) return VG_ERR_INVALID;
+  if (k->field == &vg::TuneParams::sort_lookback && value != 1 && value != 4) return VG_ERR_INVALID;
   ctx->c.tune.*(k->field) = static_cast<uint32_t>(value);
   return VG_OK;
 }

@@ -47,14 +47,18 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-// Relaxed/acquire/release global accesses used by decoupled look-back.
-__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
+// Look-back status words.  A word carries its flag and its value together
+// and a reader uses nothing but that value, so the accesses need to be
+// single-copy atomic and coherent at GPU scope, not ordered against the
+// thread's other memory operations: relaxed loads and stores, without the
+// fences that acquire and release semantics add to every publish and probe.
+__device__ __forceinline__ uint64_t ld_status_u64(const uint64_t* p) {
   uint64_t v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void st_status_u64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 #endif  // __CUDACC__
 

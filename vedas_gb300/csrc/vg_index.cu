@@ -20,6 +20,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kRows = 8;                 // rows per thread (blocked)
 constexpr int kTileRows = kBlock * kRows;
+static_assert(kRows % 4 == 0, "unpack_rle_kernel moves a thread's rows in 16-byte pieces");
 
 __global__ void max3_kernel(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
                             const uint32_t* __restrict__ c, uint64_t n, uint32_t* out3) {
@@ -80,8 +81,19 @@ __global__ void __launch_bounds__(kBlock) unpack_rle_kernel(UnpackArgs a) {
   const uint64_t r0 = static_cast<uint64_t>(tile) * kTileRows + threadIdx.x * kRows;
 
   uint64_t key[kRows];
+  if (r0 + kRows <= a.n) {
+    // the thread's rows are consecutive and 64-byte aligned (r0 is a multiple
+    // of kRows, the keys an arena block): 16-byte loads
 #pragma unroll
-  for (int i = 0; i < kRows; ++i) key[i] = (r0 + i < a.n) ? a.keys[r0 + i] : 0ull;
+    for (int i = 0; i < kRows; i += 2) {
+      const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(a.keys + r0 + i);
+      key[i] = v.x;
+      key[i + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) key[i] = (r0 + i < a.n) ? a.keys[r0 + i] : 0ull;
+  }
   uint64_t prev = (r0 > 0 && r0 - 1 < a.n) ? a.keys[r0 - 1] : 0ull;
   uint32_t f1 = 0, f2 = 0;
 #pragma unroll
@@ -102,6 +114,28 @@ __global__ void __launch_bounds__(kBlock) unpack_rle_kernel(UnpackArgs a) {
     a.counts[0] = g1 + t1;
     a.counts[1] = g2 + t2;
   }
+  if (r0 + kRows <= a.n) {
+    // the columns' words of the thread's rows: 16-byte stores (32-byte aligned)
+    uint32_t w1[kRows], w2[kRows];
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+      w1[i] = static_cast<uint32_t>((key[i] >> a.sh1) & a.m1);
+      w2[i] = static_cast<uint32_t>(key[i] & a.m2);
+    }
+#pragma unroll
+    for (int i = 0; i < kRows; i += 4) {
+      if (a.col1) *reinterpret_cast<uint4*>(a.col1 + r0 + i) = make_uint4(w1[i], w1[i + 1], w1[i + 2], w1[i + 3]);
+      if (a.col2) *reinterpret_cast<uint4*>(a.col2 + r0 + i) = make_uint4(w2[i], w2[i + 1], w2[i + 2], w2[i + 3]);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+      const uint64_t r = r0 + i;
+      if (r >= a.n) break;
+      if (a.col1) a.col1[r] = static_cast<uint32_t>((key[i] >> a.sh1) & a.m1);
+      if (a.col2) a.col2[r] = static_cast<uint32_t>(key[i] & a.m2);
+    }
+  }
   uint32_t c1 = 0, c2 = 0;
 #pragma unroll
   for (int i = 0; i < kRows; ++i) {
@@ -109,9 +143,6 @@ __global__ void __launch_bounds__(kBlock) unpack_rle_kernel(UnpackArgs a) {
     if (r >= a.n) break;
     const uint32_t v0 = static_cast<uint32_t>(key[i] >> a.sh0);
     const uint32_t v1 = static_cast<uint32_t>((key[i] >> a.sh1) & a.m1);
-    const uint32_t v2 = static_cast<uint32_t>(key[i] & a.m2);
-    if (a.col1) a.col1[r] = v1;
-    if (a.col2) a.col2[r] = v2;
     if (a.l1_vals && (f1 >> i & 1u)) {
       const uint64_t o = g1 + e1 + c1++;
       a.l1_vals[o] = v0;

@@ -77,7 +77,7 @@ __device__ __forceinline__ uint64_t block_excl_scan64(uint64_t v, uint64_t& tota
 // Gives up after kSpinLimit polls: records the timeout and returns an
 // inclusive zero so that every waiter still terminates.
 __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, DeviceErrors* err) {
-  uint64_t s = ld_acquire_u64(p);
+  uint64_t s = ld_status_u64(p);
   uint32_t spins = 0;
   while ((s & ~kValueMask) == 0) {
     if (++spins > kSpinLimit) {
@@ -85,7 +85,7 @@ __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, DeviceErrors*
       return kFlagInc;
     }
     __nanosleep(32);
-    s = ld_acquire_u64(p);
+    s = ld_status_u64(p);
   }
   return s;
 }
@@ -96,7 +96,7 @@ __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, DeviceErrors*
 __device__ __forceinline__ uint64_t warp_lookback(uint64_t* status, uint32_t tile, uint64_t tile_total,
                                                   DeviceErrors* err) {
   const uint32_t lane = lane_id();
-  if (lane == 0) st_release_u64(&status[tile], (tile == 0 ? kFlagInc : kFlagAgg) | tile_total);
+  if (lane == 0) st_status_u64(&status[tile], (tile == 0 ? kFlagInc : kFlagAgg) | tile_total);
   uint64_t prefix = 0;
   if (tile > 0) {
     int64_t j = static_cast<int64_t>(tile) - 1 - lane;
@@ -113,7 +113,7 @@ __device__ __forceinline__ uint64_t warp_lookback(uint64_t* status, uint32_t til
       prefix += warp_sum64(v);
       j -= 32;
     }
-    if (lane == 0) st_release_u64(&status[tile], kFlagInc | (prefix + tile_total));
+    if (lane == 0) st_status_u64(&status[tile], kFlagInc | (prefix + tile_total));
   }
   return prefix;
 }
@@ -124,7 +124,7 @@ __device__ __forceinline__ uint64_t warp_lookback_seg(uint64_t* status, uint64_t
                                                       uint64_t tile_total, DeviceErrors* err) {
   const uint32_t lane = lane_id();
   const bool head = tile == first_tile;
-  if (lane == 0) st_release_u64(&status[tile], (head ? kFlagInc : kFlagAgg) | tile_total);
+  if (lane == 0) st_status_u64(&status[tile], (head ? kFlagInc : kFlagAgg) | tile_total);
   uint64_t prefix = 0;
   if (!head) {
     int64_t j = static_cast<int64_t>(tile) - 1 - lane;
@@ -141,7 +141,7 @@ __device__ __forceinline__ uint64_t warp_lookback_seg(uint64_t* status, uint64_t
       prefix += warp_sum64(v);
       j -= 32;
     }
-    if (lane == 0) st_release_u64(&status[tile], kFlagInc | (prefix + tile_total));
+    if (lane == 0) st_status_u64(&status[tile], kFlagInc | (prefix + tile_total));
   }
   return prefix;
 }
@@ -244,6 +244,38 @@ __device__ __forceinline__ uint32_t unique_diff_bits(const uint32_t* __restrict_
     prev = v[i];
   }
   return d;
+}
+
+// Row copies between column sets.  Every value of the row is loaded before
+// any is stored, through the read-only path (the source columns are never
+// written while a kernel copies from them): the loads of a row are in flight
+// together, where a load after each store would wait for that store (the
+// compiler cannot tell the column pointers apart).
+// out[c][dst] = in[c][src] for c < ncols.
+__device__ __forceinline__ void copy_row(uint32_t* const* out, const uint32_t* const* in, uint32_t ncols,
+                                         uint64_t src, uint64_t dst) {
+  uint32_t v[VG_MAX_COLS];
+#pragma unroll
+  for (int c = 0; c < VG_MAX_COLS; ++c)
+    if (c < static_cast<int>(ncols)) v[c] = __ldg(in[c] + src);
+#pragma unroll
+  for (int c = 0; c < VG_MAX_COLS; ++c)
+    if (c < static_cast<int>(ncols)) out[c][dst] = v[c];
+}
+
+// A join output row: out[c][k] = lc[c][a] for c < nlc, then
+// out[nlc + x][k] = rc[x][b] for x < nrc.
+__device__ __forceinline__ void copy_join_row(uint32_t* const* out, const uint32_t* const* lc, uint32_t nlc,
+                                              const uint32_t* const* rc, uint32_t nrc, uint64_t a, uint64_t b,
+                                              uint64_t k) {
+  uint32_t v[VG_MAX_COLS];
+  const int ncols = static_cast<int>(nlc + nrc);
+#pragma unroll
+  for (int c = 0; c < VG_MAX_COLS; ++c)
+    if (c < ncols) v[c] = c < static_cast<int>(nlc) ? __ldg(lc[c] + a) : __ldg(rc[c - nlc] + b);
+#pragma unroll
+  for (int c = 0; c < VG_MAX_COLS; ++c)
+    if (c < ncols) out[c][k] = v[c];
 }
 
 // compact_store: the kept rows of a tile (bit i of `keep` for row r0 + i,

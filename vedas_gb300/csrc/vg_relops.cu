@@ -234,9 +234,15 @@ __global__ void __launch_bounds__(kBlock) join_write_kernel(JoinWriteArgs a) {
     if (k >= a.total) break;
     const uint64_t i = upper_bound_dev(a.offs, ib, ie, k) - 1;
     const uint64_t j = a.lo[i] + (k - a.offs[i]);
-    uint32_t c = 0;
-    for (uint32_t x = 0; x < a.nlc; ++x) a.oc[c++][k] = a.lc[x][i];
-    for (uint32_t x = 0; x < a.nrc; ++x) a.oc[c++][k] = a.rc[x][j];
+    // every value of the row loaded (read-only path) before any is stored
+    uint32_t v[VG_MAX_COLS];
+    const int ncols = static_cast<int>(a.nlc + a.nrc);
+#pragma unroll
+    for (int c = 0; c < VG_MAX_COLS; ++c)
+      if (c < ncols) v[c] = c < static_cast<int>(a.nlc) ? __ldg(a.lc[c] + i) : __ldg(a.rc[c - a.nlc] + j);
+#pragma unroll
+    for (int c = 0; c < VG_MAX_COLS; ++c)
+      if (c < ncols) a.oc[c][k] = v[c];
   }
 }
 
@@ -251,7 +257,13 @@ __global__ void __launch_bounds__(kBlock) gather_kernel(const uint32_t* __restri
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
   for (uint64_t r = static_cast<uint64_t>(blockIdx.x) * kBlock + threadIdx.x; r < n; r += stride) {
     const uint32_t p = perm[r];
-    for (uint32_t c = 0; c < g.ncols; ++c) g.out[c][r] = g.in[c][p];
+    uint32_t v[VG_MAX_COLS];
+#pragma unroll
+    for (int c = 0; c < VG_MAX_COLS; ++c)
+      if (c < static_cast<int>(g.ncols)) v[c] = __ldg(g.in[c] + p);
+#pragma unroll
+    for (int c = 0; c < VG_MAX_COLS; ++c)
+      if (c < static_cast<int>(g.ncols)) g.out[c][r] = v[c];
   }
 }
 }  // namespace

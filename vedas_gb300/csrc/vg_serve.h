@@ -2,7 +2,7 @@
 //
 // Clients submit query text from any thread; the query is planned on the
 // caller's thread (host work only) and queued.  Each of the server's wave
-// engines (VG_BATCH_ENGINES, default 4) has a worker thread, a stream and a
+// engines (VG_SERVE_ENGINES, default 1) has a worker thread, a stream and a
 // join-output region of its own.  Before each of its waves a worker admits
 // queued queries into its engine, first come first served, while the sum of
 // the estimated relation bytes of every query in flight and the bytes of
@@ -13,8 +13,9 @@
 // that arrived while others were on the GPU join them at the next wave
 // boundary and share its batched launches.  The engines' waves overlap on
 // the device as in a batch.  A queue limit, when set, refuses the queries
-// that waited longer than it before admission (load shedding: under
-// overload the admitted ones keep their latency).  Finished queries release
+// that waited longer than it before admission, and new ones while the head
+// of the queue has waited half of it (load shedding: under overload the
+// admitted ones keep their latency).  Finished queries release
 // their reservation and wake their waiters.  Results are read on a separate
 // stream, so a download does not wait for any engine's next wave.
 #pragma once
@@ -49,7 +50,7 @@ class Server {
   Server(Ctx& ctx, vedas::VedasStorage* st, uint64_t budget) : ctx_(ctx), st_(st), budget_(budget) {
     prepare_mirrors(st_);
     VG_CUDA(cudaStreamCreateWithFlags(&dl_stream_, cudaStreamNonBlocking));
-    const size_t ne = batch_engines();
+    const size_t ne = serve_engines();
     const size_t region = join_region_bytes(ctx_, ne);
     const bool streams = engine_streams();
     for (size_t e = 0; e < ne; ++e) {
@@ -57,7 +58,13 @@ class Server {
       if (region) eng_.back()->use_region(region);
       if (streams) eng_.back()->use_own_stream();
     }
-    for (size_t e = 0; e < ne; ++e) workers_.emplace_back([this, e] { run_on_engine_pool(e, [&] { loop(e); }); });
+    // one engine works with the process-wide pool; several split the host
+    // threads as a batch's engines do
+    for (size_t e = 0; e < ne; ++e)
+      workers_.emplace_back([this, e, ne] {
+        if (ne > 1) run_on_engine_pool(e, [&] { loop(e); });
+        else loop(e);
+      });
   }
 
   ~Server() {
@@ -81,7 +88,11 @@ class Server {
   }
 
   // Plans n queries (host only; on the worker pool when there are many,
-  // otherwise on the caller's thread) and queues them in order.
+  // otherwise on the caller's thread) and queues them in order.  With a
+  // queue limit, queries that arrive while the head of the queue has already
+  // waited half the limit are refused at once, without planning: under
+  // overload the planning of queries that would be shed costs the host time
+  // the admitted ones need.
   void submit_many(const char* const* texts, size_t n, uint64_t* tickets) {
     std::vector<std::unique_ptr<ServeItem>> its(n);
     const auto now = Clock::now();
@@ -90,7 +101,21 @@ class Server {
       its[i]->t_submit = now;
       its[i]->pq.out = &its[i]->q;
     }
-    parallel_for(n, [&](size_t i) { plan_query(ctx_, st_, texts[i] ? texts[i] : "", its[i]->pq); });
+    bool overloaded = false;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      shed_locked(now);
+      overloaded = queue_limit_s_ > 0 && !queue_.empty() &&
+                   std::chrono::duration<double>(now - queue_.front()->t_submit).count() > 0.5 * queue_limit_s_;
+    }
+    if (overloaded) {
+      for (size_t i = 0; i < n; ++i) {
+        its[i]->q.status = VG_ERR_REJECTED;
+        its[i]->q.error = "the serving queue is past half its limit";
+      }
+    } else {
+      parallel_for(n, [&](size_t i) { plan_query(ctx_, st_, texts[i] ? texts[i] : "", its[i]->pq); });
+    }
     std::lock_guard<std::mutex> lk(mu_);
     for (size_t i = 0; i < n; ++i) {
       ServeItem* raw = its[i].get();

@@ -22,7 +22,6 @@ constexpr int kBlock = 256;
 // Keys per thread of a onesweep tile: 16 (tiles of 4096 keys) or 8 (2048),
 // chosen per context (Ctx::tune.sort_items).
 constexpr int kItemsMax = 16;
-constexpr int kLookMax = 4;   // look-back words loaded at once, at most
 constexpr int kRadix = 256;
 constexpr int kMaxPasses = 8;
 
@@ -66,27 +65,11 @@ __global__ void iota_kernel(uint32_t* out, uint64_t n) {
     out[i] = static_cast<uint32_t>(i);
 }
 
-// Lanes of the warp whose digit equals this lane's: one match instruction,
-// or (kBallot) eight ballots, one per digit bit, intersected.  Lanes with
-// ok false take part in neither set.
-template <bool kBallot>
-__device__ __forceinline__ uint32_t digit_peers(uint32_t d, bool ok) {
-  if (!kBallot) return __match_any_sync(0xffffffffu, ok ? d : 0x100u);
-  uint32_t peers = __ballot_sync(0xffffffffu, ok);
-#pragma unroll
-  for (int b = 0; b < 8; ++b) {
-    const bool bit = (d >> b) & 1u;
-    const uint32_t m = __ballot_sync(0xffffffffu, bit);
-    peers &= bit ? m : ~m;
-  }
-  return ok ? peers : 0u;
-}
-
-template <typename K, bool HAS_V, bool IOTA, int kItems, bool kBallot>
+template <typename K, bool HAS_V, bool IOTA, int kItems, int kLook>
 __global__ void __launch_bounds__(kBlock, kItems <= 8 ? 4 : 3) onesweep_kernel(
     const K* __restrict__ kin, K* __restrict__ kout, const uint32_t* __restrict__ vin,
     uint32_t* __restrict__ vout, uint64_t n, uint32_t shift, const uint64_t* __restrict__ bucket_base,
-    uint64_t* status, uint32_t* ticket, uint32_t look, DeviceErrors* err) {
+    uint64_t* status, uint32_t* ticket, DeviceErrors* err) {
   constexpr int kTile = kBlock * kItems;
   extern __shared__ __align__(16) unsigned char smem[];
   K* s_keys = reinterpret_cast<K*>(smem);
@@ -121,7 +104,7 @@ __global__ void __launch_bounds__(kBlock, kItems <= 8 ? 4 : 3) onesweep_kernel(
   for (int i = 0; i < kItems; ++i) {
     const bool ok = wbase + i * 32u + lane < n;
     const uint32_t d = static_cast<uint32_t>(key[i] >> shift) & 0xFFu;
-    const uint32_t peers = digit_peers<kBallot>(d, ok);
+    const uint32_t peers = __match_any_sync(0xffffffffu, ok ? d : 0x100u);
     uint32_t prior = 0;
     if (ok) prior = wh[d];
     __syncwarp();
@@ -141,39 +124,32 @@ __global__ void __launch_bounds__(kBlock, kItems <= 8 ? 4 : 3) onesweep_kernel(
     run += c;
   }
   // Decoupled look-back for digit d over earlier tiles ([tile][digit] layout):
-  // `look` (1..kLookMax) earlier tiles' words are loaded at once, then
-  // summed in order until one holds an inclusive prefix (a word not yet
-  // published is waited for).
+  // kLook earlier tiles' words are loaded at once, then summed in order until
+  // one holds an inclusive prefix (a word not yet published is waited for).
   uint64_t prefix = 0;
   uint64_t* my = status + static_cast<uint64_t>(tile) * kRadix + d;
   if (tile == 0) {
-    st_release_u64(my, kFlagInc | run);
+    st_status_u64(my, kFlagInc | run);
   } else {
-    st_release_u64(my, kFlagAgg | run);
+    st_status_u64(my, kFlagAgg | run);
     int64_t j = static_cast<int64_t>(tile) - 1;
     bool found = false;
     while (!found) {
-      uint64_t w[kLookMax];
+      uint64_t w[kLook];
 #pragma unroll
-      for (int q = 0; q < kLookMax; ++q)
-        w[q] = (q < static_cast<int>(look) && j - q >= 0)
-                   ? ld_acquire_u64(status + static_cast<uint64_t>(j - q) * kRadix + d)
-                   : 0;
+      for (int q = 0; q < kLook; ++q)
+        w[q] = (j - q >= 0) ? ld_status_u64(status + static_cast<uint64_t>(j - q) * kRadix + d) : kFlagInc;
 #pragma unroll
-      for (int q = 0; q < kLookMax; ++q) {
-        if (found || q >= static_cast<int>(look)) break;
-        if (j - q < 0) {
-          found = true;
-          break;
-        }
+      for (int q = 0; q < kLook; ++q) {
+        if (found) break;
         uint64_t v = w[q];
         if ((v & ~kValueMask) == 0) v = wait_status(status + static_cast<uint64_t>(j - q) * kRadix + d, err);
         prefix += v & kValueMask;
-        if (v & kFlagInc) found = true;
+        found = (v & kFlagInc) != 0;
       }
-      j -= look;
+      j -= kLook;
     }
-    st_release_u64(my, kFlagInc | (prefix + run));
+    st_status_u64(my, kFlagInc | (prefix + run));
   }
   uint32_t tot;
   const uint32_t excl = block_excl_scan<kBlock>(run, tot, s_scan);
@@ -202,18 +178,18 @@ __global__ void __launch_bounds__(kBlock, kItems <= 8 ? 4 : 3) onesweep_kernel(
   }
 }
 
-template <typename K, bool HAS_V, bool IOTA, int kItems, bool kBallot>
+template <typename K, bool HAS_V, bool IOTA, int kItems, int kLook>
 void launch_pass_items(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint64_t n,
                        uint32_t shift, const uint64_t* bases, uint64_t* status, uint32_t* ticket) {
   constexpr int kTile = kBlock * kItems;
   const size_t smem = kTile * sizeof(K) + (HAS_V ? kTile * sizeof(uint32_t) : 0);
   // once per instantiation (thread-safe static initialisation)
   static const bool attr_set = [smem] {
-    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA, kItems, kBallot>,
+    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA, kItems, kLook>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     // all of the unified L1/shared storage as shared memory: three or more
     // blocks of a tile's keys (and values) per SM
-    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA, kItems, kBallot>,
+    VG_CUDA(cudaFuncSetAttribute(onesweep_kernel<K, HAS_V, IOTA, kItems, kLook>,
                                  cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
     return true;
   }();
@@ -221,8 +197,8 @@ void launch_pass_items(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uin
   const uint64_t tiles = div_up(n, kTile);
   const double bytes = static_cast<double>(n) * (2 * sizeof(K) + (HAS_V ? (IOTA ? 4 : 8) : 0));
   ctx.launch("radix_onesweep", bytes, [&] {
-    onesweep_kernel<K, HAS_V, IOTA, kItems, kBallot><<<static_cast<unsigned>(tiles), kBlock, smem, ctx.stream>>>(
-        kin, kout, vin, vout, n, shift, bases, status, ticket, ctx.tune.sort_lookback, ctx.d_err);
+    onesweep_kernel<K, HAS_V, IOTA, kItems, kLook><<<static_cast<unsigned>(tiles), kBlock, smem, ctx.stream>>>(
+        kin, kout, vin, vout, n, shift, bases, status, ticket, ctx.d_err);
   });
   VG_CUDA(cudaGetLastError());
 }
@@ -230,15 +206,15 @@ void launch_pass_items(Ctx& ctx, const K* kin, K* kout, const uint32_t* vin, uin
 template <typename K, bool HAS_V, bool IOTA>
 void launch_pass(Ctx& ctx, int items, const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint64_t n,
                  uint32_t shift, const uint64_t* bases, uint64_t* status, uint32_t* ticket) {
-  const bool ballot = ctx.tune.sort_ballot != 0;
+  const bool look4 = ctx.tune.sort_lookback == 4;
   if (items == 8) {
-    if (ballot) launch_pass_items<K, HAS_V, IOTA, 8, true>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
-    else launch_pass_items<K, HAS_V, IOTA, 8, false>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
+    if (look4) launch_pass_items<K, HAS_V, IOTA, 8, 4>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
+    else launch_pass_items<K, HAS_V, IOTA, 8, 1>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
   } else {
-    if (ballot)
-      launch_pass_items<K, HAS_V, IOTA, kItemsMax, true>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
+    if (look4)
+      launch_pass_items<K, HAS_V, IOTA, kItemsMax, 4>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
     else
-      launch_pass_items<K, HAS_V, IOTA, kItemsMax, false>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
+      launch_pass_items<K, HAS_V, IOTA, kItemsMax, 1>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
   }
 }
 

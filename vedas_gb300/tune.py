@@ -2,7 +2,8 @@
 
 The kernels' launch shapes have choices whose best value depends on the GPU
 and on the workload's shape (relation sizes, how many queries run together):
-radix-sort keys per thread (the sort tile), the sizes below which a join, a
+radix-sort keys per thread (the sort tile) and look-back words loaded at
+once, the sizes below which a join, a
 join output or a final compaction takes one warp instead of tiles, and the
 block count of a join write sized on the device.  No choice changes a result.
 
@@ -26,12 +27,13 @@ import time
 # knob -> (candidate values, value of a fresh context)
 KNOBS = {
     "sort_items": ([16, 8], 16),
+    "sort_lookback": ([1, 4], 1),
     "join_small_rows": ([256, 64, 0], 256),
     "write_small_rows": ([1024, 256, 4096, 0], 1024),
     "unique_small_rows": ([256, 0], 256),
     "write_blocks_per_sm": ([8, 4, 2], 8),
 }
-ORDER = ["sort_items", "join_small_rows", "write_small_rows", "unique_small_rows", "write_blocks_per_sm"]
+ORDER = ["sort_items", "sort_lookback", "join_small_rows", "write_small_rows", "unique_small_rows", "write_blocks_per_sm"]
 
 
 def select(timings: dict, current, margin: float = 0.02):
