@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(kBlock) jw_range_kernel(const JoinOut* __restr
   }
 }
 
-__global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __restrict__ jo,
+__global__ void __launch_bounds__(kBlock, 5) bjoin_write_kernel(const JoinOut* __restrict__ jo,
                                                              const uint64_t* __restrict__ ostart,
                                                              const uint32_t* __restrict__ tile_join,
                                                              const uint2* __restrict__ ranges,
@@ -513,51 +513,77 @@ __global__ void __launch_bounds__(kBlock) bjoin_write_kernel(const JoinOut* __re
         s_lo[e] = s_o.lo[ib + e];
       }
     __syncthreads();
-    // unstaged (a sparse tile: more than kStage left rows, most without
-    // matches): the left rows of the thread's kRows output rows come from
-    // kRows binary searches of the offsets advanced in lockstep, so each
-    // round has kRows independent loads in flight
-    uint64_t li[kRows];
-    if (!staged) {
-      uint64_t k8[kRows];
+    // 1. the left and right row of each of the thread's output rows
+    uint32_t li[kRows], ri[kRows];
+    if (staged) {
+      uint32_t p = 0;   // the current left row, relative to ib
 #pragma unroll
       for (int it = 0; it < kRows; ++it) {
         const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
-        k8[it] = k < kend ? k : kend - 1;
-        li[it] = ib;
+        li[it] = ri[it] = 0;
+        if (k < kend) {
+          // last p with s_off[p] <= k, moving forward from the previous row's p
+          uint32_t step = 1;
+          while (p + step < m && s_off[p + step] <= k) {
+            p += step;
+            step <<= 1;
+          }
+          while (step > 1) {
+            step >>= 1;
+            if (p + step < m && s_off[p + step] <= k) p += step;
+          }
+          li[it] = static_cast<uint32_t>(ib + p);
+          ri[it] = static_cast<uint32_t>(s_lo[p] + (k - s_off[p]));
+        }
       }
-      uint64_t n = ie - ib;                     // last i in [ib, ie) with offs[i] <= k
-      while (n > 1) {
-        const uint64_t half = n >> 1;
+    } else {
+      // a sparse tile (more than kStage left rows, most without matches): the
+      // left rows of kGroup of the thread's output rows at a time come from
+      // kGroup binary searches of the offsets advanced in lockstep, so each
+      // round has kGroup independent loads in flight
+      constexpr int kGroup = 4;
 #pragma unroll
-        for (int it = 0; it < kRows; ++it)
-          li[it] = (s_o.offs[li[it] + half] <= k8[it]) ? li[it] + half : li[it];
-        n -= half;
+      for (int g0 = 0; g0 < kRows; g0 += kGroup) {
+        uint64_t lq[kGroup], kk[kGroup];
+#pragma unroll
+        for (int q = 0; q < kGroup; ++q) {
+          const uint64_t k = kb + static_cast<uint64_t>(g0 + q) * kBlock + threadIdx.x;
+          kk[q] = k < kend ? k : kend - 1;
+          lq[q] = ib;
+        }
+        uint64_t n = ie - ib;                     // last i in [ib, ie) with offs[i] <= k
+        while (n > 1) {
+          const uint64_t half = n >> 1;
+#pragma unroll
+          for (int q = 0; q < kGroup; ++q) lq[q] = (s_o.offs[lq[q] + half] <= kk[q]) ? lq[q] + half : lq[q];
+          n -= half;
+        }
+#pragma unroll
+        for (int q = 0; q < kGroup; ++q) {
+          li[g0 + q] = static_cast<uint32_t>(lq[q]);
+          ri[g0 + q] = static_cast<uint32_t>(s_o.lo[lq[q]] + (kk[q] - s_o.offs[lq[q]]));
+        }
       }
     }
-    uint32_t p = 0;   // staged: the current left row, relative to ib
-    for (int it = 0; it < kRows; ++it) {
-      const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
-      if (k >= kend) break;
-      uint64_t i, jj;
-      if (staged) {
-        // last p with s_off[p] <= k, moving forward from the previous row's p
-        uint32_t step = 1;
-        while (p + step < m && s_off[p + step] <= k) {
-          p += step;
-          step <<= 1;
-        }
-        while (step > 1) {
-          step >>= 1;
-          if (p + step < m && s_off[p + step] <= k) p += step;
-        }
-        i = ib + p;
-        jj = s_lo[p] + (k - s_off[p]);
-      } else {
-        i = li[it];
-        jj = s_o.lo[i] + (k - s_o.offs[i]);
+    // 2. column by column: each thread's kRows loads of a column are in
+    // flight together (read-only path), each store instruction writes
+    // consecutive rows, and one column's pointers are live at a time
+    const uint32_t nlc = s_o.nlc, ncols = s_o.nlc + s_o.nrc;
+    for (uint32_t c = 0; c < ncols; ++c) {
+      const bool left = c < nlc;
+      const uint32_t* src = left ? s_o.lc[c] : s_o.rc[c - nlc];
+      uint32_t* dst = s_o.oc[c];
+      uint32_t v[kRows];
+#pragma unroll
+      for (int it = 0; it < kRows; ++it) {
+        const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
+        if (k < kend) v[it] = __ldg(src + (left ? li[it] : ri[it]));
       }
-      copy_join_row(s_o.oc, s_o.lc, s_o.nlc, s_o.rc, s_o.nrc, i, jj, k);
+#pragma unroll
+      for (int it = 0; it < kRows; ++it) {
+        const uint64_t k = kb + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
+        if (k < kend) dst[k] = v[it];
+      }
     }
   }
 }

@@ -192,7 +192,7 @@ struct TuneParams {
   uint32_t join_small_rows = 256;    // joins with at most this many left rows: one warp each (0..256)
   uint32_t write_small_rows = 1024;  // outputs with at most this many rows: one warp each (0..4096)
   uint32_t unique_small_rows = 256;  // final compactions with at most this many rows: one warp each (0..256)
-  uint32_t write_blocks_per_sm = 8;  // blocks per SM of a join write whose size is on the device (1..8)
+  uint32_t write_blocks_per_sm = 5;  // blocks per SM of a join write whose size is on the device (1..8; 5 fit)
 };
 
 struct Ctx {

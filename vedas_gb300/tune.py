@@ -31,7 +31,7 @@ KNOBS = {
     "join_small_rows": ([256, 64, 0], 256),
     "write_small_rows": ([1024, 256, 4096, 0], 1024),
     "unique_small_rows": ([256, 0], 256),
-    "write_blocks_per_sm": ([8, 4, 2], 8),
+    "write_blocks_per_sm": ([5, 8, 4, 2], 5),
 }
 ORDER = ["sort_items", "sort_lookback", "join_small_rows", "write_small_rows", "unique_small_rows", "write_blocks_per_sm"]
 
