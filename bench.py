@@ -333,17 +333,21 @@ def bench_ingest(args, ctx, g):
 
 
 def bench_profile(args, local):
-    """For profilers: the index build (from device columns) and then only
-    --warmup + --steps batches of the workload, the batches inside an NVTX
-    range named timed_batch (ncu --nvtx --nvtx-include "timed_batch/").  Prints
-    the step time, which is not a reported number."""
+    """For profilers: the index build (from device columns, inside an NVTX
+    range named index_build) and then only --warmup + --steps batches of the
+    workload, the timed ones inside an NVTX range named timed_batch (ncu --nvtx
+    --nvtx-include "timed_batch/").  Prints the step time, which is not a
+    reported number."""
     import torch
     import vedas_gb300 as vg
     g, queries, _ = make_workload(args, 0)
     ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
     dcols = [torch.from_numpy(x.astype(np.int32)).cuda(local) for x in (g.s, g.p, g.o)]
     torch.cuda.synchronize(local)
+    torch.cuda.nvtx.range_push("index_build")
     ix = vg.Index(ctx, device_ptrs=[c.data_ptr() for c in dcols], n=g.n)
+    ctx.sync()
+    torch.cuda.nvtx.range_pop()
     del dcols
     batch_in = [q.encode() for q in queries]
     for _ in range(args.warmup):
