@@ -268,10 +268,10 @@ __device__ __forceinline__ void count_small_join(const JoinSeg& g, uint32_t* __r
   const uint64_t w1 = warp_bound<true, uint32_t>(g.rk, w0, g.nr, g.lk[nl - 1]);
   const uint64_t first = static_cast<uint64_t>(lane) * kJcKeys;
   uint32_t key[kJcKeys];
-  uint64_t lb[kJcKeys], ub[kJcKeys];
+  uint32_t lb[kJcKeys], ub[kJcKeys];
 #pragma unroll
   for (int q = 0; q < kJcKeys; ++q) key[q] = g.lk[first + q < nl ? first + q : nl - 1];
-  lockstep_bounds<kJcKeys>(g.rk, w0, w1, key, lb, ub);
+  lockstep_bounds32<kJcKeys>(g.rk, static_cast<uint32_t>(w0), static_cast<uint32_t>(w1), key, lb, ub);
   uint64_t sum = 0;
 #pragma unroll
   for (int q = 0; q < kJcKeys; ++q)
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kJcBlock) jc_window_kernel(const JoinSeg* __re
   }
 }
 
-__global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
+__global__ void __launch_bounds__(kJcBlock, 5) bjoin_count_scan_kernel(
     const JoinSeg* __restrict__ js, const uint64_t* __restrict__ bstart, const uint32_t* __restrict__ tile_join,
     const uint2* __restrict__ win, const uint32_t* __restrict__ small, uint32_t nsmall, uint32_t small_blocks,
     uint32_t* __restrict__ lo, uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket,
@@ -901,6 +901,13 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
     });
     VG_CUDA(cudaGetLastError());
   }
+  // all unified storage as shared memory: five blocks' windows per SM
+  static const bool carveout_set = [] {
+    VG_CUDA(cudaFuncSetAttribute(bjoin_count_scan_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared));
+    return true;
+  }();
+  (void)carveout_set;
   ctx.launch("join_count_scan", cbytes + 12.0 * rows, [&] {
     bjoin_count_scan_kernel<<<static_cast<unsigned>(small_blocks + T), kJcBlock, 0, ctx.stream>>>(
         djs, dbs, dtj, dwin, dsm, nsmall, small_blocks, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);

@@ -9,7 +9,7 @@ namespace vg {
 constexpr int kJcBlock = 256;
 constexpr int kJcKeys = 8;                      // left keys per thread, consecutive
 constexpr int kJcTile = kJcBlock * kJcKeys;     // 2048 left keys per block
-constexpr int kJcWindow = 11264;                // right keys staged per block (44 KiB)
+constexpr int kJcWindow = 10752;                // right keys staged per block (42 KiB: five blocks per SM)
 
 struct JoinCountSmem {
   alignas(16) uint32_t keys[kJcWindow + 8];
@@ -180,6 +180,33 @@ __device__ __forceinline__ void lockstep_bounds(const uint32_t* __restrict__ R, 
   }
 }
 
+// lockstep_bounds with 32-bit positions (every join side has fewer than 2^32
+// rows), which halves the registers the bounds hold.
+template <int K>
+__device__ __forceinline__ void lockstep_bounds32(const uint32_t* __restrict__ R, uint32_t w0, uint32_t w1,
+                                                  const uint32_t (&key)[K], uint32_t (&lo)[K], uint32_t (&hi)[K]) {
+#pragma unroll
+  for (int j = 0; j < K; ++j) lo[j] = hi[j] = w0;
+  if (w1 <= w0) return;
+  uint32_t n = w1 - w0;
+  while (n > 1) {
+    const uint32_t half = n >> 1;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const uint32_t a = __ldg(R + lo[j] + half);
+      const uint32_t b = __ldg(R + hi[j] + half);
+      lo[j] = (a < key[j]) ? lo[j] + half : lo[j];
+      hi[j] = (b <= key[j]) ? hi[j] + half : hi[j];
+    }
+    n -= half;
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    lo[j] += (__ldg(R + lo[j]) < key[j]) ? 1 : 0;
+    hi[j] += (__ldg(R + hi[j]) <= key[j]) ? 1 : 0;
+  }
+}
+
 // Thread 0 of the block: records the tile's right-key window [w0, w1) and
 // decides how it is staged in shared memory (sm.staged: 0 not staged, 1 by
 // the block's threads, 2 its 16-byte aligned middle by one cp.async.bulk
@@ -266,8 +293,8 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
   if (first >= i_end) return;   // counts stay zero
 
   if (!use_smem) {
-    uint64_t lo[kJcKeys], hi[kJcKeys];
-    lockstep_bounds<kJcKeys>(R, w0, w1, key, lo, hi);
+    uint32_t lo[kJcKeys], hi[kJcKeys];
+    lockstep_bounds32<kJcKeys>(R, static_cast<uint32_t>(w0), static_cast<uint32_t>(w1), key, lo, hi);
 #pragma unroll
     for (int j = 0; j < kJcKeys; ++j) {
       const uint64_t i = first + j;
