@@ -466,42 +466,6 @@ void WaveEngine::use_region(size_t bytes) {
 
 void WaveEngine::add(PlannedQuery* pq) { active_.push_back(pq); }
 
-void WaveEngine::open_intake() {
-  std::lock_guard<std::mutex> lk(intake_mu_);
-  intake_open_ = true;
-}
-
-void WaveEngine::offer(std::vector<PlannedQuery*> qs) {
-  {
-    std::lock_guard<std::mutex> lk(intake_mu_);
-    intake_.insert(intake_.end(), qs.begin(), qs.end());
-  }
-  intake_cv_.notify_all();
-}
-
-void WaveEngine::close_intake() {
-  {
-    std::lock_guard<std::mutex> lk(intake_mu_);
-    intake_open_ = false;
-  }
-  intake_cv_.notify_all();
-}
-
-void WaveEngine::take_intake() {
-  std::lock_guard<std::mutex> lk(intake_mu_);
-  active_.insert(active_.end(), intake_.begin(), intake_.end());
-  intake_.clear();
-}
-
-bool WaveEngine::take_or_wait() {
-  std::unique_lock<std::mutex> lk(intake_mu_);
-  intake_cv_.wait(lk, [&] { return !intake_.empty() || !intake_open_; });
-  if (intake_.empty()) return false;
-  active_.insert(active_.end(), intake_.begin(), intake_.end());
-  intake_.clear();
-  return true;
-}
-
 void WaveEngine::bury() {
   release_later(graveyard_);
   graveyard_.clear();
@@ -610,8 +574,6 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     tr.h_finish = since(tf);
   }
 
-  // queries planned since the last wave join this one
-  take_intake();
   // queries with a next job run it; the others finish (or have failed)
   std::vector<PlannedQuery*> done;
   for (PlannedQuery* q : active_) {
@@ -1042,7 +1004,12 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
   out.queries.resize(n);
   prepare_mirrors(storage);
   std::vector<PlannedQuery> pq(n);
-  for (size_t i = 0; i < n; ++i) pq[i].out = &out.queries[i];
+  auto t0 = Clock::now();
+  pfor(n, [&](size_t i) {
+    pq[i].out = &out.queries[i];
+    plan_query(ctx, storage, texts[i] ? texts[i] : "", pq[i]);
+  });
+  const double plan_s = since(t0);
   // engines take turns on the stream: while the device runs one engine's
   // half-wave, the host runs the others' stages.  Each engine runs on its own
   // host thread with its own share of the worker threads, so the engines'
@@ -1069,53 +1036,25 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
     e->tracing = trace_path != nullptr;
     e->trace_origin = t_all;
   }
-  // Queries are planned in chunks on the calling thread (the process-wide
-  // pool) while the engines already run the chunks planned before: the first
-  // chunk is small, so the device starts soon.  Queries are dealt in batch
-  // order.  (Dealing by cost, so that every engine got the same mix of long
-  // and short job lists, was measured slower on the 4096-query batch: 27.3 ms
-  // against 22.7 ms per batch, since every engine then ran the longest chain
-  // of waves, each wave with few queries.)
-  for (auto& e : eng) e->open_intake();
+  // Queries are dealt in batch order.  (Dealing by cost, so that every
+  // engine got the same mix of long and short job lists, was measured slower
+  // on the 4096-query batch: 27.3 ms against 22.7 ms per batch, since every
+  // engine then ran the longest chain of waves, each wave with few queries.)
+  for (size_t i = 0; i < pq.size(); ++i) eng[i % ne]->add(&pq[i]);
   std::vector<std::exception_ptr> err(ne);
   auto drive = [&](size_t e) {
     UseEnginePool use(e);
     std::vector<PlannedQuery*> done;
     try {
-      while (eng[e]->active() > 0 || eng[e]->take_or_wait()) eng[e]->step(done);
+      while (eng[e]->active() > 0) eng[e]->step(done);
     } catch (...) {
       err[e] = std::current_exception();
-      // the engine takes no more queries: drain what it was offered
-      while (eng[e]->take_or_wait()) {
-      }
     }
   };
   std::vector<std::thread> th;
-  for (size_t e = 0; e < ne; ++e) th.emplace_back(drive, e);
-  auto t0 = Clock::now();
-  std::exception_ptr plan_err;
-  try {
-    const size_t first = std::min<size_t>(n, 64 * ne);
-    size_t b = 0;
-    while (b < n) {
-      const size_t e_ = b == 0 ? first : std::min(n, b + std::max<size_t>(first, n / 4));
-      pfor(e_ - b, [&](size_t k) { plan_query(ctx, storage, texts[b + k] ? texts[b + k] : "", pq[b + k]); });
-      std::vector<std::vector<PlannedQuery*>> deal(ne);
-      for (size_t i = b; i < e_; ++i) deal[i % ne].push_back(&pq[i]);
-      for (size_t e = 0; e < ne; ++e)
-        if (!deal[e].empty()) eng[e]->offer(std::move(deal[e]));
-      b = e_;
-    }
-  } catch (...) {
-    plan_err = std::current_exception();   // raised once the engines have stopped
-  }
-  const double plan_s = since(t0);
-  for (auto& e : eng) e->close_intake();
+  for (size_t e = 1; e < ne; ++e) th.emplace_back(drive, e);
+  drive(0);
   for (auto& t : th) t.join();
-  if (plan_err) {
-    for (auto& e : eng) e->finish_stream();
-    std::rethrow_exception(plan_err);
-  }
   // the results are read on the context's stream: the engines' streams finish first
   for (auto& e : eng) e->finish_stream();
   for (auto& e : err)

@@ -1,7 +1,6 @@
 #pragma once
 
 #include <chrono>
-#include <condition_variable>
 #include <functional>
 #include <memory>
 #include <mutex>
@@ -122,15 +121,6 @@ class WaveEngine {
   void add(PlannedQuery* pq);
   // Queries added and not yet handed back (waiting, in flight or finishing).
   size_t active() const { return active_.size() + run_.size() + final_.size(); }
-  // Queries handed over from another thread while the engine runs: offered
-  // queries join at the engine's next stage A.  open_intake before the first
-  // offer, close_intake after the last; take_or_wait (engine thread) moves
-  // offered queries in, waiting for some while the intake is open, and
-  // returns false once it is closed and empty.
-  void open_intake();
-  void offer(std::vector<PlannedQuery*> qs);
-  void close_intake();
-  bool take_or_wait();
   // Forgets every query in flight (after a device-level failure).
   void reset();
   // Stage A then stage B.
@@ -200,11 +190,6 @@ class WaveEngine {
   uint32_t waves_ = 0;
   bool next_is_a_ = true;
   std::vector<PlannedQuery*> active_;   // queries waiting for their next job
-  std::mutex intake_mu_;
-  std::condition_variable intake_cv_;
-  std::vector<PlannedQuery*> intake_;   // offered, not yet taken in
-  bool intake_open_ = false;
-  void take_intake();                   // offered queries into active_ (no wait)
   // the wave in flight
   std::vector<PlannedQuery*> run_;
   std::vector<Item> items_;
