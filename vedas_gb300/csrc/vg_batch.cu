@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kJcBlock) jc_window_kernel(const JoinSeg* __re
   }
 }
 
-__global__ void __launch_bounds__(kJcBlock, 5) bjoin_count_scan_kernel(
+__global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
     const JoinSeg* __restrict__ js, const uint64_t* __restrict__ bstart, const uint32_t* __restrict__ tile_join,
     const uint2* __restrict__ win, const uint32_t* __restrict__ small, uint32_t nsmall, uint32_t small_blocks,
     uint32_t* __restrict__ lo, uint64_t* __restrict__ offs, uint64_t* status, uint32_t* ticket,
@@ -901,7 +901,7 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
     });
     VG_CUDA(cudaGetLastError());
   }
-  // all unified storage as shared memory: five blocks' windows per SM
+  // all unified storage as shared memory: four blocks' windows per SM
   static const bool carveout_set = [] {
     VG_CUDA(cudaFuncSetAttribute(bjoin_count_scan_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared));

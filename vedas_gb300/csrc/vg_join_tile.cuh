@@ -9,7 +9,7 @@ namespace vg {
 constexpr int kJcBlock = 256;
 constexpr int kJcKeys = 8;                      // left keys per thread, consecutive
 constexpr int kJcTile = kJcBlock * kJcKeys;     // 2048 left keys per block
-constexpr int kJcWindow = 10752;                // right keys staged per block (42 KiB: five blocks per SM)
+constexpr int kJcWindow = 11264;                // right keys staged per block (44 KiB)
 
 struct JoinCountSmem {
   alignas(16) uint32_t keys[kJcWindow + 8];

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kBlock) join_count_kernel(KeyOf<TWO> L, uint64
 
 // One block per 2048 left keys; the right-key window is staged in shared
 // memory by a bulk copy (vg_join_tile.cuh).
-__global__ void __launch_bounds__(kJcBlock, 5) join_count_tiled_kernel(const uint32_t* __restrict__ L, uint64_t nl,
+__global__ void __launch_bounds__(kJcBlock, 4) join_count_tiled_kernel(const uint32_t* __restrict__ L, uint64_t nl,
                                                                     const uint32_t* __restrict__ R, uint64_t nr,
                                                                     uint32_t* __restrict__ lo,
                                                                     uint32_t* __restrict__ cnt, DeviceErrors* err) {
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kJcBlock, 5) join_count_tiled_kernel(const uin
   if (threadIdx.x == 0) jc_drain_window(sm, err);
 }
 
-// All unified storage as shared memory for the tiled count: five blocks'
+// All unified storage as shared memory for the tiled count: four blocks'
 // windows per SM (once per process).
 void count_tiled_carveout() {
   static const bool set = [] {
