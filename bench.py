@@ -334,32 +334,33 @@ def bench_ingest(args, ctx, g):
 
 def bench_profile(args, local):
     """For profilers: the index build (from device columns, inside an NVTX
-    range named index_build) and then only --warmup + --steps batches of the
-    workload, the timed ones inside an NVTX range named timed_batch (ncu --nvtx
-    --nvtx-include "timed_batch/").  Prints the step time, which is not a
-    reported number."""
+    start/end range named index_build) and then only --warmup + --steps
+    batches of the workload, the timed ones inside a start/end range named
+    timed_batch (ncu --nvtx --nvtx-include timed_batch).  Start/end ranges are
+    process-wide, so they hold the launches of every wave engine's thread.
+    Prints the step time, which is not a reported number."""
     import torch
     import vedas_gb300 as vg
     g, queries, _ = make_workload(args, 0)
     ctx = vg.Context(local, arena_bytes=int(args.arena_gb * (1 << 30)))
     dcols = [torch.from_numpy(x.astype(np.int32)).cuda(local) for x in (g.s, g.p, g.o)]
     torch.cuda.synchronize(local)
-    torch.cuda.nvtx.range_push("index_build")
+    r_build = torch.cuda.nvtx.range_start("index_build")
     ix = vg.Index(ctx, device_ptrs=[c.data_ptr() for c in dcols], n=g.n)
     ctx.sync()
-    torch.cuda.nvtx.range_pop()
+    torch.cuda.nvtx.range_end(r_build)
     del dcols
     batch_in = [q.encode() for q in queries]
     for _ in range(args.warmup):
         run_batch(ix, batch_in)
     ctx.sync()
-    torch.cuda.nvtx.range_push("timed_batch")
+    r_batch = torch.cuda.nvtx.range_start("timed_batch")
     t0 = time.perf_counter()
     for _ in range(args.steps):
         run_batch(ix, batch_in)
     ctx.sync()
     dt = (time.perf_counter() - t0) / max(args.steps, 1)
-    torch.cuda.nvtx.range_pop()
+    torch.cuda.nvtx.range_end(r_batch)
     print(json.dumps({"mode": "profile", "triples": g.n, "queries": len(queries), "s_per_step": dt}), flush=True)
     ix.close()
     ctx.close()

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kBlock) bunique_kernel(const SegRows* __restri
   __shared__ uint32_t s_tile;
   __shared__ SegRows s_seg;
   __shared__ uint32_t s_s;
-  __shared__ uint32_t s_keep[kTileRows];
+  __shared__ uint32_t s_keep[2 * kTileRows];   // compact_store: two columns at a time
   if (threadIdx.x == 0) {
     s_tile = atomicAdd(ticket, 1u);
     s_s = tile_seg[s_tile];
@@ -187,50 +187,58 @@ __device__ __forceinline__ uint32_t seg_of_row(const uint64_t* __restrict__ rsta
   return lo;
 }
 
+// Segmented row loops: blocks take chunks of kChunkRows consecutive rows
+// (each thread kRows of them, kBlock apart, so loads and stores coalesce);
+// a chunk's first segment comes from a table made on the host and the next
+// chunk's bounds its last, so each row searches only between those two
+// (usually one segment).
+constexpr uint32_t kChunkRows = kBlock * kRows;
+
+__device__ __forceinline__ void chunk_segments(const uint32_t* __restrict__ chunk_seg, uint64_t nchunks,
+                                               uint32_t S, uint64_t c, uint32_t& k0, uint32_t& k1) {
+  k0 = chunk_seg[c];
+  k1 = c + 1 < nchunks ? chunk_seg[c + 1] : S - 1;
+}
+
 // (segment, key) composite sort keys: the segment sits above the key's
 // key_bits bits, so one sort orders rows by segment and, within it, by key.
 __global__ void __launch_bounds__(kBlock) composite_keys_kernel(const uint32_t* const* __restrict__ col0,
                                                                 const uint64_t* __restrict__ rstart, uint32_t S,
-                                                                uint32_t key_bits, uint64_t* __restrict__ keys) {
-  __shared__ uint32_t s_k[2];
+                                                                const uint32_t* __restrict__ chunk_seg,
+                                                                uint64_t nchunks, uint32_t key_bits,
+                                                                uint64_t* __restrict__ keys) {
   const uint64_t total = rstart[S];
-  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
-  for (uint64_t b = static_cast<uint64_t>(blockIdx.x) * kBlock; b < total; b += stride) {
-    const uint64_t e = (b + kBlock < total) ? b + kBlock : total;
-    if (threadIdx.x == 0) s_k[0] = seg_of(rstart, S, b);
-    if (threadIdx.x == 32) s_k[1] = seg_of(rstart, S, e - 1);
-    __syncthreads();
-    const uint32_t k0 = s_k[0], k1 = s_k[1];
-    __syncthreads();
-    const uint64_t r = b + threadIdx.x;
-    if (r < e) {
-      const uint32_t s = seg_of_row(rstart, k0, k1, r);
-      keys[r] = (static_cast<uint64_t>(s) << key_bits) | col0[s][r - rstart[s]];
+  for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    uint32_t k0, k1;
+    chunk_segments(chunk_seg, nchunks, S, c, k0, k1);
+#pragma unroll
+    for (int it = 0; it < kRows; ++it) {
+      const uint64_t r = c * kChunkRows + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
+      if (r < total) {
+        const uint32_t s = seg_of_row(rstart, k0, k1, r);
+        keys[r] = (static_cast<uint64_t>(s) << key_bits) | __ldg(col0[s] + (r - rstart[s]));
+      }
     }
   }
 }
 
 __global__ void __launch_bounds__(kBlock) seg_gather_kernel(const SegRows* __restrict__ segs,
                                                             const uint64_t* __restrict__ rstart, uint32_t S,
-                                                            const uint32_t* __restrict__ perm) {
-  __shared__ uint32_t s_k[2];
+                                                            const uint32_t* __restrict__ chunk_seg,
+                                                            uint64_t nchunks, const uint32_t* __restrict__ perm) {
   const uint64_t total = rstart[S];
-  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kBlock;
-  for (uint64_t b = static_cast<uint64_t>(blockIdx.x) * kBlock; b < total; b += stride) {
-    const uint64_t e = (b + kBlock < total) ? b + kBlock : total;
-    if (threadIdx.x == 0) s_k[0] = seg_of(rstart, S, b);
-    if (threadIdx.x == 32) s_k[1] = seg_of(rstart, S, e - 1);
-    __syncthreads();
-    const uint32_t k0 = s_k[0], k1 = s_k[1];
-    __syncthreads();
-    const uint64_t r = b + threadIdx.x;
-    if (r < e) {
-      const uint32_t s = seg_of_row(rstart, k0, k1, r);
-      const uint64_t base = rstart[s];
-      const uint64_t src = perm[r] - base;
-      const uint64_t dst = r - base;
-      const SegRows& g = segs[s];
-      copy_row(g.out, g.in, g.ncols, src, dst);
+  for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    uint32_t k0, k1;
+    chunk_segments(chunk_seg, nchunks, S, c, k0, k1);
+#pragma unroll 2
+    for (int it = 0; it < kRows; ++it) {
+      const uint64_t r = c * kChunkRows + static_cast<uint64_t>(it) * kBlock + threadIdx.x;
+      if (r < total) {
+        const uint32_t s = seg_of_row(rstart, k0, k1, r);
+        const uint64_t base = rstart[s];
+        const SegRows& g = segs[s];
+        copy_row(g.out, g.in, g.ncols, perm[r] - base, r - base);
+      }
     }
   }
 }
@@ -805,13 +813,26 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in, int key_b
   const int kb = known ? key_bits : 32;
   uint64_t* drs = upload(ctx, rstart);
   const uint32_t** dc0 = upload(ctx, col0);
+  // each chunk's first segment
+  const uint64_t nchunks = div_up(N, static_cast<uint64_t>(kChunkRows));
+  std::vector<uint32_t> chunk_seg(nchunks);
+  {
+    uint32_t sg = 0;
+    for (uint64_t c = 0; c < nchunks; ++c) {
+      const uint64_t r = c * kChunkRows;
+      while (rstart[sg + 1] <= r) ++sg;
+      chunk_seg[c] = sg;
+    }
+  }
+  uint32_t* dcs = upload(ctx, chunk_seg);
+  const unsigned cgrid = static_cast<unsigned>(std::min<uint64_t>(nchunks, static_cast<uint64_t>(ctx.num_sms) * 8));
   uint64_t* keys = ctx.alloc<uint64_t>(N);
   uint64_t* keys_alt = ctx.alloc<uint64_t>(N);
   uint32_t* vals = ctx.alloc<uint32_t>(N);
   uint32_t* vals_alt = ctx.alloc<uint32_t>(N);
   ctx.launch("sort_keys", 12.0 * N, [&] {
-    composite_keys_kernel<<<grid_cap(ctx, N, 4), kBlock, 0, ctx.stream>>>(dc0, drs, S, static_cast<uint32_t>(kb),
-                                                                          keys);
+    composite_keys_kernel<<<cgrid, kBlock, 0, ctx.stream>>>(dc0, drs, S, dcs, nchunks, static_cast<uint32_t>(kb),
+                                                            keys);
   });
   VG_CUDA(cudaGetLastError());
   // with the key width known the passes are fixed and nothing waits on the device
@@ -832,7 +853,7 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in, int key_b
   });
   SegRows* dsg = upload(ctx, segs);
   ctx.launch("gather", bytes, [&] {
-    seg_gather_kernel<<<grid_cap(ctx, N, 4), kBlock, 0, ctx.stream>>>(dsg, drs, S, perm);
+    seg_gather_kernel<<<cgrid, kBlock, 0, ctx.stream>>>(dsg, drs, S, dcs, nchunks, perm);
   });
   VG_CUDA(cudaGetLastError());
   parallel_for(S, [&](size_t s) {
@@ -845,6 +866,7 @@ void batched_sort_by_first(Ctx& ctx, const std::vector<Rel*>& rels_in, int key_b
   ctx.free(vals_alt);
   ctx.free(dsg);
   ctx.free(drs);
+  ctx.free(dcs);
   ctx.free(const_cast<uint32_t**>(dc0));
 }
 

@@ -280,22 +280,34 @@ __device__ __forceinline__ void copy_join_row(uint32_t* const* out, const uint32
 
 // compact_store: the kept rows of a tile (bit i of `keep` for row r0 + i,
 // the thread's first kept row at tile position e, `tot` kept in the tile,
-// the tile's first at output row g) written column by column through shared
-// memory (s_buf: BLOCK * 8 words), so that every store of a column is
-// coalesced.  Every thread of the block calls it.
+// the tile's first at output row g) written two columns at a time through
+// shared memory (s_buf: 2 * BLOCK * 8 words), so that every store of a column
+// is coalesced and a pair of columns costs one pair of barriers.  Every
+// thread of the block calls it.
 template <int BLOCK>
 __device__ __forceinline__ void compact_store(const uint32_t* const* in, uint32_t* const* out, uint32_t ncols,
                                               uint64_t n, uint64_t r0, uint32_t keep, uint32_t e, uint32_t tot,
                                               uint64_t g, uint32_t* s_buf) {
-  for (uint32_t c = 0; c < ncols; ++c) {
-    const uint32_t* col = in[c];
+  constexpr uint32_t kTile = BLOCK * 8;
+  for (uint32_t c = 0; c < ncols; c += 2) {
+    const bool two = c + 1 < ncols;
+    const uint32_t* col_a = in[c];
+    const uint32_t* col_b = two ? in[c + 1] : nullptr;
     uint32_t o = e;
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-      if ((keep >> i & 1u) && r0 + i < n) s_buf[o++] = col[r0 + i];
+      if ((keep >> i & 1u) && r0 + i < n) {
+        s_buf[o] = __ldg(col_a + r0 + i);
+        if (two) s_buf[kTile + o] = __ldg(col_b + r0 + i);
+        ++o;
+      }
     __syncthreads();
-    uint32_t* dst = out[c] + g;
-    for (uint32_t k = threadIdx.x; k < tot; k += BLOCK) dst[k] = s_buf[k];
+    uint32_t* dst_a = out[c] + g;
+    for (uint32_t k = threadIdx.x; k < tot; k += BLOCK) dst_a[k] = s_buf[k];
+    if (two) {
+      uint32_t* dst_b = out[c + 1] + g;
+      for (uint32_t k = threadIdx.x; k < tot; k += BLOCK) dst_b[k] = s_buf[kTile + k];
+    }
     __syncthreads();
   }
 }

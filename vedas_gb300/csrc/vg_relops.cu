@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kBlock) unique_kernel(UniqueArgs a) {
   __shared__ uint32_t s_scan[kBlock / 32 + 1];
   __shared__ uint64_t s_b;
   __shared__ uint32_t s_tile;
-  __shared__ uint32_t s_keep[kTileRows];
+  __shared__ uint32_t s_keep[2 * kTileRows];   // compact_store: two columns at a time
   if (threadIdx.x == 0) s_tile = atomicAdd(a.ticket, 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
