@@ -1040,18 +1040,7 @@ void run_batch(Ctx& ctx, vedas::VedasStorage* storage, const char* const* texts,
   // engine got the same mix of long and short job lists, was measured slower
   // on the 4096-query batch: 27.3 ms against 22.7 ms per batch, since every
   // engine then ran the longest chain of waves, each wave with few queries.)
-  // VG_BATCH_DEAL=hash deals by a multiplicative hash of the batch index
-  // instead, so a workload whose queries cycle through a few shapes does not
-  // give each engine a fixed subset of them.
-  const bool hash_deal = [] {
-    const char* d = std::getenv("VG_BATCH_DEAL");
-    return d && std::strcmp(d, "hash") == 0;
-  }();
-  for (size_t i = 0; i < pq.size(); ++i) {
-    const size_t e = hash_deal ? static_cast<size_t>((static_cast<uint64_t>(i) * 0x9E3779B97F4A7C15ull) >> 40) % ne
-                               : i % ne;
-    eng[e]->add(&pq[i]);
-  }
+  for (size_t i = 0; i < pq.size(); ++i) eng[i % ne]->add(&pq[i]);
   std::vector<std::exception_ptr> err(ne);
   auto drive = [&](size_t e) {
     UseEnginePool use(e);
