@@ -923,13 +923,6 @@ void batched_join_count(Ctx& ctx, const std::vector<const Rel*>& l, const std::v
     });
     VG_CUDA(cudaGetLastError());
   }
-  // all unified storage as shared memory: four blocks' windows per SM
-  static const bool carveout_set = [] {
-    VG_CUDA(cudaFuncSetAttribute(bjoin_count_scan_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared));
-    return true;
-  }();
-  (void)carveout_set;
   ctx.launch("join_count_scan", cbytes + 12.0 * rows, [&] {
     bjoin_count_scan_kernel<<<static_cast<unsigned>(small_blocks + T), kJcBlock, 0, ctx.stream>>>(
         djs, dbs, dtj, dwin, dsm, nsmall, small_blocks, jb.lo, jb.offs, status, ticket, totals, ctx.d_err);

@@ -175,17 +175,6 @@ __global__ void __launch_bounds__(kJcBlock, 4) join_count_tiled_kernel(const uin
   if (threadIdx.x == 0) jc_drain_window(sm, err);
 }
 
-// All unified storage as shared memory for the tiled count: four blocks'
-// windows per SM (once per process).
-void count_tiled_carveout() {
-  static const bool set = [] {
-    VG_CUDA(cudaFuncSetAttribute(join_count_tiled_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared));
-    return true;
-  }();
-  (void)set;
-}
-
 // Exclusive scan of uint32 counts into uint64 offsets (+ total).
 __global__ void __launch_bounds__(kBlock) scan_counts_kernel(const uint32_t* __restrict__ in,
                                                              uint64_t* __restrict__ out, uint64_t n,
@@ -385,7 +374,6 @@ void join(Ctx& ctx, const Rel& l, const Rel& r, bool two_keys, Rel& out) {
       join_count_kernel<true><<<cgrid, kBlock, 0, ctx.stream>>>(kl, l.nrows, kr, r.nrows, lo.get(), cnt.get());
     });
   } else {
-    count_tiled_carveout();
     ctx.launch("join_count", cbytes, [&] {
       join_count_tiled_kernel<<<static_cast<unsigned>(div_up(l.nrows, kJcTile)), kJcBlock, 0, ctx.stream>>>(
           l.cols[0], l.nrows, r.cols[0], r.nrows, lo.get(), cnt.get(), ctx.d_err);
@@ -438,7 +426,6 @@ uint64_t join_into(cudaStream_t stream, int num_sms, const Rel& l, const Rel& r,
   (void)num_sms;
   if (l.nrows == 0 || r.nrows == 0) return 0;
   const uint32_t ncols = l.ncols + r.ncols - 1;
-  count_tiled_carveout();
   join_count_tiled_kernel<<<static_cast<unsigned>(div_up(l.nrows, kJcTile)), kJcBlock, 0, stream>>>(
       l.cols[0], l.nrows, r.cols[0], r.nrows, lo, cnt, err);
   VG_CUDA(cudaGetLastError());
