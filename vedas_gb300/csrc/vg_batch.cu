@@ -354,18 +354,34 @@ __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
   for (int k = 0; k < kJcKeys; ++k) sum += cnt[k];
   uint64_t tot;
   const uint64_t e = block_excl_scan64<kJcBlock>(sum, tot, s_scan);   // every thread is past its search
+  const uint32_t tid = threadIdx.x;
+  const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
+  const uint32_t tile_n = static_cast<uint32_t>(g.nl - i0 < kJcTile ? g.nl - i0 : kJcTile);
+  // a bulk copy that gave up may still land in the window: no staging there
+  const bool stage = !(sm.staged == 2 && sm.failed);
+  if (stage) {
+    // lower bounds and tile-relative offsets staged in the window while warp 0
+    // looks back; the tile's prefix is added when they are stored
+    uint32_t* s_lo = jc_stage_lo(sm);
+    uint64_t* s_off = jc_stage_off(sm);
+    uint64_t run = e;
+#pragma unroll
+    for (int k = 0; k < kJcKeys; ++k) {
+      const uint32_t q = tid * kJcKeys + k;
+      s_lo[q + q / 32] = lov[k];
+      s_off[q + q / 16] = run;
+      run += cnt[k];
+    }
+  }
   if (threadIdx.x < 32) {
     const uint64_t p = warp_lookback_seg(status, tile, bstart[j], tot, err);
     if (threadIdx.x == 0) s_b = p;
   }
   __syncthreads();
-  if (tile == bstart[j + 1] - 1 && threadIdx.x == 0) totals[j] = s_b + tot;
-  uint64_t run = s_b + e;
-  const uint32_t tid = threadIdx.x;
-  const uint64_t first = i0 + static_cast<uint64_t>(tid) * kJcKeys;
-  const uint32_t tile_n = static_cast<uint32_t>(g.nl - i0 < kJcTile ? g.nl - i0 : kJcTile);
-  if (sm.staged == 2 && sm.failed) {
-    // a bulk copy that gave up may still land in the window: no staging there
+  const uint64_t base = s_b;
+  if (tile == bstart[j + 1] - 1 && tid == 0) totals[j] = base + tot;
+  if (!stage) {
+    uint64_t run = base + e;
 #pragma unroll
     for (int k = 0; k < kJcKeys; ++k) {
       if (first + k < g.nl) {
@@ -377,21 +393,13 @@ __global__ void __launch_bounds__(kJcBlock, 4) bjoin_count_scan_kernel(
     if (tid == 0) jc_drain_window(sm, err);
     return;
   }
-  uint32_t* s_lo = jc_stage_lo(sm);
-  uint64_t* s_off = jc_stage_off(sm);
-#pragma unroll
-  for (int k = 0; k < kJcKeys; ++k) {
-    const uint32_t q = tid * kJcKeys + k;
-    s_lo[q + q / 32] = lov[k];
-    s_off[q + q / 16] = run;
-    run += cnt[k];
-  }
-  __syncthreads();
+  const uint32_t* s_lo = jc_stage_lo(sm);
+  const uint64_t* s_off = jc_stage_off(sm);
   uint32_t* lo_t = lo + g.row0 + i0;
   uint64_t* off_t = offs + g.row0 + i0;
   for (uint32_t q = tid; q < tile_n; q += kJcBlock) {
     lo_t[q] = s_lo[q + q / 32];
-    off_t[q] = s_off[q + q / 16];
+    off_t[q] = base + s_off[q + q / 16];
   }
 }
 
