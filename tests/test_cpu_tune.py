@@ -23,7 +23,7 @@ def test_select_smallest_median_with_margin_and_ties():
 
 def test_descent_is_deterministic_from_a_fake_timing_table():
     # a fake device: a trial's time is a fixed function of the parameters
-    cost = {"sort_items": {16: 3.0, 8: 2.0}, "sort_lookback": {1: 1.0, 4: 0.5},
+    cost = {"sort_items": {16: 3.0, 12: 2.5, 8: 2.0}, "sort_lookback": {1: 1.0, 4: 0.5},
             "join_small_rows": {256: 1.0, 64: 1.5, 0: 4.0},
             "write_small_rows": {1024: 2.0, 256: 2.0, 4096: 1.0, 0: 3.0},
             "unique_small_rows": {256: 1.0, 0: 1.01}, "write_blocks_per_sm": {5: 2.0, 8: 2.0, 4: 1.0, 2: 1.0}}

@@ -453,7 +453,7 @@ const TuneKnob* find_knob(const char* name) {
 vg_status vg_tune_set(vg_ctx* ctx, const char* name, int64_t value) {
   const TuneKnob* k = find_knob(name);
   if (!ctx || !k || value < static_cast<int64_t>(k->lo) || value > static_cast<int64_t>(k->hi)) return VG_ERR_INVALID;
-  if (k->field == &vg::TuneParams::sort_items && value != 8 && value != 16) return VG_ERR_INVALID;
+  if (k->field == &vg::TuneParams::sort_items && value != 8 && value != 12 && value != 16) return VG_ERR_INVALID;
   if (k->field == &vg::TuneParams::sort_lookback && value != 1 && value != 4) return VG_ERR_INVALID;
   ctx->c.tune.*(k->field) = static_cast<uint32_t>(value);
   return VG_OK;

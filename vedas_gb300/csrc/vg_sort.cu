@@ -66,7 +66,7 @@ __global__ void iota_kernel(uint32_t* out, uint64_t n) {
 }
 
 template <typename K, bool HAS_V, bool IOTA, int kItems, int kLook>
-__global__ void __launch_bounds__(kBlock, kItems <= 8 ? 4 : 3) onesweep_kernel(
+__global__ void __launch_bounds__(kBlock, kItems <= 12 ? 4 : 3) onesweep_kernel(
     const K* __restrict__ kin, K* __restrict__ kout, const uint32_t* __restrict__ vin,
     uint32_t* __restrict__ vout, uint64_t n, uint32_t shift, const uint64_t* __restrict__ bucket_base,
     uint64_t* status, uint32_t* ticket, DeviceErrors* err) {
@@ -207,7 +207,10 @@ template <typename K, bool HAS_V, bool IOTA>
 void launch_pass(Ctx& ctx, int items, const K* kin, K* kout, const uint32_t* vin, uint32_t* vout, uint64_t n,
                  uint32_t shift, const uint64_t* bases, uint64_t* status, uint32_t* ticket) {
   const bool look4 = ctx.tune.sort_lookback == 4;
-  if (items == 8) {
+  if (items == 12) {
+    if (look4) launch_pass_items<K, HAS_V, IOTA, 12, 4>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
+    else launch_pass_items<K, HAS_V, IOTA, 12, 1>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
+  } else if (items == 8) {
     if (look4) launch_pass_items<K, HAS_V, IOTA, 8, 4>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
     else launch_pass_items<K, HAS_V, IOTA, 8, 1>(ctx, kin, kout, vin, vout, n, shift, bases, status, ticket);
   } else {
@@ -277,7 +280,8 @@ bool radix_sort_impl(Ctx& ctx, K* keys, K* keys_alt, uint32_t* vals, uint32_t* v
     VG_CUDA(cudaGetLastError());
     for (int p = 0; p < passes; ++p) todo.push_back(p);
   }
-  const int items = ctx.tune.sort_items == 8 ? 8 : kItemsMax;
+  const int items = (ctx.tune.sort_items == 8 || ctx.tune.sort_items == 12) ? static_cast<int>(ctx.tune.sort_items)
+                                                                            : kItemsMax;
   const uint64_t tiles = div_up(n, static_cast<uint64_t>(kBlock) * items);
   Scratch<uint64_t> status(ctx, tiles * kRadix);
   Scratch<uint32_t> ticket(ctx, todo.size());
