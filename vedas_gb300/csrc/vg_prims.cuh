@@ -279,36 +279,47 @@ __device__ __forceinline__ void copy_join_row(uint32_t* const* out, const uint32
 }
 
 // compact_store: the kept rows of a tile (bit i of `keep` for row r0 + i,
-// the thread's first kept row at tile position e, `tot` kept in the tile,
-// the tile's first at output row g) written two columns at a time through
-// shared memory (s_buf: 2 * BLOCK * 8 words), so that every store of a column
-// is coalesced and a pair of columns costs one pair of barriers.  Every
-// thread of the block calls it.
+// the thread's first kept row at tile position e, the tile's first at output
+// row g) written by each warp on its own: a warp's kept rows are one
+// contiguous run of the output, so the warp stages two columns at a time in
+// its own slice of shared memory (s_buf: 2 * BLOCK * 8 words, 512 words per
+// warp) and stores the run with coalesced stores, between warp barriers only.
+// Every thread of the block calls it (no block barrier inside).
 template <int BLOCK>
 __device__ __forceinline__ void compact_store(const uint32_t* const* in, uint32_t* const* out, uint32_t ncols,
                                               uint64_t n, uint64_t r0, uint32_t keep, uint32_t e, uint32_t tot,
                                               uint64_t g, uint32_t* s_buf) {
-  constexpr uint32_t kTile = BLOCK * 8;
+  (void)tot;
+  constexpr uint32_t kSlice = 32 * 8;   // one column of a warp's rows
+  const uint32_t lane = lane_id();
+  uint32_t mine = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    if ((keep >> i & 1u) && r0 + i < n) ++mine;
+  const uint32_t w0 = __shfl_sync(0xffffffffu, e, 0);                 // the warp's first kept row in the tile
+  const uint32_t wtot = __shfl_sync(0xffffffffu, e + mine, 31) - w0;  // the warp's kept rows
+  uint32_t* sw = s_buf + (threadIdx.x >> 5) * 2 * kSlice;
+  const uint64_t dst0 = g + w0;
   for (uint32_t c = 0; c < ncols; c += 2) {
     const bool two = c + 1 < ncols;
     const uint32_t* col_a = in[c];
     const uint32_t* col_b = two ? in[c + 1] : nullptr;
-    uint32_t o = e;
+    uint32_t o = e - w0;
 #pragma unroll
     for (int i = 0; i < 8; ++i)
       if ((keep >> i & 1u) && r0 + i < n) {
-        s_buf[o] = __ldg(col_a + r0 + i);
-        if (two) s_buf[kTile + o] = __ldg(col_b + r0 + i);
+        sw[o] = __ldg(col_a + r0 + i);
+        if (two) sw[kSlice + o] = __ldg(col_b + r0 + i);
         ++o;
       }
-    __syncthreads();
-    uint32_t* dst_a = out[c] + g;
-    for (uint32_t k = threadIdx.x; k < tot; k += BLOCK) dst_a[k] = s_buf[k];
+    __syncwarp();
+    uint32_t* dst_a = out[c] + dst0;
+    for (uint32_t k = lane; k < wtot; k += 32) dst_a[k] = sw[k];
     if (two) {
-      uint32_t* dst_b = out[c + 1] + g;
-      for (uint32_t k = threadIdx.x; k < tot; k += BLOCK) dst_b[k] = s_buf[kTile + k];
+      uint32_t* dst_b = out[c + 1] + dst0;
+      for (uint32_t k = lane; k < wtot; k += 32) dst_b[k] = sw[kSlice + k];
     }
-    __syncthreads();
+    __syncwarp();
   }
 }
 
