@@ -1,6 +1,7 @@
 // Batched relation kernels.  Work from many queries is laid out as segments;
-// a kernel maps its block/tile/row index to a segment by an upper-bound
-// search over a per-segment prefix array in device memory.
+// a kernel maps its tile or chunk to its segments through a table made on the
+// host (the tile's first segment), and a row to its segment by a search
+// between the tile's first and last segments only.
 #include "vg_batch.h"
 
 #include <algorithm>
@@ -17,11 +18,6 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kRows = 8;
 constexpr int kTileRows = kBlock * kRows;
-
-// Segment s of unit u: the last s with start[s] <= u (start has S+1 entries).
-__device__ __forceinline__ uint32_t seg_of(const uint64_t* start, uint32_t S, uint64_t u) {
-  return static_cast<uint32_t>(upper_bound_dev(start, 0, S + 1, u) - 1);
-}
 
 template <typename T>
 T* upload(Ctx& ctx, const std::vector<T>& v) {
@@ -43,21 +39,17 @@ constexpr uint64_t kCopyTile = static_cast<uint64_t>(kBlock) * kCopyPer;
 
 // Copies every piece; destination chunks are 16-byte aligned (head and tail
 // elements are copied by the piece's first chunk).  Blocks take tiles of
-// kCopyTile consecutive chunks; the pieces a tile covers are found once per
-// tile, so a thread's piece lookup is a search over those few pieces only.
+// kCopyTile consecutive chunks; a tile's first piece comes from a table made
+// on the host and the next tile's bounds its last, so a thread's piece lookup
+// is a search over those few pieces only (no global search, no barrier).
 __global__ void __launch_bounds__(kBlock) bcopy_kernel(const CopyPiece* __restrict__ p,
-                                                       const uint64_t* __restrict__ cstart, uint32_t P) {
-  __shared__ uint32_t s_k[2];
+                                                       const uint64_t* __restrict__ cstart, uint32_t P,
+                                                       const uint32_t* __restrict__ tile_piece, uint64_t ntiles) {
   const uint64_t total = cstart[P];
-  const uint64_t ntiles = (total + kCopyTile - 1) / kCopyTile;
   for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const uint64_t q0 = t * kCopyTile;
     const uint64_t q1 = (q0 + kCopyTile < total) ? q0 + kCopyTile : total;
-    if (threadIdx.x == 0) s_k[0] = seg_of(cstart, P, q0);
-    if (threadIdx.x == 32) s_k[1] = seg_of(cstart, P, q1 - 1);
-    __syncthreads();
-    const uint32_t k0 = s_k[0], k1 = s_k[1];
-    __syncthreads();
+    const uint32_t k0 = tile_piece[t], k1 = t + 1 < ntiles ? tile_piece[t + 1] : P - 1;
 #pragma unroll
     for (int i = 0; i < kCopyPer; ++i) {
       const uint64_t q = q0 + static_cast<uint64_t>(i) * kBlock + threadIdx.x;
@@ -732,15 +724,28 @@ void batched_copy(Ctx& ctx, const std::vector<CopyPiece>& pieces) {
     bytes += 8.0 * pc.len;
   }
   if (p.empty()) return;
+  const uint32_t P = static_cast<uint32_t>(p.size());
+  // each tile's first piece
+  const uint64_t ntiles = div_up(cstart.back(), kCopyTile);
+  std::vector<uint32_t> tile_piece(ntiles);
+  {
+    uint32_t k = 0;
+    for (uint64_t t = 0; t < ntiles; ++t) {
+      const uint64_t q = t * kCopyTile;
+      while (cstart[k + 1] <= q) ++k;
+      tile_piece[t] = k;
+    }
+  }
   CopyPiece* dp = upload(ctx, p);
   uint64_t* dc = upload(ctx, cstart);
-  const uint32_t P = static_cast<uint32_t>(p.size());
+  uint32_t* dtp = upload(ctx, tile_piece);
   ctx.launch("select_copy", bytes, [&] {
-    bcopy_kernel<<<grid_cap(ctx, cstart.back(), kCopyPer), kBlock, 0, ctx.stream>>>(dp, dc, P);
+    bcopy_kernel<<<grid_cap(ctx, cstart.back(), kCopyPer), kBlock, 0, ctx.stream>>>(dp, dc, P, dtp, ntiles);
   });
   VG_CUDA(cudaGetLastError());
   ctx.free(dp);
   ctx.free(dc);
+  ctx.free(dtp);
 }
 
 void batched_unique_enqueue(Ctx& ctx, const std::vector<SegRows>& segs, uint64_t* counts_host) {
