@@ -450,19 +450,6 @@ void Ctx::release_dl_stream() {
     cudaStreamDestroy(dl_stream_);
   }
   dl_stream_ = nullptr;
-  for (cudaStream_t& s : copy_lanes_) {
-    if (s) {
-      cudaStreamSynchronize(s);
-      cudaStreamDestroy(s);
-    }
-    s = nullptr;
-  }
-}
-
-cudaStream_t Ctx::copy_lane(int i) {
-  std::lock_guard<std::recursive_mutex> lk(host_mu);
-  if (!copy_lanes_[i]) VG_CUDA(cudaStreamCreateWithFlags(&copy_lanes_[i], cudaStreamNonBlocking));
-  return copy_lanes_[i];
 }
 
 cudaEvent_t Ctx::take_event() {

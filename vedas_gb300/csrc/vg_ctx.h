@@ -263,11 +263,6 @@ struct Ctx {
   cudaStream_t dl_stream();
   void release_dl_stream();
   cudaStream_t dl_stream_ = nullptr;
-  // Streams that split one large device-to-host copy into parallel pieces
-  // (created on first use, released with the download stream).
-  static constexpr int kCopyLanes = 4;
-  cudaStream_t copy_lane(int i);
-  cudaStream_t copy_lanes_[kCopyLanes] = {};
 
   // Copies `bytes` from host memory to device memory `dst` on the stream,
   // through a page-locked ring, so the copy never waits for earlier work

@@ -560,33 +560,8 @@ void unique_in_place(Ctx& ctx, Rel& r) {
 }
 
 void download(Ctx& ctx, const uint32_t* dev, uint64_t n, uint32_t* host) {
-  constexpr uint64_t kSplit = uint64_t{64} << 20;   // bytes from which a copy is split over the copy lanes
-  const uint64_t bytes = n * sizeof(uint32_t);
-  if (bytes < kSplit) {
-    if (n) VG_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx.stream));
-    ctx.sync();
-    return;
-  }
-  // a large column leaves in Ctx::kCopyLanes pieces on streams of their own,
-  // each ordered after the work already on the context's stream, so that
-  // several copy engines move it at once
-  cudaEvent_t ready = ctx.take_event();
-  VG_CUDA(cudaEventRecord(ready, ctx.stream));
-  const uint64_t piece = (n + Ctx::kCopyLanes - 1) / Ctx::kCopyLanes;
-  for (int i = 0; i < Ctx::kCopyLanes; ++i) {
-    const uint64_t b = static_cast<uint64_t>(i) * piece;
-    if (b >= n) break;
-    const uint64_t m = (b + piece < n ? piece : n - b);
-    cudaStream_t s = ctx.copy_lane(i);
-    VG_CUDA(cudaStreamWaitEvent(s, ready, 0));
-    VG_CUDA(cudaMemcpyAsync(host + b, dev + b, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  }
-  for (int i = 0; i < Ctx::kCopyLanes; ++i)
-    if (ctx.copy_lanes_[i]) VG_CUDA(cudaStreamSynchronize(ctx.copy_lanes_[i]));
-  {
-    std::lock_guard<std::recursive_mutex> lk(ctx.host_mu);
-    ctx.event_pool.push_back(ready);
-  }
+  if (n) VG_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
+  ctx.sync();
 }
 
 }  // namespace vg
