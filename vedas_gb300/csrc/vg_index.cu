@@ -105,11 +105,22 @@ __global__ void __launch_bounds__(kBlock) unpack_rle_kernel(UnpackArgs a) {
       if (r == 0 || (key[i] >> a.sh1) != (pv >> a.sh1)) f2 |= 1u << i;
     }
   }
-  uint32_t t1, t2;
-  const uint32_t e1 = block_excl_scan<kBlock>(__popc(f1), t1, s_scan);
-  const uint32_t e2 = block_excl_scan<kBlock>(__popc(f2), t2, s_scan);
-  const uint64_t g1 = a.l1_vals ? block_lookback(a.status1, tile, t1, a.err, &s_b) : 0;
-  const uint64_t g2 = a.l2_vals ? block_lookback(a.status2, tile, t2, a.err, &s_b) : 0;
+  // both levels' run counts in one scan (a tile has at most kTileRows < 2^16
+  // of each) and, when the row count allows, one look-back over both
+  // (level 1 above bit 31, level 2 below)
+  uint32_t tt;
+  const uint32_t ee = block_excl_scan<kBlock>((__popc(f1) << 16) | __popc(f2), tt, s_scan);
+  const uint32_t e1 = ee >> 16, e2 = ee & 0xFFFFu, t1 = tt >> 16, t2 = tt & 0xFFFFu;
+  uint64_t g1 = 0, g2 = 0;
+  if (a.l1_vals && a.l2_vals && a.n < (1ull << 31)) {
+    const uint64_t g = block_lookback(a.status1, tile, (static_cast<uint64_t>(t1) << 31) | t2, a.err, &s_b);
+    g1 = g >> 31;
+    g2 = g & ((1ull << 31) - 1);
+  } else {
+    g1 = a.l1_vals ? block_lookback(a.status1, tile, t1, a.err, &s_b) : 0;
+    g2 = a.l2_vals ? block_lookback(a.status2, tile, t2, a.err, &s_b) : 0;
+  }
+  static_assert(kTileRows < (1 << 16), "a tile's run counts fit 16 bits each");
   if (tile == a.tiles - 1 && threadIdx.x == 0) {
     a.counts[0] = g1 + t1;
     a.counts[1] = g2 + t2;
