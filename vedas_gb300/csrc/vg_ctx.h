@@ -188,7 +188,7 @@ struct StreamRef {
 // them from timed trials).  Each choice changes only speed, never results.
 struct TuneParams {
   uint32_t sort_items = 16;          // onesweep keys per thread: 8, 12 or 16
-  uint32_t sort_lookback = 1;        // onesweep look-back words loaded at once: 1 or 4
+  uint32_t sort_lookback = 4;        // onesweep look-back words loaded at once: 1 or 4
   uint32_t join_small_rows = 256;    // joins with at most this many left rows: one warp each (0..256)
   uint32_t write_small_rows = 1024;  // outputs with at most this many rows: one warp each (0..4096)
   uint32_t unique_small_rows = 256;  // final compactions with at most this many rows: one warp each (0..256)

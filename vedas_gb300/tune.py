@@ -27,7 +27,7 @@ import time
 # knob -> (candidate values, value of a fresh context)
 KNOBS = {
     "sort_items": ([16, 12, 8], 16),
-    "sort_lookback": ([1, 4], 1),
+    "sort_lookback": ([4, 1], 4),
     "join_small_rows": ([256, 64, 0], 256),
     "write_small_rows": ([1024, 256, 4096, 0], 1024),
     "unique_small_rows": ([256, 0], 256),
