@@ -142,13 +142,17 @@ def test_batch_join_placement_regions(ctx, monkeypatch, region_mb, streams):
 
 
 @pytest.mark.parametrize("params", [
-    {"sort_items": 8, "join_small_rows": 0, "write_small_rows": 0, "unique_small_rows": 0, "write_blocks_per_sm": 1},
-    {"sort_items": 16, "join_small_rows": 64, "write_small_rows": 4096, "unique_small_rows": 256,
-     "write_blocks_per_sm": 2},
+    {"sort_items": 8, "sort_lookback": 1, "join_small_rows": 0, "write_small_rows": 0, "unique_small_rows": 0,
+     "write_blocks_per_sm": 1},
+    {"sort_items": 12, "sort_lookback": 4, "join_small_rows": 256, "write_small_rows": 1024,
+     "unique_small_rows": 0, "write_blocks_per_sm": 5},
+    {"sort_items": 16, "sort_lookback": 1, "join_small_rows": 64, "write_small_rows": 4096,
+     "unique_small_rows": 256, "write_blocks_per_sm": 2},
 ])
 def test_launch_parameters_change_speed_only(ctx, params):
-    """Every autotuner choice (sort tile, warp-per-join thresholds, write
-    grid) gives the oracle's results, logs included."""
+    """Every autotuner choice (sort tile and look-back width, warp-per-join
+    thresholds, write grid) gives the oracle's results, logs included, and the
+    index build with the same sort choices gives the oracle's arrays."""
     import vedas_gb300 as vg
     from vedas_gb300 import tune
     g = workloads.graph_chain(n=300_000, n_entities=30_000, seed=31)
