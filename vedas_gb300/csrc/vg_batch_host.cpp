@@ -564,8 +564,7 @@ void WaveEngine::stage_a(std::vector<PlannedQuery*>& completed) {
     prof.device_s += since(t0);
   }
   // everything enqueued on the engine's stream so far is done (waited for
-  // now, or in stage B, which records ev_b_ whenever it enqueues work):
-  // held-back frees are safe
+  // now, or in stage B with nothing enqueued since): held-back frees are safe
   if (own_stream_) ctx_.flush(defer_);
   if (tracing) tr.t_wait = since(trace_origin);
   {
@@ -758,7 +757,6 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   if (own_stream_) ctx_.flush(defer_);
   if (tracing) tr.t_wait = since(trace_origin);
   const uint64_t* ha = h_a_.data();
-  bool enqueued_b = false;   // device work enqueued by this stage (ev_b_ must cover it)
 
   // staged columns of the wave in flight
   {
@@ -803,8 +801,7 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
     if (host_) {
       std::vector<BatchQuery*> outs;
       for (PlannedQuery* q : final_) outs.push_back(q->out);
-      ThreadExecScope es(enqueue_exec());
-      enqueued_b = host_->add(outs);
+      host_->add(outs);   // on the download stream, after an event on the engine's
     }
     final_.clear();
     fin_seg_.clear();
@@ -906,12 +903,6 @@ void WaveEngine::stage_b(std::vector<PlannedQuery*>& completed) {
   } else {
     jsmall_.clear();
   }
-  // the result packing above was enqueued with its scratch held back: the
-  // next stage A waits for it before the held-back blocks are freed
-  if (enqueued_b && !b_pending_) {
-    VG_CUDA(cudaEventRecord(ev_b_, ctx_.stream));
-    b_pending_ = true;
-  }
   prof.device_s += since(t0);
   if (tracing) {
     tr.t_end = since(trace_origin);
@@ -944,7 +935,7 @@ void HostResults::retire_stages(bool all) {
       continue;
     }
     VG_CUDA(cudaStreamWaitEvent(ctx_.stream, p.done, 0));
-    ctx_.free(p.stage);
+    for (void* b : p.scratch) ctx_.free(b);
     cudaEventDestroy(p.done);
   }
   pending_.swap(keep);
@@ -965,26 +956,30 @@ bool HostResults::add(const std::vector<BatchQuery*>& qs) {
   }
   Chunk& ch = chunks_.back();
   uint32_t* host = reinterpret_cast<uint32_t*>(ch.p + ch.used);
-  uint32_t* stage = ctx_.alloc<uint32_t>(words);
   std::vector<CopyPiece> pieces;
   uint64_t off = 0;
   for (BatchQuery* q : qs)
     for (uint32_t c = 0; c < q->rel.ncols; ++c) {
-      pieces.push_back({q->rel.cols[c], stage + off, q->rel.nrows});
+      pieces.push_back({q->rel.cols[c], host + off, q->rel.nrows});
       q->host[c] = host + off;
       off += q->rel.nrows;
     }
-  batched_copy(ctx_, pieces);
-  cudaEvent_t packed, done;
-  VG_CUDA(cudaEventCreateWithFlags(&packed, cudaEventDisableTiming));
+  // the copy kernel runs on the download stream after the results are
+  // complete on the calling thread's stream; its scratch is freed once it is done
+  cudaEvent_t ready, done;
+  VG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
   VG_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
-  VG_CUDA(cudaEventRecord(packed, ctx_.stream));
+  VG_CUDA(cudaEventRecord(ready, ctx_.stream));
   cudaStream_t dl = ctx_.dl_stream();
-  VG_CUDA(cudaStreamWaitEvent(dl, packed, 0));
-  VG_CUDA(cudaMemcpyAsync(host, stage, bytes, cudaMemcpyDeviceToHost, dl));
-  VG_CUDA(cudaEventRecord(done, dl));
-  cudaEventDestroy(packed);
-  pending_.push_back({stage, done});
+  VG_CUDA(cudaStreamWaitEvent(dl, ready, 0));
+  DeferredFrees scratch;
+  {
+    ThreadExecScope sc(ThreadExec{dl, &scratch});
+    batched_copy(ctx_, pieces);
+    VG_CUDA(cudaEventRecord(done, dl));
+  }
+  cudaEventDestroy(ready);
+  pending_.push_back({std::move(scratch.blocks), done});
   ch.used += span;
   bytes_ += bytes;
   return true;

@@ -24,9 +24,10 @@ struct BatchQuery {
 };
 
 // Page-locked host copies of finished queries' results, made while the batch
-// runs: each time queries finish, one gather packs their columns on the
-// device and one copy on a second stream brings them to host memory, so the
-// transfers overlap the rest of the batch.  Chunks of page-locked memory come
+// runs: each time queries finish, one copy kernel on a second stream packs
+// their columns straight into page-locked host memory (which kernels address
+// directly under unified addressing), so the transfers overlap the rest of
+// the batch and need no device staging.  Chunks of page-locked memory come
 // from the context's pool and go back to it with the HostResults.
 class HostResults {
  public:
@@ -34,9 +35,9 @@ class HostResults {
   ~HostResults();
   HostResults(const HostResults&) = delete;
   HostResults& operator=(const HostResults&) = delete;
-  // Enqueues the copies of these queries' result columns on the calling
-  // thread's stream (scratch freed through the thread's held-back frees);
-  // false when there was nothing to copy.
+  // Enqueues the copies of these queries' result columns on the download
+  // stream, after the work already on the calling thread's stream; false
+  // when there was nothing to copy.
   bool add(const std::vector<BatchQuery*>& qs);
   // Waits for every copy.
   void finish();
@@ -48,7 +49,7 @@ class HostResults {
     size_t cap, used;
   };
   struct Pending {
-    uint32_t* stage;
+    std::vector<void*> scratch;   // device blocks of the copy, freed once it is done
     cudaEvent_t done;
   };
   Ctx& ctx_;
