@@ -668,17 +668,28 @@ __global__ void tile_join_fill_kernel(const uint64_t* __restrict__ ostart, uint3
     for (uint64_t t = ostart[j] + threadIdx.x; t < ostart[j + 1]; t += blockDim.x) tile_join[t] = j;
 }
 
-// Column 0 of small join outputs (2 < rows < kSmallC0Words) into stage slots
-// of kSmallC0Words words, for the joins whose slot is not negative (their
-// host-side completion scans it for empty intervals).
-__global__ void small_c0_kernel(const JoinOut* __restrict__ jo, uint32_t J, const int32_t* __restrict__ slot,
-                                uint32_t* __restrict__ stage) {
-  for (uint32_t j = blockIdx.x; j < J; j += gridDim.x) {
-    const int32_t s = slot[j];
+// After a placed write, one warp per join: lane 0 writes the output's first
+// and last key; when the join has a stage slot (its host-side completion
+// scans column 0 for empty intervals) and a small output (2 < rows <
+// kSmallC0Words), the warp copies that column 0 into the slot's
+// kSmallC0Words-word stage.
+__global__ void __launch_bounds__(kBlock) join_edges_kernel(const JoinOut* __restrict__ jo, uint32_t J,
+                                                            uint32_t* __restrict__ fl,
+                                                            const int32_t* __restrict__ slot,
+                                                            uint32_t* __restrict__ stage) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nw = static_cast<uint64_t>(gridDim.x) * (kBlock / 32);
+  for (uint64_t j = static_cast<uint64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5); j < J; j += nw) {
     const uint64_t t = jo[j].total;
-    if (s < 0 || t <= 2 || t >= kSmallC0Words) continue;
-    for (uint32_t i = threadIdx.x; i < t; i += blockDim.x)
-      stage[static_cast<uint64_t>(s) * kSmallC0Words + i] = jo[j].oc[0][i];
+    if (t == 0) continue;
+    const uint32_t* c0 = jo[j].oc[0];
+    if (lane == 0) {
+      fl[2 * j] = c0[0];
+      fl[2 * j + 1] = c0[t - 1];
+    }
+    const int32_t sl = slot ? slot[j] : -1;
+    if (sl < 0 || t <= 2 || t >= kSmallC0Words) continue;
+    for (uint32_t i = lane; i < t; i += 32) stage[static_cast<uint64_t>(sl) * kSmallC0Words + i] = c0[i];
   }
 }
 
@@ -1111,18 +1122,17 @@ void batched_join_place_write(Ctx& ctx, JoinBatch& jb, const Arena::Region* regi
                          ctx.stream>>>(djo, dos, dtj, drg, 0, dos + J, dsm, 0, dsm + J);
   });
   VG_CUDA(cudaGetLastError());
-  ctx.launch("join_first_last", 8.0 * J, [&] {
-    first_last_kernel<<<static_cast<unsigned>(div_up(J, 128)), 128, 0, ctx.stream>>>(djo, J, dfl);
-  });
-  VG_CUDA(cudaGetLastError());
-  if (nslots) {
-    ctx.launch("col0_stage", 8.0 * nslots * kSmallC0Words, [&] {
-      small_c0_kernel<<<jgrid, 128, 0, ctx.stream>>>(djo, J, dslot, dstage);
+  {
+    const uint64_t eblocks = std::min<uint64_t>(div_up(J, kBlock / 32), static_cast<uint64_t>(ctx.num_sms) * 8);
+    ctx.launch("join_first_last", 8.0 * J + 8.0 * nslots * kSmallC0Words, [&] {
+      join_edges_kernel<<<static_cast<unsigned>(eblocks), kBlock, 0, ctx.stream>>>(djo, J, dfl,
+                                                                                   nslots ? dslot : nullptr, dstage);
     });
     VG_CUDA(cudaGetLastError());
+  }
+  if (nslots)
     VG_CUDA(cudaMemcpyAsync(c0_host, dstage, static_cast<size_t>(nslots) * kSmallC0Words * sizeof(uint32_t),
                             cudaMemcpyDeviceToHost, ctx.stream));
-  }
   VG_CUDA(cudaMemcpyAsync(first_last_host, dfl, 2 * J * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx.stream));
   VG_CUDA(cudaMemcpyAsync(bump_host, d_bump, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx.stream));
   ctx.free(djo);
