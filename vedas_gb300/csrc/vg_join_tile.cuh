@@ -65,33 +65,6 @@ __device__ __forceinline__ uint32_t smem_gallop(const uint32_t* s, uint32_t from
   return smem_search<kUpper>(s, lo + 1, hi, key);
 }
 
-// The same answer as smem_search over [0, n) for a key whose answer is at or
-// before `from` (below(from) is false): gallops backwards from `from`
-// (steps 1, 2, 4, ...), then a binary search inside the last step.
-template <bool kUpper>
-__device__ __forceinline__ uint32_t smem_gallop_back(const uint32_t* s, uint32_t from, uint32_t key) {
-  uint32_t hi = from, step = 1;   // below(hi) is false
-  while (true) {
-    if (hi < step) return smem_search<kUpper>(s, 0, hi, key);
-    const uint32_t nx = hi - step;
-    if (smem_below<kUpper>(s, nx, key)) return smem_search<kUpper>(s, nx + 1, hi, key);
-    hi = nx;
-    step <<= 1;
-  }
-}
-
-// The answer of smem_search over [0, n) (n > 0), starting from the key's
-// position interpolated between the window's first and last keys and
-// galloping from there: on evenly spread keys a few steps instead of log2(n).
-template <bool kUpper>
-__device__ __forceinline__ uint32_t smem_interp_search(const uint32_t* s, uint32_t n, uint32_t key) {
-  const uint32_t a = s[0], b = s[n - 1];
-  uint32_t g = 0;
-  if (b > a && key > a)
-    g = key >= b ? n - 1 : static_cast<uint32_t>((static_cast<uint64_t>(key - a) * (n - 1)) / (b - a));
-  return smem_below<kUpper>(s, g, key) ? smem_gallop<kUpper>(s, g, n, key) : smem_gallop_back<kUpper>(s, g, key);
-}
-
 // First index in R[lo, hi) whose key is not below `key` (kUpper: above it),
 // found by one warp: each round 31 lanes probe evenly spaced keys and the
 // ballot of their comparisons narrows the range 32-fold, so a search over
@@ -347,7 +320,7 @@ __device__ __forceinline__ void jc_count_staged(const uint32_t* __restrict__ L, 
         lo = plo;
         hi = phi;
       } else {
-        lo = (j == 0) ? smem_interp_search<false>(win, n, k) : smem_gallop<false>(win, phi, n, k);
+        lo = (j == 0) ? smem_search<false>(win, 0, n, k) : smem_gallop<false>(win, phi, n, k);
         hi = smem_gallop<true>(win, lo, n, k);
       }
       lov[j] = static_cast<uint32_t>(w0 + lo);
